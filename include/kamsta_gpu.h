@@ -1,0 +1,188 @@
+/*
+ * kamsta_gpu.h -- C ABI of the GB300 minimum-spanning-forest solver.
+ *
+ * This is the drop-in boundary for KaMSTa's single-node MST hot path
+ * (Boruvka rounds and filter-Boruvka).  Every entry point takes plain
+ * pointers and sizes; no CUDA or C++ type appears in a signature, so the
+ * header binds from C, C++ (see kamsta_gpu.hpp), ctypes, cgo or JNI alike.
+ *
+ * Reference interfaces replaced (paths relative to the KaMSTa tree):
+ *   hybridMST::boruvka(std::vector<WEdge>, const AlgorithmConfig&)
+ *       include/algorithms/hybrid_boruvka.hpp:263-301
+ *   hybridMST::filter_boruvka(std::vector<WEdge>, const AlgorithmConfig&)
+ *       include/algorithms/hybrid_boruvka_edgefilter.hpp:420-462
+ *   hybridMST::AlgorithmConfig / LocalPreprocessing / Compression
+ *       include/algorithms/algorithm_configurations.hpp:6-34
+ *   hybridMST::WEdge (24-byte input edge)      include/definitions.hpp:66-84
+ *   hybridMST::WEdge_4_4 (12-byte packed edge) include/edge_types.hpp:135-146
+ *
+ * Input contract (same as the reference, utils.hpp:388-403 and
+ * benchmarks/mst.cpp:166-167): directed edge entries sorted by (src, dst),
+ * both directions of every undirected edge present, no self loops, ids < n.
+ * The solver reads each undirected edge from its src < dst copy, exactly like
+ * the reference's local path (local_contraction/utils.hpp:38-56).
+ *
+ * Output: the minimum spanning forest under the total order
+ * (w, min(u,v), max(u,v)) -- the order of the reference's own checker
+ * (base_case_mst_algos.hpp:91-112) -- one entry per forest edge, written as
+ * (min, max, w).  The order of the entries is deterministic; pass
+ * KAMSTA_FLAG_SORT_OUTPUT to get them sorted by (src, dst).
+ *
+ * Errors: every call returns a kamsta_status; kamsta_last_error() gives a
+ * thread-local message for the last failing call on the calling thread.
+ * The reference aborts the process instead (include/mpi/context.hpp:77-97).
+ */
+#ifndef KAMSTA_GPU_H
+#define KAMSTA_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+typedef int kamsta_status;
+#define KAMSTA_OK 0
+#define KAMSTA_E_INPUT 1       /* malformed input (ids >= n, unsorted, sizes) */
+#define KAMSTA_E_OOM 2         /* device or host allocation failed            */
+#define KAMSTA_E_CUDA 3        /* a CUDA runtime call failed                  */
+#define KAMSTA_E_NOCONVERGE 4  /* an iteration cap was hit (no hang, no trap) */
+#define KAMSTA_E_UNSUPPORTED 5 /* option not implemented on this build        */
+#define KAMSTA_E_BUDGET 6      /* request larger than the serving budget      */
+#define KAMSTA_E_NOTREADY 7    /* serving: result not finished yet            */
+
+/* ---- edge layouts -------------------------------------------------------- */
+/* Packed 12-byte weighted edge; same field order and width as WEdge_4_4
+ * (edge_types.hpp:135-146). */
+typedef struct kamsta_wedge {
+  uint32_t src;
+  uint32_t dst;
+  uint32_t w;
+} kamsta_wedge;
+
+/* The reference's std::vector<WEdge> element (definitions.hpp:66-84):
+ * 64-bit ids, 32-bit weight, 4 bytes tail padding (24 bytes). */
+typedef struct kamsta_wedge64 {
+  uint64_t src;
+  uint64_t dst;
+  uint32_t w;
+  uint32_t pad_;
+} kamsta_wedge64;
+
+/* ---- configuration ------------------------------------------------------- */
+/* LocalPreprocessing (algorithm_configurations.hpp:6-16). */
+#define KAMSTA_NO_PREPROCESSING 0
+#define KAMSTA_MODIFIED_BORUVKA 1
+#define KAMSTA_REDUCE_EDGES_THEN_BORUVKA 2
+/* Compression (algorithm_configurations.hpp:18-25). */
+#define KAMSTA_NO_COMPRESSION 0
+#define KAMSTA_SEVEN_BIT_DIFF_ENCODING 1
+
+/* flags */
+#define KAMSTA_FLAG_VALIDATE 0x1u     /* check sortedness / id range on device */
+#define KAMSTA_FLAG_SORT_OUTPUT 0x2u  /* sort forest edges by (src, dst)      */
+#define KAMSTA_FLAG_DEDUPE_NEVER 0x4u /* never remove parallel edges          */
+#define KAMSTA_FLAG_DEDUPE_ALWAYS 0x8u/* remove parallel edges every round   */
+#define KAMSTA_FLAG_TRACE 0x10u       /* record per-round (m_r, n_r) in stats  */
+
+/* AlgorithmConfig (algorithm_configurations.hpp:27-34) plus GPU knobs. */
+typedef struct kamsta_cfg {
+  int32_t local_preprocessing; /* KAMSTA_*_PREPROCESSING / _BORUVKA         */
+  int32_t compression;         /* KAMSTA_*_COMPRESSION                       */
+  uint64_t filter_threshold;   /* filter_boruvka base-case average degree    */
+  uint32_t flags;              /* KAMSTA_FLAG_*                              */
+  uint32_t dedupe_ratio;       /* auto dedupe when m_r > ratio * n_r (0=off) */
+  uint64_t seed;               /* pivot-sampling seed                        */
+  uint32_t block_threads;      /* 0 = autotuned / built-in default           */
+  uint32_t items_per_thread;   /* 0 = autotuned / built-in default           */
+} kamsta_cfg;
+
+#define KAMSTA_TRACE_MAX 128
+typedef struct kamsta_stats {
+  uint64_t num_mst_edges;  /* forest edges written                         */
+  uint64_t total_weight;   /* sum of forest edge weights                   */
+  uint32_t rounds;         /* Boruvka rounds over all levels               */
+  uint32_t levels;         /* filter recursion levels / weight classes     */
+  uint32_t dedupe_passes;  /* radix-sort dedupe passes run                 */
+  uint32_t gpu_launches;   /* kernels launched by the call                 */
+  double device_ms;        /* device time of the solve (CUDA events)       */
+  uint64_t alg_bytes;      /* algorithmic HBM bytes of the solve            */
+  uint32_t trace_len;      /* entries in trace_m / trace_n                  */
+  uint32_t pad_;
+  uint64_t trace_m[KAMSTA_TRACE_MAX]; /* live undirected edges per round   */
+  uint64_t trace_n[KAMSTA_TRACE_MAX]; /* live vertices per round           */
+} kamsta_stats;
+
+/* Fills cfg with AlgorithmConfig's defaults: NO_PREPROCESSING,
+ * NO_COMPRESSION, filter_threshold 4 (algorithm_configurations.hpp:31-33). */
+kamsta_status kamsta_cfg_default(kamsta_cfg* cfg);
+
+const char* kamsta_version(void);
+const char* kamsta_last_error(void);
+
+/* ---- context: device scratch pool + stream ----------------------------- */
+typedef struct kamsta_ctx kamsta_ctx;
+typedef void* kamsta_stream; /* a cudaStream_t; NULL = the context's stream */
+
+kamsta_status kamsta_ctx_create(int device, kamsta_ctx** out);
+kamsta_status kamsta_ctx_destroy(kamsta_ctx* ctx);
+/* Releases cached scratch memory of the context. */
+kamsta_status kamsta_ctx_trim(kamsta_ctx* ctx);
+/* Device bytes currently held by the context's scratch pool. */
+uint64_t kamsta_ctx_pool_bytes(const kamsta_ctx* ctx);
+
+/* ---- single-graph solve, host buffers ----------------------------------
+ * edges: m_directed entries (host memory); out: capacity >= n-1 entries
+ * (host memory).  Uses a per-thread default context on the current device.
+ * Replaces hybridMST::boruvka (hybrid_boruvka.hpp:263-301).                 */
+kamsta_status kamsta_mst_boruvka(const kamsta_wedge* edges, uint64_t m_directed,
+                                 uint32_t n, const kamsta_cfg* cfg,
+                                 kamsta_wedge* out, uint64_t* out_count,
+                                 kamsta_stats* stats);
+/* Replaces hybridMST::filter_boruvka (hybrid_boruvka_edgefilter.hpp:420-462). */
+kamsta_status kamsta_mst_filter_boruvka(const kamsta_wedge* edges,
+                                        uint64_t m_directed, uint32_t n,
+                                        const kamsta_cfg* cfg, kamsta_wedge* out,
+                                        uint64_t* out_count, kamsta_stats* stats);
+/* Same as kamsta_mst_boruvka for the reference's 24-byte WEdge input; ids
+ * must be < 2^32 (checked, KAMSTA_E_INPUT otherwise). */
+kamsta_status kamsta_mst_boruvka_wedge64(const kamsta_wedge64* edges,
+                                         uint64_t m_directed, uint64_t n,
+                                         const kamsta_cfg* cfg,
+                                         kamsta_wedge64* out,
+                                         uint64_t* out_count,
+                                         kamsta_stats* stats);
+
+/* ---- single-graph solve, device buffers --------------------------------
+ * d_edges / d_out are device pointers; the call is stream-ordered on
+ * `stream` and returns after the result count is known (one host read per
+ * Boruvka round).  out_count and stats are host pointers.                   */
+kamsta_status kamsta_mst_boruvka_dev(kamsta_ctx* ctx, const kamsta_wedge* d_edges,
+                                     uint64_t m_directed, uint32_t n,
+                                     const kamsta_cfg* cfg, kamsta_wedge* d_out,
+                                     uint64_t* out_count, kamsta_stats* stats,
+                                     kamsta_stream stream);
+kamsta_status kamsta_mst_filter_boruvka_dev(kamsta_ctx* ctx,
+                                            const kamsta_wedge* d_edges,
+                                            uint64_t m_directed, uint32_t n,
+                                            const kamsta_cfg* cfg,
+                                            kamsta_wedge* d_out,
+                                            uint64_t* out_count,
+                                            kamsta_stats* stats,
+                                            kamsta_stream stream);
+
+/* ---- device graph generators (seeded; identical to the oracle's CPU
+ * generators).  d_out must hold 2*m entries; *m_directed_out receives the
+ * number written.  Stand-ins for KaGen's get_gnm / get_rgg2D / get_rhg
+ * (benchmarks/mst_benchmarks.hpp:116-199). -------------------------------- */
+kamsta_status kamsta_gen_gnm_dev(kamsta_ctx* ctx, uint32_t n, uint64_t m,
+                                 uint64_t seed, uint32_t max_weight,
+                                 kamsta_wedge* d_out, uint64_t* m_directed_out,
+                                 kamsta_stream stream);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+#endif /* KAMSTA_GPU_H */

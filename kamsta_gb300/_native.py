@@ -1,0 +1,111 @@
+"""ctypes binding of libkamsta_gpu.so (the C ABI in include/kamsta_gpu.h).
+
+The library is loaded from the package directory only.  There is no CPU
+fallback: if the library is missing or a call fails, an exception is raised.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libkamsta_gpu.so")
+
+# status codes (kamsta_gpu.h)
+OK, E_INPUT, E_OOM, E_CUDA, E_NOCONVERGE, E_UNSUPPORTED, E_BUDGET, E_NOTREADY = range(8)
+STATUS_NAMES = {0: "OK", 1: "E_INPUT", 2: "E_OOM", 3: "E_CUDA", 4: "E_NOCONVERGE",
+                5: "E_UNSUPPORTED", 6: "E_BUDGET", 7: "E_NOTREADY"}
+
+FLAG_VALIDATE = 0x1
+FLAG_SORT_OUTPUT = 0x2
+FLAG_DEDUPE_NEVER = 0x4
+FLAG_DEDUPE_ALWAYS = 0x8
+FLAG_TRACE = 0x10
+TRACE_MAX = 128
+
+# numpy views of the edge layouts
+WEDGE = np.dtype([("src", "<u4"), ("dst", "<u4"), ("w", "<u4")])          # kamsta_wedge
+WEDGE64 = np.dtype([("src", "<u8"), ("dst", "<u8"), ("w", "<u4"), ("pad_", "<u4")])
+
+
+class KamstaError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class Cfg(C.Structure):
+    _fields_ = [("local_preprocessing", C.c_int32), ("compression", C.c_int32),
+                ("filter_threshold", C.c_uint64), ("flags", C.c_uint32),
+                ("dedupe_ratio", C.c_uint32), ("seed", C.c_uint64),
+                ("block_threads", C.c_uint32), ("items_per_thread", C.c_uint32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("num_mst_edges", C.c_uint64), ("total_weight", C.c_uint64),
+                ("rounds", C.c_uint32), ("levels", C.c_uint32),
+                ("dedupe_passes", C.c_uint32), ("gpu_launches", C.c_uint32),
+                ("device_ms", C.c_double), ("alg_bytes", C.c_uint64),
+                ("trace_len", C.c_uint32), ("pad_", C.c_uint32),
+                ("trace_m", C.c_uint64 * TRACE_MAX), ("trace_n", C.c_uint64 * TRACE_MAX)]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_
+             if k not in ("trace_m", "trace_n", "pad_")}
+        d["trace"] = [(int(self.trace_m[i]), int(self.trace_n[i])) for i in range(self.trace_len)]
+        return d
+
+
+_lib = None
+
+# Every symbol declared in include/kamsta_gpu.h, with its ctypes signature.
+P = C.c_void_p
+U32, U64, I32 = C.c_uint32, C.c_uint64, C.c_int
+SIGNATURES = {
+    "kamsta_cfg_default": (I32, [C.POINTER(Cfg)]),
+    "kamsta_version": (C.c_char_p, []),
+    "kamsta_last_error": (C.c_char_p, []),
+    "kamsta_ctx_create": (I32, [C.c_int, C.POINTER(P)]),
+    "kamsta_ctx_destroy": (I32, [P]),
+    "kamsta_ctx_trim": (I32, [P]),
+    "kamsta_ctx_pool_bytes": (U64, [P]),
+    "kamsta_mst_boruvka": (I32, [P, U64, U32, C.POINTER(Cfg), P, C.POINTER(U64), C.POINTER(Stats)]),
+    "kamsta_mst_filter_boruvka": (I32, [P, U64, U32, C.POINTER(Cfg), P, C.POINTER(U64),
+                                        C.POINTER(Stats)]),
+    "kamsta_mst_boruvka_wedge64": (I32, [P, U64, U64, C.POINTER(Cfg), P, C.POINTER(U64),
+                                         C.POINTER(Stats)]),
+    "kamsta_mst_boruvka_dev": (I32, [P, P, U64, U32, C.POINTER(Cfg), P, C.POINTER(U64),
+                                     C.POINTER(Stats), P]),
+    "kamsta_mst_filter_boruvka_dev": (I32, [P, P, U64, U32, C.POINTER(Cfg), P, C.POINTER(U64),
+                                            C.POINTER(Stats), P]),
+    "kamsta_gen_gnm_dev": (I32, [P, U32, U64, U64, U32, P, C.POINTER(U64), P]),
+}
+
+
+def lib():
+    """Load libkamsta_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run kamsta_gb300.build.build() first")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != OK:
+        msg = lib().kamsta_last_error()
+        raise KamstaError(status, msg.decode() if msg else "")
+
+
+def default_cfg() -> Cfg:
+    c = Cfg()
+    check(lib().kamsta_cfg_default(C.byref(c)))
+    return c

@@ -1,0 +1,277 @@
+// abi.cu -- extern "C" entry points declared in include/kamsta_gpu.h.
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "solver.cuh"
+
+namespace kamsta {
+const char* last_error_cstr();
+
+namespace {
+
+kamsta_status check_cfg(const kamsta_cfg* cfg) {
+  if (!cfg) return KAMSTA_OK;
+  if (cfg->compression != KAMSTA_NO_COMPRESSION) {
+    set_error("compression: only NO_COMPRESSION is implemented");
+    return KAMSTA_E_UNSUPPORTED;
+  }
+  if (cfg->local_preprocessing < KAMSTA_NO_PREPROCESSING ||
+      cfg->local_preprocessing > KAMSTA_REDUCE_EDGES_THEN_BORUVKA) {
+    set_error("local_preprocessing: unknown value");
+    return KAMSTA_E_INPUT;
+  }
+  return KAMSTA_OK;
+}
+
+kamsta_cfg cfg_or_default(const kamsta_cfg* cfg) {
+  kamsta_cfg c;
+  kamsta_cfg_default(&c);
+  return cfg ? *cfg : c;
+}
+
+// Per-thread default context for the host-buffer entry points, one per
+// device the thread has used.
+struct DefaultCtx {
+  std::vector<std::pair<int, kamsta_ctx*>> ctxs;
+  ~DefaultCtx() {
+    for (auto& p : ctxs) kamsta_ctx_destroy(p.second);
+  }
+  kamsta_status get(kamsta_ctx** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
+    for (auto& p : ctxs)
+      if (p.first == dev) {
+        *out = p.second;
+        return KAMSTA_OK;
+      }
+    kamsta_ctx* c = nullptr;
+    kamsta_status s = kamsta_ctx_create(dev, &c);
+    if (s != KAMSTA_OK) return s;
+    ctxs.emplace_back(dev, c);
+    *out = c;
+    return KAMSTA_OK;
+  }
+};
+thread_local DefaultCtx g_default;
+
+struct DevBuf {
+  void* p = nullptr;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+};
+
+kamsta_status solve_host(Algo algo, const kamsta_wedge* edges, uint64_t m, uint32_t n,
+                         const kamsta_cfg* cfg, kamsta_wedge* out, uint64_t* out_count,
+                         kamsta_stats* stats) {
+  if (!out_count || (m && !edges) || (n > 1 && !out)) {
+    set_error("null pointer argument");
+    return KAMSTA_E_INPUT;
+  }
+  kamsta_status s = check_cfg(cfg);
+  if (s != KAMSTA_OK) return s;
+  kamsta_cfg c = cfg_or_default(cfg);
+  kamsta_ctx* ctx = nullptr;
+  s = g_default.get(&ctx);
+  if (s != KAMSTA_OK) return s;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  *out_count = 0;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  if (m == 0 || n == 0) return KAMSTA_OK;
+  DevBuf din, dout;
+  cudaError_t e = cudaMalloc(&din.p, m * sizeof(kamsta_wedge));
+  if (e != cudaSuccess) return cuda_status(e, "cudaMalloc(input)");
+  e = cudaMalloc(&dout.p, std::max<uint64_t>(n, 1) * sizeof(kamsta_wedge));
+  if (e != cudaSuccess) return cuda_status(e, "cudaMalloc(output)");
+  e = cudaMemcpyAsync(din.p, edges, m * sizeof(kamsta_wedge), cudaMemcpyHostToDevice,
+                      ctx->stream);
+  if (e != cudaSuccess) return cuda_status(e, "cudaMemcpyAsync(H2D)");
+  SolveOut so;
+  s = solve_device(ctx, algo, static_cast<const kamsta_wedge*>(din.p), m, n, c,
+                   static_cast<kamsta_wedge*>(dout.p), &so, stats, ctx->stream);
+  if (s != KAMSTA_OK) return s;
+  if (so.count) {
+    e = cudaMemcpyAsync(out, dout.p, so.count * sizeof(kamsta_wedge), cudaMemcpyDeviceToHost,
+                        ctx->stream);
+    if (e != cudaSuccess) return cuda_status(e, "cudaMemcpyAsync(D2H)");
+  }
+  e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_status(e, "cudaStreamSynchronize");
+  if (c.flags & KAMSTA_FLAG_SORT_OUTPUT)
+    std::sort(out, out + so.count, [](const kamsta_wedge& a, const kamsta_wedge& b) {
+      return a.src != b.src ? a.src < b.src : a.dst < b.dst;
+    });
+  *out_count = so.count;
+  return KAMSTA_OK;
+}
+
+kamsta_status solve_dev(Algo algo, kamsta_ctx* ctx, const kamsta_wedge* d_edges, uint64_t m,
+                        uint32_t n, const kamsta_cfg* cfg, kamsta_wedge* d_out,
+                        uint64_t* out_count, kamsta_stats* stats, kamsta_stream stream) {
+  if (!ctx || !out_count || (m && !d_edges) || (n > 1 && !d_out)) {
+    set_error("null pointer argument");
+    return KAMSTA_E_INPUT;
+  }
+  kamsta_status s = check_cfg(cfg);
+  if (s != KAMSTA_OK) return s;
+  kamsta_cfg c = cfg_or_default(cfg);
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  int cur = 0;
+  cudaGetDevice(&cur);
+  if (cur != ctx->device) {
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return cuda_status(e, "cudaSetDevice");
+  }
+  SolveOut so;
+  s = solve_device(ctx, algo, d_edges, m, n, c, d_out, &so, stats,
+                   static_cast<cudaStream_t>(stream));
+  if (cur != ctx->device) cudaSetDevice(cur);
+  *out_count = so.count;
+  return s;
+}
+
+}  // namespace
+}  // namespace kamsta
+
+using namespace kamsta;
+
+extern "C" {
+
+kamsta_status kamsta_cfg_default(kamsta_cfg* cfg) {
+  if (!cfg) return KAMSTA_E_INPUT;
+  std::memset(cfg, 0, sizeof(*cfg));
+  cfg->local_preprocessing = KAMSTA_NO_PREPROCESSING;
+  cfg->compression = KAMSTA_NO_COMPRESSION;
+  cfg->filter_threshold = 4;
+  cfg->dedupe_ratio = 0;
+  cfg->seed = 0x243f6a8885a308d3ull;
+  return KAMSTA_OK;
+}
+
+const char* kamsta_version(void) { return "kamsta-gb300 0.1 (sm_103a)"; }
+
+const char* kamsta_last_error(void) { return last_error_cstr(); }
+
+kamsta_status kamsta_ctx_create(int device, kamsta_ctx** out) {
+  if (!out) return KAMSTA_E_INPUT;
+  *out = nullptr;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return cuda_status(e, "cudaSetDevice");
+  std::unique_ptr<kamsta_ctx> c(new kamsta_ctx());
+  c->device = device;
+  kamsta_status s = KAMSTA_OK;
+  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaMalloc(&c->d_counters, sizeof(DevCounters) * kCSlots)) != cudaSuccess ||
+      (e = cudaMalloc(&c->d_err, sizeof(uint32_t))) != cudaSuccess ||
+      (e = cudaMalloc(&c->d_samples, sizeof(uint32_t) * kSampleCap)) != cudaSuccess ||
+      (e = cudaMallocHost(&c->h_counters, sizeof(DevCounters) * kCSlots)) != cudaSuccess ||
+      (e = cudaMallocHost(&c->h_err, sizeof(uint32_t))) != cudaSuccess ||
+      (e = cudaEventCreate(&c->ev0)) != cudaSuccess ||
+      (e = cudaEventCreate(&c->ev1)) != cudaSuccess) {
+    s = cuda_status(e, "kamsta_ctx_create");
+  }
+  cudaSetDevice(prev);
+  if (s != KAMSTA_OK) {
+    kamsta_ctx_destroy(c.release());
+    return s;
+  }
+  *out = c.release();
+  return KAMSTA_OK;
+}
+
+kamsta_status kamsta_ctx_destroy(kamsta_ctx* ctx) {
+  if (!ctx) return KAMSTA_OK;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  ctx->fixed.release();
+  ctx->edges.release();
+  if (ctx->d_counters) cudaFree(ctx->d_counters);
+  if (ctx->d_err) cudaFree(ctx->d_err);
+  if (ctx->d_samples) cudaFree(ctx->d_samples);
+  if (ctx->h_counters) cudaFreeHost(ctx->h_counters);
+  if (ctx->h_err) cudaFreeHost(ctx->h_err);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  cudaSetDevice(prev);
+  delete ctx;
+  return KAMSTA_OK;
+}
+
+kamsta_status kamsta_ctx_trim(kamsta_ctx* ctx) {
+  if (!ctx) return KAMSTA_E_INPUT;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  ctx->fixed.release();
+  ctx->edges.release();
+  return KAMSTA_OK;
+}
+
+uint64_t kamsta_ctx_pool_bytes(const kamsta_ctx* ctx) {
+  return ctx ? ctx->fixed.cap + ctx->edges.cap : 0;
+}
+
+kamsta_status kamsta_mst_boruvka(const kamsta_wedge* edges, uint64_t m, uint32_t n,
+                                 const kamsta_cfg* cfg, kamsta_wedge* out,
+                                 uint64_t* out_count, kamsta_stats* stats) {
+  return solve_host(Algo::kBoruvka, edges, m, n, cfg, out, out_count, stats);
+}
+
+kamsta_status kamsta_mst_filter_boruvka(const kamsta_wedge* edges, uint64_t m, uint32_t n,
+                                        const kamsta_cfg* cfg, kamsta_wedge* out,
+                                        uint64_t* out_count, kamsta_stats* stats) {
+  return solve_host(Algo::kFilterBoruvka, edges, m, n, cfg, out, out_count, stats);
+}
+
+kamsta_status kamsta_mst_boruvka_wedge64(const kamsta_wedge64* edges, uint64_t m, uint64_t n,
+                                         const kamsta_cfg* cfg, kamsta_wedge64* out,
+                                         uint64_t* out_count, kamsta_stats* stats) {
+  if (!out_count || (m && !edges)) {
+    set_error("null pointer argument");
+    return KAMSTA_E_INPUT;
+  }
+  if (n > 0xffffffffull) {
+    set_error("input: n must be < 2^32 for the packed layout");
+    return KAMSTA_E_INPUT;
+  }
+  std::vector<kamsta_wedge> packed(m);
+  for (uint64_t i = 0; i < m; ++i) {
+    if (edges[i].src >= n || edges[i].dst >= n) {
+      set_error("input: vertex id >= n");
+      return KAMSTA_E_INPUT;
+    }
+    packed[i] = kamsta_wedge{static_cast<uint32_t>(edges[i].src),
+                             static_cast<uint32_t>(edges[i].dst), edges[i].w};
+  }
+  std::vector<kamsta_wedge> res(std::max<uint64_t>(n, 1));
+  kamsta_status s = solve_host(Algo::kBoruvka, packed.data(), m, static_cast<uint32_t>(n), cfg,
+                               res.data(), out_count, stats);
+  if (s != KAMSTA_OK) return s;
+  for (uint64_t i = 0; i < *out_count; ++i)
+    out[i] = kamsta_wedge64{res[i].src, res[i].dst, res[i].w, 0};
+  return KAMSTA_OK;
+}
+
+kamsta_status kamsta_mst_boruvka_dev(kamsta_ctx* ctx, const kamsta_wedge* d_edges, uint64_t m,
+                                     uint32_t n, const kamsta_cfg* cfg, kamsta_wedge* d_out,
+                                     uint64_t* out_count, kamsta_stats* stats,
+                                     kamsta_stream stream) {
+  return solve_dev(Algo::kBoruvka, ctx, d_edges, m, n, cfg, d_out, out_count, stats, stream);
+}
+
+kamsta_status kamsta_mst_filter_boruvka_dev(kamsta_ctx* ctx, const kamsta_wedge* d_edges,
+                                            uint64_t m, uint32_t n, const kamsta_cfg* cfg,
+                                            kamsta_wedge* d_out, uint64_t* out_count,
+                                            kamsta_stats* stats, kamsta_stream stream) {
+  return solve_dev(Algo::kFilterBoruvka, ctx, d_edges, m, n, cfg, d_out, out_count, stats,
+                   stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,200 @@
+// common.cuh -- shared device helpers of the GB300 MSF solver.
+//
+// Everything here is integer work: records, relaxed loads/stores for the
+// single-pass (decoupled look-back) scans, stable in-tile ranking by warp
+// ballots, and the bounded spin used by every wait.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace kamsta {
+
+constexpr uint64_t kInf64 = ~0ull;
+constexpr uint32_t kNone = 0xffffffffu;
+constexpr uint32_t kFull = 0xffffffffu;
+
+// A live undirected edge inside the solver.  Lists of Rec are always kept in
+// the input's (min, max) order, so (w << 32 | position) orders edges exactly
+// like the reference's (weight, local edge index) key
+// (mst_utils_common.hpp:76-81) and like its checker's (w, src, dst) order.
+struct __align__(16) Rec {
+  uint32_t a;    // current label of one endpoint
+  uint32_t b;    // current label of the other endpoint
+  uint32_t w;    // weight
+  uint32_t oid;  // index of the src<dst copy in the directed input
+};
+static_assert(sizeof(Rec) == 16, "Rec must be 16 bytes");
+
+// Device error bits (ORed into a device word, read by the host).
+enum : uint32_t {
+  kErrRange = 1u,     // id >= n in the input
+  kErrOrder = 2u,     // input not sorted by (src, dst)
+  kErrLookback = 4u,  // a look-back spin hit its cap
+  kErrJump = 8u,      // pointer jumping hit its cap
+  kErrHook = 16u,     // min edge not incident to its vertex (corruption)
+  kErrChase = 32u,    // label chase longer than the round count
+  kErrSpin = 64u,     // generic bounded wait expired
+  kErrOverflow = 128u,  // an output buffer was too small (retry sized)
+};
+
+// Bounded spins: every wait in a kernel gives up after this many polls and
+// reports kErrLookback instead of hanging the device.
+constexpr uint32_t kSpinCap = 1u << 22;
+// Pointer-jumping steps per vertex (a legal hook chain is shorter than n).
+constexpr uint32_t kJumpCap = 1u << 26;
+
+__device__ __forceinline__ uint64_t ld_relaxed(const uint64_t* p) {
+  uint64_t v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed(uint64_t* p, uint64_t v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// 64-bit minimum with a read first: most candidates lose against the value
+// already stored, so they never issue the atomic (keeps hub vertices from
+// serialising the L2 atomic unit).  Correct under any interleaving.
+__device__ __forceinline__ void min_update(uint64_t* p, uint64_t v) {
+  if (v < ld_relaxed(p)) atomicMin(reinterpret_cast<unsigned long long*>(p), v);
+}
+
+// SplitMix64's output function (Steele, Lea, Flood 2014): the counter-based
+// hash behind weight sampling and the seeded graph generators.
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// Decoupled look-back (Merrill & Garland, "Single-pass Parallel Prefix Scan
+// with Decoupled Look-back", 2016).  One 64-bit status word per tile:
+// bits 63:62 flag (0 empty, 1 aggregate, 2 inclusive prefix), 61:0 value.
+// Tiles are numbered by an atomic ticket, so every predecessor of a tile has
+// started before the tile looks back; the spin is still capped.
+constexpr uint64_t kLbAgg = 1ull << 62;
+constexpr uint64_t kLbInc = 2ull << 62;
+constexpr uint64_t kLbVal = (1ull << 62) - 1;
+
+// Called by all 32 lanes of one warp.  Returns the exclusive prefix of
+// `tile` (same value in every lane) and publishes its inclusive prefix.
+__device__ __forceinline__ uint64_t lookback(uint64_t* status, uint32_t tile,
+                                             uint64_t local, uint32_t* err) {
+  const uint32_t lane = lane_id();
+  if (tile == 0) {
+    if (lane == 0) st_relaxed(&status[0], kLbInc | local);
+    return 0;
+  }
+  if (lane == 0) st_relaxed(&status[tile], kLbAgg | local);
+  uint64_t excl = 0;
+  int64_t window = static_cast<int64_t>(tile) - 1;
+  uint32_t spins = 0;
+  for (;;) {
+    const int64_t idx = window - static_cast<int64_t>(lane);
+    const uint64_t s = idx >= 0 ? ld_relaxed(&status[idx]) : kLbInc;
+    const uint32_t flag = static_cast<uint32_t>(s >> 62);
+    const uint32_t inc = __ballot_sync(kFull, flag == 2);
+    const uint32_t empty = __ballot_sync(kFull, flag == 0);
+    const uint32_t limit = inc ? static_cast<uint32_t>(__ffs(inc) - 1) : 31u;
+    const uint32_t relevant = limit == 31u ? kFull : ((2u << limit) - 1u);
+    if (empty & relevant) {
+      if (++spins > kSpinCap) {
+        if (lane == 0) atomicOr(err, kErrLookback);
+        break;
+      }
+      __nanosleep(20);
+      continue;
+    }
+    excl += warp_sum(lane <= limit ? (s & kLbVal) : 0ull);
+    if (inc) break;
+    window -= 32;
+  }
+  if (lane == 0) st_relaxed(&status[tile], kLbInc | (excl + local));
+  return excl;
+}
+
+// ---------------------------------------------------------------------------
+// Stable in-tile ranking for up to NC output classes.
+//
+// Tile layout ("striped"): item j of thread t sits at tile position
+// j * BLOCK + t, so the (j, warp, lane) order is the input order and a warp
+// ballot per (j, warp) gives each kept item its rank inside its row.
+// cls[j] = class in [0, NC) or 0xff for "dropped".  On return offs[j] is the
+// item's rank among the tile's items of the same class, and tot[c] (shared)
+// is the tile's count of class c.  smem must hold NC * ITEMS * WARPS words.
+template <int NC, int ITEMS, int BLOCK>
+__device__ __forceinline__ void tile_rank(const uint8_t (&cls)[ITEMS],
+                                          uint32_t (&offs)[ITEMS],
+                                          uint32_t* smem, uint32_t* tot) {
+  constexpr int WARPS = BLOCK / 32;
+  constexpr int ROWS = ITEMS * WARPS;
+  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+  const uint32_t lt = lanemask_lt();
+#pragma unroll
+  for (int j = 0; j < ITEMS; ++j) {
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      const uint32_t b = __ballot_sync(kFull, cls[j] == c);
+      if (cls[j] == c) offs[j] = __popc(b & lt);
+      if (lane == 0) smem[c * ROWS + j * WARPS + warp] = __popc(b);
+    }
+  }
+  __syncthreads();
+  // exclusive scan of each class row-list, one warp per class
+  if (warp < NC) {
+    const int c = warp;
+    constexpr int PER = (ROWS + 31) / 32;
+    uint32_t vals[PER];
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const int r = lane * PER + k;
+      vals[k] = r < ROWS ? smem[c * ROWS + r] : 0u;
+      s += vals[k];
+    }
+    uint32_t incl = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, incl, o);
+      if (lane >= static_cast<uint32_t>(o)) incl += y;
+    }
+    uint32_t run = incl - s;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const int r = lane * PER + k;
+      if (r < ROWS) smem[c * ROWS + r] = run;
+      run += vals[k];
+    }
+    if (lane == 31) tot[c] = incl;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < ITEMS; ++j)
+    if (cls[j] != 0xff) offs[j] += smem[cls[j] * ROWS + j * WARPS + warp];
+}
+
+}  // namespace kamsta

@@ -1,0 +1,84 @@
+// solver.cuh -- host-side driver of the GB300 MSF solver (C++ over CUDA).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/kamsta_gpu.h"
+#include "common.cuh"
+
+namespace kamsta {
+
+// Grow-only device arena.  A solve carves its buffers from it; the memory
+// stays with the context between calls (the reference's analogue is the
+// per-call std::vector scratch of boruvka3, re-created every call).
+struct Arena {
+  char* base = nullptr;
+  size_t cap = 0;
+  size_t off = 0;
+  cudaError_t reserve(size_t bytes);
+  void release();
+  void reset() { off = 0; }
+  template <typename T>
+  T* take(size_t count) {
+    const size_t bytes = (count * sizeof(T) + 255) & ~static_cast<size_t>(255);
+    if (off + bytes > cap) return nullptr;
+    T* p = reinterpret_cast<T*>(base + off);
+    off += bytes;
+    return p;
+  }
+};
+
+// Per-kernel counter block in device memory (zeroed before each round).
+struct DevCounters {
+  unsigned long long cnt[8];
+  unsigned long long weight;
+  uint32_t ticket;
+  uint32_t err;
+  uint32_t pad[12];
+};
+static_assert(sizeof(DevCounters) == 128, "counter block size");
+
+enum CounterSlot : int { kCVertex = 0, kCEdge = 1, kCRep = 2, kCMisc = 3, kCSlots = 4 };
+constexpr uint32_t kSampleCap = 4096;
+
+}  // namespace kamsta
+
+struct kamsta_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  kamsta::Arena fixed;   // vertex arrays, class lists, status words
+  kamsta::Arena edges;   // round ping-pong lists (sized after the first pass)
+  kamsta::DevCounters* d_counters = nullptr;  // kCSlots blocks
+  uint32_t* d_samples = nullptr;               // weight samples (kSampleCap)
+  uint32_t* d_err = nullptr;
+  kamsta::DevCounters* h_counters = nullptr;  // pinned mirror
+  uint32_t* h_err = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::mutex mu;
+};
+
+namespace kamsta {
+
+struct SolveOut {
+  uint64_t count = 0;
+  uint64_t weight = 0;
+};
+
+// Which reference entry point a call mirrors.
+enum class Algo { kBoruvka, kFilterBoruvka };
+
+// Solves one graph whose directed, (src,dst)-sorted input lies in device
+// memory.  Writes the forest to d_out (device, capacity >= n-1).
+kamsta_status solve_device(kamsta_ctx* ctx, Algo algo, const kamsta_wedge* d_in,
+                           uint64_t m_directed, uint32_t n, const kamsta_cfg& cfg,
+                           kamsta_wedge* d_out, SolveOut* out, kamsta_stats* st,
+                           cudaStream_t stream);
+
+void set_error(const std::string& msg);
+kamsta_status cuda_status(cudaError_t e, const char* what);
+
+}  // namespace kamsta

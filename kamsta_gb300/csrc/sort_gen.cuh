@@ -1,0 +1,36 @@
+// sort_gen.cuh -- radix sort entry points and the device graph generators.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/kamsta_gpu.h"
+
+namespace kamsta {
+
+// Scratch element counts of one radix sort of n keys: `counts` u32 words and
+// `status` u64 words.
+struct RadixScratch {
+  uint64_t counts = 0;
+  uint64_t status = 0;
+};
+RadixScratch radix_scratch_bytes(uint64_t n);
+
+// Stable LSD radix sorts over the low `bits` bits of 64-bit keys (n < 2^32 -
+// 4096).  The result is in the *_alt buffers when *result_alt == 1.
+cudaError_t radix_sort_keys(cudaStream_t st, uint64_t* keys, uint64_t* keys_alt, uint64_t n,
+                            int bits, uint32_t* counts, uint64_t* status, uint32_t* ticket,
+                            uint32_t* err, int* result_alt, int sms);
+cudaError_t radix_sort_pairs_u32(cudaStream_t st, uint64_t* keys, uint64_t* keys_alt,
+                                 uint32_t* vals, uint32_t* vals_alt, uint64_t n, int bits,
+                                 uint32_t* counts, uint64_t* status, uint32_t* ticket,
+                                 uint32_t* err, int* result_alt, int sms);
+cudaError_t radix_sort_pairs_u64(cudaStream_t st, uint64_t* keys, uint64_t* keys_alt,
+                                 uint64_t* vals, uint64_t* vals_alt, uint64_t n, int bits,
+                                 uint32_t* counts, uint64_t* status, uint32_t* ticket,
+                                 uint32_t* err, int* result_alt, int sms);
+
+kamsta_status gen_gnm(kamsta_ctx* ctx, uint32_t n, uint64_t m, uint64_t seed,
+                      uint32_t max_weight, kamsta_wedge* d_out, uint64_t* m_out,
+                      cudaStream_t st);
+
+}  // namespace kamsta

@@ -1,0 +1,33 @@
+"""Build recipe for the oracle (test infrastructure, not the product).
+
+Compiles oracle/oracle.cpp into oracle/liboracle.so with g++ and OpenMP.
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline and
+reference arms load the result.
+"""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+SRC = [os.path.join(HERE, "oracle.cpp")]
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    deps = SRC + [os.path.join(HERE, "oracle.h"),
+                  os.path.join(HERE, "..", "include", "kamsta_gpu.h")]
+    if not force and os.path.exists(LIB):
+        t = os.path.getmtime(LIB)
+        if all(os.path.getmtime(d) <= t for d in deps):
+            return LIB
+    cmd = ["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared",
+           "-Wall", "-Wno-unused-function", "-o", LIB + ".tmp"] + SRC
+    if verbose:
+        print(" ".join(cmd), file=sys.stderr)
+    subprocess.run(cmd, check=True)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

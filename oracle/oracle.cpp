@@ -1,0 +1,468 @@
+// oracle.cpp -- CPU oracle and CPU baseline for the GB300 MSF solver.
+//
+// TEST INFRASTRUCTURE ONLY (see oracle.h).  Reference citations are paths in
+// the KaMSTa source tree.
+#include "oracle.h"
+
+#include <omp.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <parallel/algorithm>
+#include <random>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Union-find with union by size and path compression, as
+// include/datastructures/union_find.hpp:9-32 (sizes stored as negatives).
+struct UnionFind {
+  std::vector<int64_t> data;
+  explicit UnionFind(size_t n) : data(n, -1) {}
+  uint32_t find(uint32_t a) {
+    uint32_t root = a;
+    while (data[root] >= 0) root = static_cast<uint32_t>(data[root]);
+    while (data[a] >= 0) {  // compress
+      uint32_t next = static_cast<uint32_t>(data[a]);
+      data[a] = root;
+      a = next;
+    }
+    return root;
+  }
+  void unify(uint32_t a, uint32_t b) {
+    uint32_t ra = find(a), rb = find(b);
+    if (ra == rb) return;
+    if (data[rb] < data[ra]) std::swap(ra, rb);
+    data[ra] += data[rb];
+    data[rb] = ra;
+  }
+};
+
+}  // namespace
+
+extern "C" int oracle_max_threads(void) { return omp_get_max_threads(); }
+
+// ---------------------------------------------------------------------------
+// Kruskal, restating base_case_mst_algos.hpp:91-112: sort all entries by
+// WeightSrcDstOrder (utils.hpp:81-86), scan, keep an entry iff its endpoints
+// are in different sets.  For an undirected edge {u<v} the (u,v) copy sorts
+// before (v,u) under equal weight, so the (v,u) copy is always rejected;
+// sorting only the src<dst copies therefore gives the same forest.  The
+// src<dst copies arrive in (src,dst) order, so a stable sort by weight alone
+// yields the (w, src, dst) order.
+extern "C" int oracle_kruskal(const kamsta_wedge* edges, uint64_t m_directed,
+                              uint32_t n, kamsta_wedge* out,
+                              uint64_t* out_count, uint64_t* total_weight) {
+  std::vector<kamsta_wedge> und;
+  und.reserve(m_directed / 2 + 1);
+  for (uint64_t i = 0; i < m_directed; ++i) {
+    if (edges[i].src < edges[i].dst) {
+      if (edges[i].dst >= n) return 1;
+      und.push_back(edges[i]);
+    }
+  }
+  std::stable_sort(und.begin(), und.end(),
+                   [](const kamsta_wedge& a, const kamsta_wedge& b) {
+                     return a.w < b.w;
+                   });
+  UnionFind uf(n);
+  uint64_t cnt = 0, weight = 0;
+  for (const auto& e : und) {
+    if (uf.find(e.src) == uf.find(e.dst)) continue;
+    uf.unify(e.src, e.dst);
+    out[cnt++] = e;
+    weight += e.w;
+  }
+  *out_count = cnt;
+  *total_weight = weight;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Restatement of the reference's single-rank local filter-Boruvka.
+//
+// On one rank the reference's hybridMST::boruvka spends its time in
+// local_contraction -> execute_contraction -> boruvka_filter
+// (local_contraction.hpp:114-188, local_mst_respecting_cut_edges.hpp:262-302).
+// With the whole graph in one process every vertex is local, so the cut-edge
+// constraints (min_cut_weights, mst_utils_cut_edges.hpp:198-225) never bind
+// and are left out; everything else follows the reference step by step.
+namespace port {
+
+constexpr uint32_t kUndef = 0xffffffffu;
+constexpr uint32_t kMsb = 0x80000000u;  // self-loop tag (MSD<LocalEdgeId>)
+
+struct LocalEdge {  // WEdgeId_4_1_7-like: labels, weight, global edge id
+  uint32_t src, dst, w, gid;
+};
+
+// Parallel stable pack: out[k++] = in[i] for every i with keep(i).
+template <typename T, typename Keep>
+size_t pack(const T* in, size_t n, T* out, Keep keep) {
+  int nt = omp_get_max_threads();
+  std::vector<size_t> cnt(nt + 1, 0);
+#pragma omp parallel num_threads(nt)
+  {
+    int t = omp_get_thread_num();
+    size_t lo = n * t / nt, hi = n * (t + 1) / nt, c = 0;
+    for (size_t i = lo; i < hi; ++i) c += keep(i) ? 1 : 0;
+    cnt[t + 1] = c;
+#pragma omp barrier
+#pragma omp single
+    for (int k = 0; k < nt; ++k) cnt[k + 1] += cnt[k];
+    size_t o = cnt[t];
+    for (size_t i = lo; i < hi; ++i)
+      if (keep(i)) out[o++] = in[i];
+  }
+  return cnt[nt];
+}
+
+// CAS-min on a packed (weight << 32 | edge id) word: the EdgeIdWeight order
+// of EdgeIdWeightBaseComparator (mst_utils_common.hpp:76-81) and
+// write_min_gbbs (util/atomic_ops.hpp:30-38).
+inline void write_min(std::atomic<uint64_t>& a, uint64_t v) {
+  uint64_t cur = a.load(std::memory_order_relaxed);
+  while (v < cur && !a.compare_exchange_weak(cur, v, std::memory_order_relaxed)) {
+  }
+}
+
+struct State {
+  uint32_t n_initial = 0;
+  std::vector<uint32_t> parents;             // parents over all vertices
+  std::vector<std::atomic<uint64_t>> min_edges;
+  std::vector<uint32_t> vertices, vertices_tmp;  // SwapStorage<VId> vertices_
+  std::vector<uint32_t> mst;                 // global edge ids of forest edges
+  uint32_t rounds = 0;
+};
+
+struct Result {
+  size_t num_mst_edges;
+  size_t num_active_vertices;
+};
+
+// boruvka3, local_mst_respecting_cut_edges.hpp:101-207.
+Result boruvka3(State& st, std::vector<LocalEdge>& edges, size_t n) {
+  size_t m = edges.size();
+  std::vector<uint32_t> edge_ids(m), edge_ids_tmp(m);
+#pragma omp parallel for schedule(static)
+  for (size_t i = 0; i < m; ++i) edge_ids[i] = static_cast<uint32_t>(i);
+  std::vector<uint32_t> exhausted;
+  std::vector<uint32_t> new_mst(n, kUndef), new_mst_packed(n);
+  std::vector<uint8_t> can_be_reactivated(n, 0), is_active(n, 1);
+  size_t nb_mst = 0;
+  uint32_t* V = st.vertices.data();
+  while (n > 0 && m > 0) {
+    st.rounds++;
+    // compute_min_edges, mst_utils_common.hpp:84-105
+#pragma omp parallel for schedule(static)
+    for (size_t i = 0; i < n; ++i)
+      st.min_edges[V[i]].store(~0ull, std::memory_order_relaxed);
+#pragma omp parallel for schedule(static)
+    for (size_t i = 0; i < m; ++i) {
+      const uint32_t e = edge_ids[i];
+      const LocalEdge& ed = edges[e];
+      const uint64_t key = (static_cast<uint64_t>(ed.w) << 32) | e;
+      write_min(st.min_edges[ed.src], key);
+      write_min(st.min_edges[ed.dst], key);
+    }
+    // determine_mst_edges_exhausted, mst_utils_cut_edges.hpp:102-166 (no
+    // cut edges: both min-cut tests pass)
+#pragma omp parallel for schedule(static)
+    for (size_t i = 0; i < n; ++i) {
+      const uint32_t v = V[i];
+      const uint64_t k = st.min_edges[v].load(std::memory_order_relaxed);
+      if (k == ~0ull) {
+        is_active[i] = 0;
+        can_be_reactivated[i] = 1;
+        new_mst[i] = kUndef;
+        continue;
+      }
+      const uint32_t e = static_cast<uint32_t>(k);
+      const uint32_t u = edges[e].src ^ edges[e].dst ^ v;
+      const uint64_t ku = st.min_edges[u].load(std::memory_order_relaxed);
+      if (u > v && static_cast<uint32_t>(ku) == e) {  // pseudo root: lower id
+        st.parents[v] = v;
+        is_active[i] = 1;
+        new_mst[i] = kUndef;
+      } else {
+        st.parents[v] = u;
+        is_active[i] = 0;
+        new_mst[i] = e;
+      }
+    }
+    // add_new_mst_edges_to_mst_array, gbbs_reimplementation.hpp:137-159
+    size_t added = pack(new_mst.data(), n, new_mst_packed.data(),
+                        [&](size_t i) { return new_mst[i] != kUndef; });
+    size_t base = st.mst.size();
+    st.mst.resize(base + added);
+#pragma omp parallel for schedule(static)
+    for (size_t i = 0; i < added; ++i) st.mst[base + i] = edges[new_mst_packed[i]].gid;
+    nb_mst += added;
+    // update_parents_min_cut_weights, mst_utils_cut_edges.hpp:168-196
+#pragma omp parallel for schedule(static)
+    for (size_t i = 0; i < n; ++i) {
+      const uint32_t v = V[i];
+      while (st.parents[v] != st.parents[st.parents[v]])
+        st.parents[v] = st.parents[st.parents[v]];
+    }
+    // identify_exhausted_vertices / compactify_vertices,
+    // mst_utils_common.hpp:106-132
+    {
+      size_t old = exhausted.size();
+      exhausted.resize(old + n);
+      size_t k = pack(V, n, exhausted.data() + old,
+                      [&](size_t i) { return can_be_reactivated[i] != 0; });
+      exhausted.resize(old + k);
+#pragma omp parallel for schedule(static)
+      for (size_t i = 0; i < n; ++i) can_be_reactivated[i] = 0;
+      n = pack(V, n, st.vertices_tmp.data(),
+               [&](size_t i) { return is_active[i] != 0; });
+      std::swap(st.vertices, st.vertices_tmp);
+      V = st.vertices.data();
+    }
+    // relabel_edges, gbbs_reimplementation.hpp:182-203
+#pragma omp parallel for schedule(static)
+    for (size_t i = 0; i < m; ++i) {
+      LocalEdge& ed = edges[edge_ids[i]];
+      const uint32_t pu = st.parents[ed.src], pv = st.parents[ed.dst];
+      ed.src = pu;
+      ed.dst = pv;
+      if (pu == pv) edge_ids[i] |= kMsb;
+    }
+    // filter_out_self_loops, mst_utils_common.hpp:157-175
+    m = pack(edge_ids.data(), m, edge_ids_tmp.data(),
+             [&](size_t i) { return (edge_ids[i] & kMsb) == 0; });
+    std::swap(edge_ids, edge_ids_tmp);
+  }
+  // append exhausted vertices, final shortcut (local_mst...:195-203)
+  for (size_t i = 0; i < exhausted.size(); ++i) V[n + i] = exhausted[i];
+  n += exhausted.size();
+#pragma omp parallel for schedule(static)
+  for (size_t i = 0; i < st.n_initial; ++i)
+    while (st.parents[i] != st.parents[st.parents[i]])
+      st.parents[i] = st.parents[st.parents[i]];
+  return Result{nb_mst, n};
+}
+
+// localMST::get_pivot, mst_utils_filter.hpp:13-30: 50 samples drawn by
+// std::mt19937(0) / uniform_int_distribution<>, 25% quantile by weight.
+uint32_t get_pivot(const std::vector<LocalEdge>& edges) {
+  if (edges.empty()) return 1;
+  if (edges.size() <= 2) return edges[0].w;
+  std::mt19937 gen(0);
+  std::uniform_int_distribution<> distrib(0, static_cast<int>(edges.size() - 1));
+  const size_t num_samples = 50;
+  std::vector<uint32_t> samples(num_samples);
+  for (size_t i = 0; i < num_samples; ++i) samples[i] = edges[distrib(gen)].w;
+  std::sort(samples.begin(), samples.end());
+  return samples[static_cast<size_t>(num_samples * 0.25)];
+}
+
+// localMST::is_unbalanced, mst_utils_filter.hpp:32-37.
+bool is_unbalanced(size_t num_edges, size_t num_light) {
+  const double diff = static_cast<double>(num_edges - num_light);
+  return std::abs(0.5 - diff / static_cast<double>(num_edges)) > 0.4;
+}
+
+// boruvka_filter_rec, local_mst_respecting_cut_edges.hpp:209-260.
+Result filter_rec(State& st, std::vector<LocalEdge>& edges, size_t n) {
+  if (n <= 1) return Result{0, n};
+  if (edges.size() <= 3 * n) return boruvka3(st, edges, n);
+  // localMST::partition, mst_utils_filter.hpp:39-99
+  const uint32_t pivot = get_pivot(edges);
+  size_t num_light = 0;
+#pragma omp parallel for reduction(+ : num_light) schedule(static)
+  for (size_t i = 0; i < edges.size(); ++i) num_light += edges[i].w <= pivot;
+  if (is_unbalanced(edges.size(), num_light)) return boruvka3(st, edges, n);
+  std::vector<LocalEdge> light(num_light);
+  pack(edges.data(), edges.size(), light.data(),
+       [&](size_t i) { return edges[i].w <= pivot; });
+  const Result lr = filter_rec(st, light, n);
+  // localMST::filter, mst_utils_filter.hpp:102-126: relabel by the final
+  // parents, zero the light edges, drop self loops (stable).
+#pragma omp parallel for schedule(static)
+  for (size_t i = 0; i < edges.size(); ++i) {
+    LocalEdge& e = edges[i];
+    const bool small = e.w <= pivot;
+    e.src = small ? 0 : st.parents[e.src];
+    e.dst = small ? 0 : st.parents[e.dst];
+  }
+  std::vector<LocalEdge> heavy(edges.size());
+  size_t k = pack(edges.data(), edges.size(), heavy.data(),
+                  [&](size_t i) { return edges[i].src != edges[i].dst; });
+  heavy.resize(k);
+  Result hr = boruvka3(st, heavy, lr.num_active_vertices);
+  hr.num_mst_edges += lr.num_mst_edges;
+  return hr;
+}
+
+}  // namespace port
+
+extern "C" int oracle_boruvka_filter(const kamsta_wedge* edges,
+                                     uint64_t m_directed, uint32_t n,
+                                     int threads, kamsta_wedge* out,
+                                     uint64_t* out_count,
+                                     uint64_t* total_weight,
+                                     uint32_t* rounds_out) {
+  using namespace port;
+  if (threads > 0) omp_set_num_threads(threads);
+  // get_WEdgeIds + get_local_edges (uncompressed_graph.hpp:38-51,
+  // local_contraction/utils.hpp:30-36): keep the src<dst copies, global id =
+  // index in the input.
+  std::vector<LocalEdge> local(m_directed / 2 + 1);
+  {
+    int nt = omp_get_max_threads();
+    std::vector<size_t> cnt(nt + 1, 0);
+#pragma omp parallel num_threads(nt)
+    {
+      int t = omp_get_thread_num();
+      size_t lo = m_directed * t / nt, hi = m_directed * (t + 1) / nt, c = 0;
+      for (size_t i = lo; i < hi; ++i) c += edges[i].src < edges[i].dst;
+      cnt[t + 1] = c;
+#pragma omp barrier
+#pragma omp single
+      for (int k = 0; k < nt; ++k) cnt[k + 1] += cnt[k];
+      size_t o = cnt[t];
+      for (size_t i = lo; i < hi; ++i)
+        if (edges[i].src < edges[i].dst)
+          local[o++] = LocalEdge{edges[i].src, edges[i].dst, edges[i].w,
+                                 static_cast<uint32_t>(i)};
+    }
+    local.resize(cnt[nt]);
+  }
+  State st;
+  st.n_initial = n;
+  st.parents.resize(n);
+  st.min_edges = std::vector<std::atomic<uint64_t>>(n);
+  st.vertices.resize(n);
+  st.vertices_tmp.resize(n);
+#pragma omp parallel for schedule(static)
+  for (size_t i = 0; i < n; ++i) {
+    st.parents[i] = static_cast<uint32_t>(i);
+    st.vertices[i] = static_cast<uint32_t>(i);
+  }
+  filter_rec(st, local, n);
+  uint64_t weight = 0;
+  const size_t k = st.mst.size();
+#pragma omp parallel for reduction(+ : weight) schedule(static)
+  for (size_t i = 0; i < k; ++i) {
+    const kamsta_wedge& e = edges[st.mst[i]];
+    out[i] = e;
+    weight += e.w;
+  }
+  *out_count = k;
+  *total_weight = weight;
+  if (rounds_out) *rounds_out = st.rounds;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Seeded G(n,m) generator.  KaGen (the reference's generator library) is not
+// vendored, so both this CPU version and the device version implement the
+// same definition:
+//   mix64     = SplitMix64's output function (Steele, Lea, Flood 2014);
+//   candidate i: h1 = mix64(base + 2i), h2 = mix64(base + 2i + 1),
+//                u = hi64(h1 * n), v = hi64(h2 * n), valid iff u != v,
+//                key = min << 32 | max,       base = mix64(seed);
+//   the graph   = the first m distinct valid keys in candidate order (a
+//                uniform m-subset of all unordered pairs);
+//   weight      = 1 + hi64(mix64(wseed ^ key) * max_weight),
+//                wseed = mix64(seed ^ 0x6a09e667f3bcc909).
+namespace gen {
+
+inline uint64_t mix64(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+inline uint64_t hi64(uint64_t a, uint64_t b) {
+  return static_cast<uint64_t>((static_cast<unsigned __int128>(a) * b) >> 64);
+}
+
+}  // namespace gen
+
+extern "C" int oracle_gen_gnm(uint32_t n, uint64_t m, uint64_t seed,
+                              uint32_t max_weight, kamsta_wedge* out,
+                              uint64_t* m_directed_out) {
+  using namespace gen;
+  const uint64_t pairs = static_cast<uint64_t>(n) * (n - 1ull) / 2;
+  if (n < 2 || m > pairs || max_weight == 0) {
+    if (m == 0) {
+      *m_directed_out = 0;
+      return 0;
+    }
+    return 1;
+  }
+  const uint64_t base = mix64(seed);
+  const uint64_t wseed = mix64(seed ^ 0x6a09e667f3bcc909ull);
+  uint64_t K = m + m / 1024 + 4096;
+  std::vector<uint64_t> sel;
+  for (;;) {
+    // (key, candidate index) for every valid candidate, sorted by key then
+    // index; the first entry of each key run is its first occurrence.
+    std::vector<std::pair<uint64_t, uint64_t>> c(K);
+#pragma omp parallel for schedule(static)
+    for (uint64_t i = 0; i < K; ++i) {
+      uint32_t u = static_cast<uint32_t>(hi64(mix64(base + 2 * i), n));
+      uint32_t v = static_cast<uint32_t>(hi64(mix64(base + 2 * i + 1), n));
+      uint64_t key = ~0ull;
+      if (u != v) key = (static_cast<uint64_t>(std::min(u, v)) << 32) | std::max(u, v);
+      c[i] = {key, i};
+    }
+    __gnu_parallel::sort(c.begin(), c.end());
+    std::vector<uint8_t> first(K, 0);
+    for (uint64_t j = 0; j < K; ++j) {
+      if (c[j].first == ~0ull) break;
+      if (j == 0 || c[j].first != c[j - 1].first) first[c[j].second] = 1;
+    }
+    uint64_t cnt = 0, T = K;
+    for (uint64_t i = 0; i < K; ++i) {
+      cnt += first[i];
+      if (cnt == m) {
+        T = i;
+        break;
+      }
+    }
+    if (T == K) {  // not enough distinct pairs yet: draw more
+      K = K + (m - cnt) * 2 + 4096;
+      continue;
+    }
+    sel.reserve(m);
+    for (uint64_t j = 0; j < K; ++j) {
+      if (c[j].first == ~0ull) break;
+      if ((j == 0 || c[j].first != c[j - 1].first) && c[j].second <= T)
+        sel.push_back(c[j].first);
+    }
+    break;
+  }
+  // Both directions sorted by (src, dst): row x = lower neighbours (from
+  // pairs (u, x), in increasing u) followed by upper neighbours (pairs (x, v),
+  // in increasing v).
+  std::vector<uint64_t> lowdeg(n, 0), deg(n, 0);
+  for (uint64_t key : sel) {
+    uint32_t u = static_cast<uint32_t>(key >> 32), v = static_cast<uint32_t>(key);
+    deg[u]++;
+    deg[v]++;
+    lowdeg[v]++;
+  }
+  std::vector<uint64_t> lo_cur(n), hi_cur(n);
+  uint64_t off = 0;
+  for (uint32_t x = 0; x < n; ++x) {
+    lo_cur[x] = off;
+    hi_cur[x] = off + lowdeg[x];
+    off += deg[x];
+  }
+  for (uint64_t key : sel) {
+    uint32_t u = static_cast<uint32_t>(key >> 32), v = static_cast<uint32_t>(key);
+    uint32_t w = 1 + static_cast<uint32_t>(hi64(mix64(wseed ^ key), max_weight));
+    out[hi_cur[u]++] = kamsta_wedge{u, v, w};
+    out[lo_cur[v]++] = kamsta_wedge{v, u, w};
+  }
+  *m_directed_out = 2 * sel.size();
+  return 0;
+}

@@ -1,0 +1,62 @@
+/*
+ * oracle.h -- CPU test infrastructure for the GB300 MSF solver.
+ *
+ * THIS IS THE ORACLE, NOT THE PRODUCT.  Only tests/, __graft_entry__.smoke()
+ * and bench.py's CPU-baseline / reference arm may load it.  The product path
+ * (kamsta_gb300, libkamsta_gpu.so) never links or calls anything here.
+ *
+ * Contents:
+ *   oracle_kruskal          -- known-answer MSF: Kruskal under the
+ *                              (w, src, dst) order over the both-directions
+ *                              input, restating the reference checker
+ *                              include/algorithms/base_case_mst_algos.hpp:91-112
+ *                              with union-find include/datastructures/union_find.hpp:9-32.
+ *   oracle_boruvka_filter   -- OpenMP restatement of the reference's
+ *                              single-rank local filter-Boruvka
+ *                              (local_mst_respecting_cut_edges.hpp:101-302 and
+ *                              the mst_utils_*.hpp round primitives); the timed
+ *                              "reference CPU" baseline (kind "port").
+ *   oracle_gen_gnm          -- seeded G(n,m) generator; bit-identical to the
+ *                              device generator kamsta_gen_gnm_dev.
+ *
+ * Parity status: the reference ships no golden vectors (its only test,
+ * tests/test_sets.sh, checks the MSF weight against this same Kruskal).
+ * Kruskal is pinned by hand-checked tiny graphs in tests/golden/.
+ */
+#ifndef KAMSTA_ORACLE_H
+#define KAMSTA_ORACLE_H
+#include <stdint.h>
+
+#include "../include/kamsta_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Kruskal MSF.  out: capacity >= n entries.  Returns 0 on success. */
+int oracle_kruskal(const kamsta_wedge* edges, uint64_t m_directed, uint32_t n,
+                   kamsta_wedge* out, uint64_t* out_count,
+                   uint64_t* total_weight);
+
+/* Restated reference local filter-Boruvka on `threads` OpenMP threads
+ * (0 = all).  out: capacity >= n entries.  Per-phase counters go to
+ * rounds_out (may be NULL). */
+int oracle_boruvka_filter(const kamsta_wedge* edges, uint64_t m_directed,
+                          uint32_t n, int threads, kamsta_wedge* out,
+                          uint64_t* out_count, uint64_t* total_weight,
+                          uint32_t* rounds_out);
+
+/* Seeded G(n,m): the first m distinct unordered pairs {u != v} of the
+ * candidate stream, weights uniform in [1, max_weight], both directions,
+ * sorted by (src, dst).  out: capacity 2*m.  Returns 0, or 1 if m exceeds
+ * n(n-1)/2. */
+int oracle_gen_gnm(uint32_t n, uint64_t m, uint64_t seed, uint32_t max_weight,
+                   kamsta_wedge* out, uint64_t* m_directed_out);
+
+/* Number of OpenMP threads the oracle uses when threads == 0. */
+int oracle_max_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,104 @@
+"""ctypes access to the oracle (oracle/liboracle.so) for the tests.
+
+The oracle is test infrastructure: it checks the GPU results and is never
+part of the product path.
+"""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+from oracle import build as _build  # noqa: E402
+
+WEDGE = np.dtype([("src", "<u4"), ("dst", "<u4"), ("w", "<u4")])
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = C.CDLL(_build.build())
+        P, U32, U64 = C.c_void_p, C.c_uint32, C.c_uint64
+        L.oracle_kruskal.argtypes = [P, U64, U32, P, C.POINTER(U64), C.POINTER(U64)]
+        L.oracle_boruvka_filter.argtypes = [P, U64, U32, C.c_int, P, C.POINTER(U64),
+                                            C.POINTER(U64), C.POINTER(U32)]
+        L.oracle_gen_gnm.argtypes = [U32, U64, U64, U32, P, C.POINTER(U64)]
+        L.oracle_max_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def gen_gnm(n: int, m: int, seed: int, max_weight: int = 254) -> np.ndarray:
+    out = np.empty(max(2 * m, 1), WEDGE)
+    cnt = C.c_uint64()
+    rc = lib().oracle_gen_gnm(n, m, seed, max_weight, out.ctypes.data, C.byref(cnt))
+    if rc != 0:
+        raise ValueError("oracle_gen_gnm: m exceeds n(n-1)/2")
+    return out[: cnt.value]
+
+
+def kruskal(edges: np.ndarray, n: int):
+    e = np.ascontiguousarray(edges, dtype=WEDGE)
+    out = np.empty(max(n, 1), WEDGE)
+    cnt, w = C.c_uint64(), C.c_uint64()
+    rc = lib().oracle_kruskal(e.ctypes.data, len(e), n, out.ctypes.data, C.byref(cnt), C.byref(w))
+    assert rc == 0
+    return out[: cnt.value].copy(), int(w.value)
+
+
+def boruvka_filter(edges: np.ndarray, n: int, threads: int = 0):
+    """Restated reference local filter-Boruvka (timed CPU baseline)."""
+    e = np.ascontiguousarray(edges, dtype=WEDGE)
+    out = np.empty(max(n, 1), WEDGE)
+    cnt, w, r = C.c_uint64(), C.c_uint64(), C.c_uint32()
+    rc = lib().oracle_boruvka_filter(e.ctypes.data, len(e), n, threads, out.ctypes.data,
+                                     C.byref(cnt), C.byref(w), C.byref(r))
+    assert rc == 0
+    return out[: cnt.value].copy(), int(w.value), int(r.value)
+
+
+def canon_keys(mst: np.ndarray) -> np.ndarray:
+    """Sorted (min << 32 | max) keys of a forest: order-free edge-set identity."""
+    a = np.minimum(mst["src"], mst["dst"]).astype(np.uint64)
+    b = np.maximum(mst["src"], mst["dst"]).astype(np.uint64)
+    return np.sort((a << np.uint64(32)) | b)
+
+
+def symmetric_from_undirected(und, n=None) -> np.ndarray:
+    """Both directions, sorted by (src, dst), from (u, v, w) triples."""
+    und = list(und)
+    rows = []
+    for u, v, w in und:
+        rows.append((u, v, w))
+        rows.append((v, u, w))
+    rows.sort(key=lambda t: (t[0], t[1]))
+    out = np.empty(len(rows), WEDGE)
+    for i, (u, v, w) in enumerate(rows):
+        out[i] = (u, v, w)
+    return out
+
+
+def py_kruskal(edges: np.ndarray, n: int):
+    """Independent pure-Python Kruskal under (w, src, dst) over all entries
+    (base_case_mst_algos.hpp:91-112), for small cases."""
+    order = sorted(range(len(edges)), key=lambda i: (int(edges["w"][i]), int(edges["src"][i]),
+                                                    int(edges["dst"][i])))
+    parent = list(range(n))
+
+    def find(x):
+        while parent[x] != x:
+            parent[x] = parent[parent[x]]
+            x = parent[x]
+        return x
+
+    res = []
+    for i in order:
+        a, b = find(int(edges["src"][i])), find(int(edges["dst"][i]))
+        if a == b:
+            continue
+        parent[a] = b
+        res.append((int(edges["src"][i]), int(edges["dst"][i]), int(edges["w"][i])))
+    return res

@@ -1,0 +1,191 @@
+"""GPU parity tests: the CUDA path through the C ABI against the oracle.
+
+Bar: bit-exact -- the forest edge set under the (w, min, max) order and its
+total weight must equal the oracle's Kruskal on the same seeded input.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _tiny():
+    with open(os.path.join(HERE, "golden", "tiny_graphs.json")) as f:
+        return json.load(f)
+
+
+def _configs(K):
+    LP = K.LocalPreprocessing
+    return {
+        "boruvka_plain": (K.boruvka, K.AlgorithmConfig(local_preprocessing=LP.NO_PREPROCESSING)),
+        "boruvka_local": (K.boruvka, K.AlgorithmConfig(local_preprocessing=LP.MODIFIED_BORUVKA)),
+    }
+
+
+ALGOS = ["boruvka_plain", "boruvka_local"]
+
+
+def _triples(mst):
+    return sorted((int(min(a, b)), int(max(a, b)), int(w))
+                  for a, b, w in zip(mst["src"], mst["dst"], mst["w"]))
+
+
+def _check(oracle, got, edges, n):
+    ref, w = oracle.kruskal(edges, n)
+    assert len(got) == len(ref)
+    assert int(got["w"].astype(np.uint64).sum()) == w
+    assert np.all(got["src"] < got["dst"])  # written as (min, max, w)
+    assert np.array_equal(oracle.canon_keys(got), oracle.canon_keys(ref))
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+@pytest.mark.parametrize("case", _tiny(), ids=lambda c: c["name"])
+def test_tiny_golden(kamsta, oracle, algo, case):
+    fn, cfg = _configs(kamsta)[algo]
+    e = oracle.symmetric_from_undirected([tuple(t) for t in case["edges"]])
+    got = fn(e, cfg, n=case["n"])
+    assert _triples(got) == [tuple(t) for t in case["forest"]]
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+@pytest.mark.parametrize("n,m,seed,wmax", [
+    (64, 100, 1, 254), (1000, 2000, 2, 254), (1000, 20000, 3, 254), (1 << 12, 1 << 15, 4, 254),
+    (1 << 16, 1 << 20, 5, 254), (1 << 16, 1 << 17, 6, 254), (1 << 14, 1 << 18, 7, 4),
+    (1 << 14, 1 << 16, 8, 1), (1 << 15, 1 << 18, 9, 1 << 30), (3000, 4000000, 10, 254)])
+def test_gnm_parity(kamsta, oracle, algo, n, m, seed, wmax):
+    fn, cfg = _configs(kamsta)[algo]
+    e = oracle.gen_gnm(n, m, seed, wmax)
+    _check(oracle, fn(e, cfg, n=n), e, n)
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+def test_isolated_and_unused_vertices(kamsta, oracle, algo):
+    fn, cfg = _configs(kamsta)[algo]
+    e = oracle.gen_gnm(500, 2000, 12)
+    e = e.copy()
+    e["src"] *= 3
+    e["dst"] *= 3  # ids spread out: 2/3 of the vertices are isolated
+    _check(oracle, fn(e, cfg, n=1600), e, 1600)
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+def test_long_increasing_path(kamsta, oracle, algo):
+    """Hook chains of depth n-1 (pointer jumping worst case)."""
+    fn, cfg = _configs(kamsta)[algo]
+    n = 1 << 16
+    und = [(i, i + 1, i + 1) for i in range(n - 1)]
+    e = oracle.symmetric_from_undirected(und)
+    _check(oracle, fn(e, cfg, n=n), e, n)
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+def test_star_hub(kamsta, oracle, algo):
+    """One vertex adjacent to all others (segmented minimum over a hub)."""
+    fn, cfg = _configs(kamsta)[algo]
+    n = 1 << 17
+    rng = np.random.default_rng(3)
+    w = rng.integers(1, 255, n - 1)
+    und = [(0, i, int(w[i - 1])) for i in range(1, n)] + [(i, i + 1, 200) for i in range(1, n - 1)]
+    e = oracle.symmetric_from_undirected(und)
+    _check(oracle, fn(e, cfg, n=n), e, n)
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+def test_disconnected_components(kamsta, oracle, algo):
+    fn, cfg = _configs(kamsta)[algo]
+    parts = []
+    off = 0
+    for k, (n, m) in enumerate([(300, 900), (2000, 3000), (1, 0), (5000, 60000), (2, 1)]):
+        if m:
+            g = oracle.gen_gnm(n, m, 20 + k)
+            g = g.copy()
+            g["src"] += off
+            g["dst"] += off
+            parts.append(g)
+        off += n
+    e = np.concatenate(parts)
+    _check(oracle, fn(e, cfg, n=off), e, off)
+
+
+def test_empty_inputs(kamsta):
+    empty = np.zeros(0, kamsta.WEDGE)
+    assert len(kamsta.boruvka(empty, n=0)) == 0
+    assert len(kamsta.boruvka(empty, n=10)) == 0
+
+
+def test_validation_rejects_unsorted_and_out_of_range(kamsta, oracle):
+    e = oracle.gen_gnm(100, 300, 1)
+    cfg = kamsta.AlgorithmConfig(validate=True)
+    bad = e.copy()
+    bad[[5, 6]] = bad[[6, 5]]
+    with pytest.raises(kamsta.KamstaError) as ei:
+        kamsta.boruvka(bad, cfg, n=100)
+    assert ei.value.status == 1
+    with pytest.raises(kamsta.KamstaError) as ei:
+        kamsta.boruvka(e, cfg, n=50)
+    assert ei.value.status == 1
+    # the context stays usable after a rejected call
+    _check(oracle, kamsta.boruvka(e, cfg, n=100), e, 100)
+
+
+def test_wedge64_entry_point(kamsta, oracle):
+    e = oracle.gen_gnm(2000, 10000, 31)
+    e64 = np.zeros(len(e), kamsta.WEDGE64)
+    e64["src"], e64["dst"], e64["w"] = e["src"], e["dst"], e["w"]
+    got = kamsta.boruvka_wedge64(e64, n=2000)
+    ref, w = oracle.kruskal(e, 2000)
+    assert int(got["w"].sum()) == w
+    a = (got["src"].astype(np.uint64) << np.uint64(32)) | got["dst"]
+    assert np.array_equal(np.sort(a), oracle.canon_keys(ref))
+
+
+def test_sort_output_flag(kamsta, oracle):
+    e = oracle.gen_gnm(4000, 40000, 32)
+    got = kamsta.boruvka(e, kamsta.AlgorithmConfig(sort_output=True), n=4000)
+    key = (got["src"].astype(np.uint64) << np.uint64(32)) | got["dst"]
+    assert np.all(np.diff(key) > 0)
+
+
+def test_device_entry_point_and_generator(kamsta, oracle):
+    import torch
+    n, m, seed = 1 << 15, 1 << 18, 77
+    ctx = kamsta.Context(0)
+    d = torch.empty((2 * m, 3), dtype=torch.int32, device="cuda")
+    assert ctx.gen_gnm_dev(n, m, seed, 254, d.data_ptr()) == 2 * m
+    torch.cuda.synchronize()
+    host = d.cpu().numpy().view(np.uint32).reshape(-1).view(kamsta.WEDGE)
+    ref_edges = oracle.gen_gnm(n, m, seed)
+    assert np.array_equal(host, ref_edges)  # device generator == oracle generator
+    out = torch.empty((n, 3), dtype=torch.int32, device="cuda")
+    stats = {}
+    k = ctx.boruvka_dev(d.data_ptr(), 2 * m, n, out.data_ptr(),
+                        kamsta.AlgorithmConfig(local_preprocessing=1),
+                        stream=torch.cuda.current_stream().cuda_stream, stats=stats)
+    got = out[:k].cpu().numpy().view(np.uint32).reshape(-1).view(kamsta.WEDGE)
+    _check(oracle, got, ref_edges, n)
+    assert stats["gpu_launches"] > 0 and stats["device_ms"] > 0
+    ctx.close()
+
+
+@pytest.mark.parametrize("n,m", [(1 << 10, 1 << 14), (1 << 20, 1 << 24)])
+def test_device_generator_matches_oracle(kamsta, oracle, n, m):
+    import torch
+    ctx = kamsta.Context(0)
+    d = torch.empty((2 * m, 3), dtype=torch.int32, device="cuda")
+    ctx.gen_gnm_dev(n, m, 5, 254, d.data_ptr())
+    torch.cuda.synchronize()
+    host = d.cpu().numpy().view(np.uint32).reshape(-1).view(kamsta.WEDGE)
+    assert np.array_equal(host, oracle.gen_gnm(n, m, 5))
+
+
+@pytest.mark.parametrize("algo", ALGOS)
+def test_exactness_n22_m26(kamsta, oracle, algo):
+    """The bit-exact check size of the large configuration: G(n=2^22, m=2^26)."""
+    fn, cfg = _configs(kamsta)[algo]
+    n, m = 1 << 22, 1 << 26
+    e = oracle.gen_gnm(n, m, 2026)
+    _check(oracle, fn(e, cfg, n=n), e, n)
