@@ -1,0 +1,370 @@
+#!/usr/bin/env python3
+"""MST throughput benchmark: directed edges per second on G(n=2^26, m=2^30).
+
+Workload: plain Boruvka on one large graph -- hybridMST::boruvka with the
+reference benchmark's default local_kernelization_level=1 (MODIFIED_BORUVKA,
+benchmarks/mst_benchmarks.hpp:84) -- on a seeded G(n, m) with weights uniform
+in [1, 254], stored in both directions (2^31 directed 12-byte entries).  A
+"step" is one full MSF solve; `value` = directed entries / solve time with the
+input already in HBM, `e2e` = the same through the host-buffer C ABI call
+(pinned host input, H2D + solve + D2H of the forest inside the timed region).
+The input (24 GiB) is far larger than L2, so no flush is needed between steps.
+
+--impl reference times the CPU restatement of the reference's own local
+filter-Boruvka (oracle/, OpenMP, all host cores) on a bounded sample of the
+same workload family.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MST edges/s (GNM n=2^26,m=2^30); batched graphs/s + p99 latency vs plain"
+UNIT = "directed edges/s"
+PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC_PATH = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse_args():
+    p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["kamsta", "reference"], default="kamsta")
+    p.add_argument("--log-n", type=int, default=26)
+    p.add_argument("--log-m", type=int, default=30)
+    p.add_argument("--seed", type=int, default=2026)
+    p.add_argument("--local-preprocessing", type=int, default=1)
+    p.add_argument("--sample-log-n", type=int, default=22, help="CPU sample graph size")
+    p.add_argument("--sample-log-m", type=int, default=26)
+    p.add_argument("--cpu-runs", type=int, default=3)
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-variants", action="store_true")
+    return p.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self._t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self._t = threading.Thread(target=self._read, daemon=True)
+        self._t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self._t:
+            self._t.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def load_peak():
+    try:
+        with open(PEAKS_PATH) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def load_traffic(kernel: str):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary."""
+    try:
+        with open(TRAFFIC_PATH) as f:
+            t = json.load(f)
+        e = t.get(kernel)
+        return (float(e["bytes_per_launch"]), e.get("source")) if e else (None, None)
+    except Exception:
+        return None, None
+
+
+def cpu_port_baseline(n: int, m: int, seed: int, runs: int, warmup: int = 1):
+    """Time the oracle port (restated reference local filter-Boruvka)."""
+    from tests import _oracle as O
+    edges = O.gen_gnm(n, m, seed)
+    threads = O.lib().oracle_max_threads()
+    times = []
+    res = None
+    for i in range(warmup + runs):
+        t0 = time.perf_counter()
+        res = O.boruvka_filter(edges, n, 0)
+        dt = time.perf_counter() - t0
+        if i >= warmup:
+            times.append(dt)
+    return edges, res, times, threads
+
+
+def run_reference(args, rep):
+    """--impl reference: rank 0 times the CPU restatement; others exit."""
+    if rep.rank != 0:
+        return 0
+    n, m = 1 << args.sample_log_n, 1 << args.sample_log_m
+    from tests import _oracle as O
+    edges = O.gen_gnm(n, m, args.seed)
+    threads = O.lib().oracle_max_threads()
+    times = []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        O.boruvka_filter(edges, n, 0)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+    per = statistics.median(times)
+    value = 2 * m / per
+    sample = (f"GNM n=2^{args.sample_log_n} m=2^{args.sample_log_m} seed={args.seed} "
+              f"(1/{(1 << (args.log_m - args.sample_log_m))} of the n=2^{args.log_n} m=2^{args.log_m} "
+              f"workload), median of {args.steps} runs")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded G(n,m), uniform weights [1,254])",
+        "config": {"workload": f"GNM n=2^{args.sample_log_n} m=2^{args.sample_log_m} (bounded sample)",
+                   "algorithm": "restated reference local filter-Boruvka (boruvka_filter), OpenMP",
+                   "threads": threads},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": ("the reference cannot be compiled here (MPI, TBB and all git submodules absent); "
+                 "this arm is the oracle's line-by-line restatement of its local filter-Boruvka"),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse_args()
+    from kamsta_gb300.replicas import Replicas
+    rep = Replicas()
+    if args.impl == "reference":
+        rc = run_reference(args, rep)
+        rep.close()
+        return rc
+
+    import numpy as np
+    import torch
+    import kamsta_gb300 as K
+    from kamsta_gb300 import build as kbuild
+    kbuild.build()
+
+    dev = rep.local_rank
+    torch.cuda.set_device(dev)
+    n, m = 1 << args.log_n, 1 << args.log_m
+    md = 2 * m
+    ctx = K.Context(dev)
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    d_edges = torch.empty((md, 3), dtype=torch.int32, device="cuda")
+    d_out = torch.empty((n, 3), dtype=torch.int32, device="cuda")
+    seed = args.seed + rep.rank
+    got = ctx.gen_gnm_dev(n, m, seed, 254, d_edges.data_ptr(), stream=sh)
+    assert got == md
+    torch.cuda.synchronize()
+
+    cfg = K.AlgorithmConfig(local_preprocessing=K.LocalPreprocessing(args.local_preprocessing))
+    results = []
+
+    def step(stats=None):
+        k = ctx.boruvka_dev(d_edges.data_ptr(), md, n, d_out.data_ptr(), cfg, stream=sh, stats=stats)
+        results.append(k)
+        return k
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # ---- timed region: K solves with the input resident in HBM
+    clocks = ClockSampler(dev)
+    clocks.start()
+    per_step = []
+    rep.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        st = {}
+        step(st)
+        per_step.append(st)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    rep.barrier()
+    clk = clocks.stop()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    max_ms = rep.max(elapsed_ms)
+    ms_per_step = max_ms / args.steps
+    value = args.gpus * md * args.steps / (max_ms / 1e3)
+    forest = results[-1]
+    weights = {s["total_weight"] for s in per_step}
+    assert len(set(results)) == 1 and len(weights) == 1, "non-deterministic forest"
+    launches = sum(s["gpu_launches"] for s in per_step)
+
+    # ---- roofline of the dominant kernel (live CUDA-event phase timings)
+    phases = {}
+    for s in per_step:
+        for name, ph in s["phases"].items():
+            a = phases.setdefault(name, {"ms": 0.0, "bytes": 0, "launches": 0})
+            a["ms"] += ph["ms"]
+            a["bytes"] += ph["bytes"]
+            a["launches"] += ph["launches"]
+    dom = "first_pass"
+    fp = phases[dom]
+    launch_ms = fp["ms"] / max(fp["launches"], 1)
+    bytes_per_launch = fp["bytes"] / max(fp["launches"], 1)
+    achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9 if launch_ms > 0 else 0.0
+    peak, peak_src = load_peak()
+    traffic, traffic_src = load_traffic("k_edge_pass_dir")
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic,
+                "kernel": "k_edge_pass_dir (first pass over the directed input)",
+                "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
+                else "fallback 6.8 TB/s",
+                "alg_bytes_per_launch": bytes_per_launch, "launch_ms": launch_ms,
+                "traffic_source": traffic_src}
+    solve_total = {k: round(v["ms"] / args.steps, 4) for k, v in phases.items()}
+    whole = sum(s["alg_bytes"] for s in per_step) / args.steps
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded G(n,m) generated on device, uniform weights [1,254])",
+        "config": {"workload": f"GNM n=2^{args.log_n} m=2^{args.log_m} (2^{args.log_m + 1} directed "
+                               "12-byte entries), single graph",
+                   "algorithm": "boruvka (hybridBoruvka), local_preprocessing="
+                                f"{args.local_preprocessing} (reference benchmark default 1)",
+                   "l2": "input (24 GiB) >> L2 (129 MB); no flush needed",
+                   "parallelism": f"replicas x{args.gpus}"},
+        "forest_edges": forest, "forest_weight": per_step[-1]["total_weight"],
+        "gpu_launches": launches, "roofline": roofline, "clocks": clk,
+        "phase_ms_per_step": solve_total,
+        "whole_solve_alg_gbs": whole / (ms_per_step / 1e3) / 1e9,
+    }
+
+    # ---- variant: plain rounds without the filter preprocessing
+    if not args.no_variants:
+        cfg0 = K.AlgorithmConfig(local_preprocessing=K.LocalPreprocessing.NO_PREPROCESSING)
+        ctx.boruvka_dev(d_edges.data_ptr(), md, n, d_out.data_ptr(), cfg0, stream=sh)
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        st0 = {}
+        k0 = ctx.boruvka_dev(d_edges.data_ptr(), md, n, d_out.data_ptr(), cfg0, stream=sh, stats=st0)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        ms0 = t0.elapsed_time(t1)
+        assert k0 == forest and st0["total_weight"] == per_step[-1]["total_weight"]
+        line["variants"] = {"no_preprocessing": {"value": md / (ms0 / 1e3), "ms_per_step": ms0,
+                                                 "rounds": st0["rounds"]}}
+
+    # ---- e2e through the host-buffer C ABI call (pinned host input)
+    if not args.no_e2e:
+        h_edges = torch.empty((md, 3), dtype=torch.int32, pin_memory=True)
+        h_edges.copy_(d_edges)
+        host = h_edges.numpy().view(np.uint32).reshape(-1).view(K.WEDGE)
+        out = np.empty(n, K.WEDGE)
+        cfgc = cfg.to_c()
+        L = K.lib()
+        cnt = C.c_uint64()
+        stc = K.Stats()
+
+        def e2e_step():
+            K.check(L.kamsta_mst_boruvka(host.ctypes.data_as(C.c_void_p), md, n, C.byref(cfgc),
+                                         out.ctypes.data_as(C.c_void_p), C.byref(cnt), C.byref(stc)))
+            return int(cnt.value)
+
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        rep.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            ke = e2e_step()
+        dt = time.perf_counter() - t0
+        dt = rep.max(dt)
+        assert ke == forest and stc.total_weight == per_step[-1]["total_weight"]
+        line["e2e"] = {"value": args.gpus * md * args.steps / dt, "unit": UNIT,
+                       "h2d_bytes_per_step": md * 12, "d2h_bytes_per_step": ke * 12,
+                       "ms_per_step": dt / args.steps * 1e3,
+                       "api": "kamsta_mst_boruvka (host buffers, pinned input)"}
+        del h_edges
+
+    # ---- CPU baseline (rank 0, N=1 only): restated reference on a sample
+    if not args.no_cpu_baseline and rep.rank == 0 and args.gpus == 1:
+        sn, sm = 1 << args.sample_log_n, 1 << args.sample_log_m
+        edges_s, res, times, threads = cpu_port_baseline(sn, sm, args.seed, args.cpu_runs)
+        per = statistics.median(times)
+        # the GPU on the same sample, for the record
+        d_s = torch.from_numpy(edges_s.view(np.uint32).reshape(-1, 3).view(np.int32)).cuda()
+        d_o = torch.empty((sn, 3), dtype=torch.int32, device="cuda")
+        ks = ctx.boruvka_dev(d_s.data_ptr(), 2 * sm, sn, d_o.data_ptr(), cfg, stream=sh)
+        sts = {}
+        ks = ctx.boruvka_dev(d_s.data_ptr(), 2 * sm, sn, d_o.data_ptr(), cfg, stream=sh, stats=sts)
+        assert ks == len(res[0]) and sts["total_weight"] == res[1], "GPU/CPU forest mismatch"
+        line["cpu_baseline"] = {
+            "value": 2 * sm / per, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"GNM n=2^{args.sample_log_n} m=2^{args.sample_log_m} seed={args.seed}, "
+                      f"median of {len(times)} runs ({per:.3f} s each)",
+            "gpu_same_sample_ms": sts["device_ms"]}
+    if rep.rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    rep.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

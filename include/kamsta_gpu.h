@@ -100,6 +100,16 @@ typedef struct kamsta_cfg {
 } kamsta_cfg;
 
 #define KAMSTA_TRACE_MAX 128
+/* Phases timed in kamsta_stats (device time from CUDA events). */
+#define KAMSTA_PHASE_PLAN 0         /* weight sampling for the pivots        */
+#define KAMSTA_PHASE_FIRST_PASS 1   /* one streaming pass over the input     */
+#define KAMSTA_PHASE_ROUND_EDGES 2  /* relabel + compact + next minimum      */
+#define KAMSTA_PHASE_ROUND_VERTS 3  /* hook, jump, renumber, map             */
+#define KAMSTA_PHASE_CLASS_PASS 4   /* relabel/filter of heavier classes     */
+#define KAMSTA_PHASE_FINALIZE 5     /* component labels after a Boruvka call */
+#define KAMSTA_PHASE_EMIT 6         /* forest output                         */
+#define KAMSTA_PHASE_DEDUPE 7       /* parallel-edge removal (radix sort)    */
+#define KAMSTA_PHASES 8
 typedef struct kamsta_stats {
   uint64_t num_mst_edges;  /* forest edges written                         */
   uint64_t total_weight;   /* sum of forest edge weights                   */
@@ -113,6 +123,9 @@ typedef struct kamsta_stats {
   uint32_t pad_;
   uint64_t trace_m[KAMSTA_TRACE_MAX]; /* live undirected edges per round   */
   uint64_t trace_n[KAMSTA_TRACE_MAX]; /* live vertices per round           */
+  double phase_ms[KAMSTA_PHASES];     /* device time per phase             */
+  uint64_t phase_bytes[KAMSTA_PHASES];/* algorithmic bytes per phase       */
+  uint32_t phase_launches[KAMSTA_PHASES];
 } kamsta_stats;
 
 /* Fills cfg with AlgorithmConfig's defaults: NO_PREPROCESSING,

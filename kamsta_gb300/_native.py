@@ -24,6 +24,8 @@ FLAG_DEDUPE_NEVER = 0x4
 FLAG_DEDUPE_ALWAYS = 0x8
 FLAG_TRACE = 0x10
 TRACE_MAX = 128
+PHASES = ["plan", "first_pass", "round_edges", "round_verts", "class_pass", "finalize", "emit",
+          "dedupe"]
 
 # numpy views of the edge layouts
 WEDGE = np.dtype([("src", "<u4"), ("dst", "<u4"), ("w", "<u4")])          # kamsta_wedge
@@ -49,12 +51,17 @@ class Stats(C.Structure):
                 ("dedupe_passes", C.c_uint32), ("gpu_launches", C.c_uint32),
                 ("device_ms", C.c_double), ("alg_bytes", C.c_uint64),
                 ("trace_len", C.c_uint32), ("pad_", C.c_uint32),
-                ("trace_m", C.c_uint64 * TRACE_MAX), ("trace_n", C.c_uint64 * TRACE_MAX)]
+                ("trace_m", C.c_uint64 * TRACE_MAX), ("trace_n", C.c_uint64 * TRACE_MAX),
+                ("phase_ms", C.c_double * len(PHASES)), ("phase_bytes", C.c_uint64 * len(PHASES)),
+                ("phase_launches", C.c_uint32 * len(PHASES))]
 
     def as_dict(self) -> dict:
-        d = {k: getattr(self, k) for k, _ in self._fields_
-             if k not in ("trace_m", "trace_n", "pad_")}
+        skip = ("trace_m", "trace_n", "pad_", "phase_ms", "phase_bytes", "phase_launches")
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in skip}
         d["trace"] = [(int(self.trace_m[i]), int(self.trace_n[i])) for i in range(self.trace_len)]
+        d["phases"] = {name: {"ms": float(self.phase_ms[i]), "bytes": int(self.phase_bytes[i]),
+                              "launches": int(self.phase_launches[i])}
+                       for i, name in enumerate(PHASES)}
         return d
 
 

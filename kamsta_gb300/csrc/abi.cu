@@ -58,13 +58,6 @@ struct DefaultCtx {
 };
 thread_local DefaultCtx g_default;
 
-struct DevBuf {
-  void* p = nullptr;
-  ~DevBuf() {
-    if (p) cudaFree(p);
-  }
-};
-
 kamsta_status solve_host(Algo algo, const kamsta_wedge* edges, uint64_t m, uint32_t n,
                          const kamsta_cfg* cfg, kamsta_wedge* out, uint64_t* out_count,
                          kamsta_stats* stats) {
@@ -82,20 +75,20 @@ kamsta_status solve_host(Algo algo, const kamsta_wedge* edges, uint64_t m, uint3
   *out_count = 0;
   if (stats) std::memset(stats, 0, sizeof(*stats));
   if (m == 0 || n == 0) return KAMSTA_OK;
-  DevBuf din, dout;
-  cudaError_t e = cudaMalloc(&din.p, m * sizeof(kamsta_wedge));
-  if (e != cudaSuccess) return cuda_status(e, "cudaMalloc(input)");
-  e = cudaMalloc(&dout.p, std::max<uint64_t>(n, 1) * sizeof(kamsta_wedge));
-  if (e != cudaSuccess) return cuda_status(e, "cudaMalloc(output)");
-  e = cudaMemcpyAsync(din.p, edges, m * sizeof(kamsta_wedge), cudaMemcpyHostToDevice,
-                      ctx->stream);
+  // device copies of input and output live in the context's grow-only io pool
+  const size_t in_bytes = (m * sizeof(kamsta_wedge) + 255) & ~size_t(255);
+  const size_t out_bytes = std::max<uint64_t>(n, 1) * sizeof(kamsta_wedge);
+  cudaError_t e = ctx->io.reserve(in_bytes + out_bytes + 256);
+  if (e != cudaSuccess) return cuda_status(e, "device buffers for host input");
+  kamsta_wedge* din = ctx->io.take<kamsta_wedge>(m);
+  kamsta_wedge* dout = ctx->io.take<kamsta_wedge>(std::max<uint64_t>(n, 1));
+  e = cudaMemcpyAsync(din, edges, m * sizeof(kamsta_wedge), cudaMemcpyHostToDevice, ctx->stream);
   if (e != cudaSuccess) return cuda_status(e, "cudaMemcpyAsync(H2D)");
   SolveOut so;
-  s = solve_device(ctx, algo, static_cast<const kamsta_wedge*>(din.p), m, n, c,
-                   static_cast<kamsta_wedge*>(dout.p), &so, stats, ctx->stream);
+  s = solve_device(ctx, algo, din, m, n, c, dout, &so, stats, ctx->stream);
   if (s != KAMSTA_OK) return s;
   if (so.count) {
-    e = cudaMemcpyAsync(out, dout.p, so.count * sizeof(kamsta_wedge), cudaMemcpyDeviceToHost,
+    e = cudaMemcpyAsync(out, dout, so.count * sizeof(kamsta_wedge), cudaMemcpyDeviceToHost,
                         ctx->stream);
     if (e != cudaSuccess) return cuda_status(e, "cudaMemcpyAsync(D2H)");
   }
@@ -176,6 +169,22 @@ kamsta_status kamsta_ctx_create(int device, kamsta_ctx** out) {
       (e = cudaEventCreate(&c->ev1)) != cudaSuccess) {
     s = cuda_status(e, "kamsta_ctx_create");
   }
+  for (int i = 0; s == KAMSTA_OK && i < kTimerEvents; ++i)
+    if ((e = cudaEventCreate(&c->tev[i])) != cudaSuccess) s = cuda_status(e, "cudaEventCreate");
+  if (s == KAMSTA_OK) {
+    // a private stream-ordered pool for edge lists; it keeps its memory
+    // between calls (release threshold = unlimited) until kamsta_ctx_trim
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    if ((e = cudaMemPoolCreate(&c->pool, &props)) != cudaSuccess) {
+      s = cuda_status(e, "cudaMemPoolCreate");
+    } else {
+      uint64_t thr = ~0ull;
+      cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+  }
   cudaSetDevice(prev);
   if (s != KAMSTA_OK) {
     kamsta_ctx_destroy(c.release());
@@ -192,7 +201,7 @@ kamsta_status kamsta_ctx_destroy(kamsta_ctx* ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   ctx->fixed.release();
-  ctx->edges.release();
+  if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
   if (ctx->d_counters) cudaFree(ctx->d_counters);
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->d_samples) cudaFree(ctx->d_samples);
@@ -200,6 +209,9 @@ kamsta_status kamsta_ctx_destroy(kamsta_ctx* ctx) {
   if (ctx->h_err) cudaFreeHost(ctx->h_err);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  for (int i = 0; i < kTimerEvents; ++i)
+    if (ctx->tev[i]) cudaEventDestroy(ctx->tev[i]);
+  ctx->io.release();
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   cudaSetDevice(prev);
   delete ctx;
@@ -210,12 +222,19 @@ kamsta_status kamsta_ctx_trim(kamsta_ctx* ctx) {
   if (!ctx) return KAMSTA_E_INPUT;
   std::lock_guard<std::mutex> lock(ctx->mu);
   ctx->fixed.release();
-  ctx->edges.release();
+  ctx->io.release();
+  if (ctx->pool) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaMemPoolTrimTo(ctx->pool, 0);
+  }
   return KAMSTA_OK;
 }
 
 uint64_t kamsta_ctx_pool_bytes(const kamsta_ctx* ctx) {
-  return ctx ? ctx->fixed.cap + ctx->edges.cap : 0;
+  if (!ctx) return 0;
+  uint64_t pool = 0;
+  if (ctx->pool) cudaMemPoolGetAttribute(ctx->pool, cudaMemPoolAttrReservedMemCurrent, &pool);
+  return ctx->fixed.cap + ctx->io.cap + pool;
 }
 
 kamsta_status kamsta_mst_boruvka(const kamsta_wedge* edges, uint64_t m, uint32_t n,

@@ -67,11 +67,21 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
   return m;
 }
 
-// 64-bit minimum with a read first: most candidates lose against the value
-// already stored, so they never issue the atomic (keeps hub vertices from
-// serialising the L2 atomic unit).  Correct under any interleaving.
-__device__ __forceinline__ void min_update(uint64_t* p, uint64_t v) {
-  if (v < ld_relaxed(p)) atomicMin(reinterpret_cast<unsigned long long*>(p), v);
+// 64-bit minimum as a fire-and-forget reduction (red.min): the issuing
+// thread never waits for the L2 round trip.  Right when few updates share
+// an address (original vertex ids).
+__device__ __forceinline__ void red_min(uint64_t* p, uint64_t v) {
+  asm volatile("red.relaxed.gpu.global.min.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+// Weak (L1-cacheable) read of a minimum word.  Used only as a filter before
+// red_min: the stored value never increases, so a stale read is an upper
+// bound and can only let through an unnecessary update, never drop a
+// needed one.  Contracted graphs have hub components (degree up to m), and
+// without the filter their updates would serialise on one L2 address.
+__device__ __forceinline__ uint64_t ld_weak(const uint64_t* p) {
+  uint64_t v;
+  asm volatile("ld.weak.global.ca.u64 %0, [%1];" : "=l"(v) : "l"(p));
+  return v;
 }
 
 // SplitMix64's output function (Steele, Lea, Flood 2014): the counter-based
@@ -102,8 +112,12 @@ constexpr uint64_t kLbVal = (1ull << 62) - 1;
 
 // Called by all 32 lanes of one warp.  Returns the exclusive prefix of
 // `tile` (same value in every lane) and publishes its inclusive prefix.
+// Each poll reads 256 predecessors (8 per lane, nearest first), so a tile
+// usually reaches an inclusive prefix of the previous wave of CTAs in one
+// or two polls instead of walking back 32 tiles at a time.
 __device__ __forceinline__ uint64_t lookback(uint64_t* status, uint32_t tile,
                                              uint64_t local, uint32_t* err) {
+  constexpr int kPer = 8;
   const uint32_t lane = lane_id();
   if (tile == 0) {
     if (lane == 0) st_relaxed(&status[0], kLbInc | local);
@@ -114,27 +128,93 @@ __device__ __forceinline__ uint64_t lookback(uint64_t* status, uint32_t tile,
   int64_t window = static_cast<int64_t>(tile) - 1;
   uint32_t spins = 0;
   for (;;) {
-    const int64_t idx = window - static_cast<int64_t>(lane);
-    const uint64_t s = idx >= 0 ? ld_relaxed(&status[idx]) : kLbInc;
-    const uint32_t flag = static_cast<uint32_t>(s >> 62);
-    const uint32_t inc = __ballot_sync(kFull, flag == 2);
-    const uint32_t empty = __ballot_sync(kFull, flag == 0);
+    uint64_t s[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+      const int64_t idx = window - static_cast<int64_t>(lane) * kPer - k;
+      s[k] = idx >= 0 ? ld_relaxed(&status[idx]) : kLbInc;
+    }
+    int first_inc = kPer;
+    bool empty_before = false;
+    uint64_t partial = 0;
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+      if (first_inc == kPer) {
+        const uint32_t flag = static_cast<uint32_t>(s[k] >> 62);
+        if (flag == 0) empty_before = true;
+        partial += s[k] & kLbVal;
+        if (flag == 2) first_inc = k;
+      }
+    }
+    const uint32_t inc = __ballot_sync(kFull, first_inc < kPer);
     const uint32_t limit = inc ? static_cast<uint32_t>(__ffs(inc) - 1) : 31u;
     const uint32_t relevant = limit == 31u ? kFull : ((2u << limit) - 1u);
-    if (empty & relevant) {
+    const uint32_t bad = __ballot_sync(kFull, empty_before) & relevant;
+    if (bad) {
       if (++spins > kSpinCap) {
         if (lane == 0) atomicOr(err, kErrLookback);
         break;
       }
-      __nanosleep(20);
+      __nanosleep(32);
       continue;
     }
-    excl += warp_sum(lane <= limit ? (s & kLbVal) : 0ull);
+    excl += warp_sum(lane <= limit ? partial : 0ull);
     if (inc) break;
-    window -= 32;
+    window -= 32 * kPer;
   }
   if (lane == 0) st_relaxed(&status[tile], kLbInc | (excl + local));
   return excl;
+}
+
+// ---------------------------------------------------------------------------
+// Bulk asynchronous copies (TMA, cp.async.bulk) into shared memory, completed
+// on an mbarrier.  Used to stream input tiles: one elected thread issues the
+// copy of the next tile while the CTA works on the current one.
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// orders this thread's earlier generic-proxy shared-memory accesses before
+// later async-proxy (bulk copy) writes to the same buffer
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// bytes and both addresses must be multiples of 16
+__device__ __forceinline__ void bulk_load(void* smem_dst, const void* gmem_src, uint32_t bytes,
+                                          uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(smem_dst)),
+      "l"(gmem_src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait for phase `parity` of `bar`; false (and kErrSpin) on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t* err) {
+  for (uint32_t i = 0; i < kSpinCap; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  atomicOr(err, kErrSpin);
+  return false;
 }
 
 // ---------------------------------------------------------------------------

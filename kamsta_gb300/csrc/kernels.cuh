@@ -1,14 +1,14 @@
 // kernels.cuh -- device kernels of the Boruvka / filter-Boruvka hot path.
 //
 // Reference steps (KaMSTa tree) and the kernel that replaces each:
-//   compute_min_edges             mst_utils_common.hpp:84-105     -> fused into k_edge_pass
+//   compute_min_edges             mst_utils_common.hpp:84-105     -> fused into k_pass_*
 //   determine_mst_edges(_exhausted) mst_utils_cut_edges.hpp:102-166 -> k_hook
 //   update_parents                gbbs_reimplementation.hpp:161-169 -> k_jump
 //   add_new_mst_edges_to_mst_array gbbs_reimplementation.hpp:137-159 -> k_vertex_scan
 //   compactify_vertices           mst_utils_common.hpp:122-132    -> k_vertex_scan
 //   relabel_edges + filter_out_self_loops  mst_utils_plain.hpp:7-29,
-//                                 mst_utils_common.hpp:157-175    -> k_edge_pass
-//   localMST::partition / filter  mst_utils_filter.hpp:39-126     -> k_edge_pass
+//                                 mst_utils_common.hpp:157-175    -> k_pass_seg
+//   localMST::partition / filter  mst_utils_filter.hpp:39-126     -> k_pass_dir / k_pass_seg
 //   final parent shortcut         local_mst_respecting_cut_edges.hpp:199-203
 //                                                                  -> k_chase + k_relabel_all
 #pragma once
@@ -22,83 +22,62 @@ constexpr int kItemsRec = 8;    // 16-byte records per thread
 constexpr int kItemsVtx = 8;    // vertices per thread in the vertex scans
 constexpr int kMaxOut = 3;      // weight classes materialised by one pass
 
+// ---------------------------------------------------------------------------
+// Segmented edge lists.
+//
+// An edge pass splits its (logical) input into one contiguous chunk per CTA
+// and every CTA appends the records it keeps to its own output segment,
+// `segment * cap + running offset`.  No CTA waits on another (there is no
+// cross-CTA scan), so a pass is a plain stream: the next input tile of a
+// CTA is known in advance and is prefetched by a bulk asynchronous copy
+// (TMA, cp.async.bulk) while the current one is processed.  Segments are
+// laid out in chunk order, so the physical index of a record -- its
+// "position" -- grows with the input's (min, max) order; (w << 32 | position)
+// therefore keeps ordering edges exactly like the reference's (weight,
+// local edge index) key (mst_utils_common.hpp:76-81), gaps and all, and the
+// hook finds a record directly at its position.
+constexpr int kMaxSeg = 1024;  // segments per list (= CTAs of the producing pass)
+
+struct SegIn {  // a list produced by an edge pass
+  const Rec* base;
+  const uint32_t* count;  // records per segment
+  uint64_t cap;           // physical records per segment
+  uint32_t nseg;
+};
+struct SegOut {
+  Rec* base;
+  uint64_t cap;     // records per segment (overflow sets kErrOverflow)
+  uint32_t* count;  // written at the end: records kept per segment
+};
+
 // Parameters of one edge pass.  Items are kept when their weight lies in
 // [wmin, wmax], their relabelled endpoints differ, and (for the directed
 // input) src < dst.  The class of a kept item is the first c with w <= thr[c]
 // (c < nout-1), else nout-1.  Class 0 optionally feeds the next round's
-// minimum (minval) with the value (w << 32 | output position).
-struct EdgePassArgs {
+// minimum (minval) with the value (w << 32 | position).
+struct PassArgs {
   const uint32_t* map;  // label map; nullptr = identity
-  uint32_t wmin, wmax;  // keep wmin <= w <= wmax
+  uint32_t wmin, wmax;
   uint32_t thr[kMaxOut];
-  Rec* out[kMaxOut];
-  uint64_t cap[kMaxOut];  // capacity of out[c]; overflow sets kErrOverflow
-  uint64_t* status[kMaxOut];
-  uint64_t* minval;      // nullptr = no fused minimum
-  unsigned long long* counts;  // [kMaxOut] kept per class, [kMaxOut] dropped by weight
-  uint32_t* ticket;
+  SegOut out[kMaxOut];
+  uint64_t* minval;
+  uint32_t min_checked;  // filter minimum updates by a cached read (hub-heavy passes)
+  uint64_t total;  // logical input items
+  uint64_t chunk;  // logical items per CTA (a multiple of the tile size)
+  unsigned long long* counts;  // [0] dropped above wmax, [1] items that reached the map
   uint32_t* err;
-  uint32_t n;            // ids must be < n (directed source)
-  uint32_t validate;     // check id range and (src,dst) order
-  uint32_t aligned16;    // directed source base is 16-byte aligned
-  uint32_t ntiles;
+  uint32_t n;         // ids must be < n (directed source)
+  uint32_t validate;  // check id range and (src,dst) order (directed source)
+  uint32_t aligned16; // directed source base is 16-byte aligned
 };
 
 template <int NOUT>
-__device__ __forceinline__ uint8_t weight_class(uint32_t w, const EdgePassArgs& p) {
+__device__ __forceinline__ uint8_t weight_class(uint32_t w, const PassArgs& p) {
   uint8_t c = NOUT - 1;
 #pragma unroll
   for (int k = NOUT - 2; k >= 0; --k)
     if (w <= p.thr[k]) c = static_cast<uint8_t>(k);
   return c;
-}
-
-// Publish per-class look-back and counts, then scatter.  Shared by both
-// sources.  a/b/w/oid/cls hold the tile's items.
-template <int NOUT, int ITEMS>
-__device__ __forceinline__ void edge_pass_finish(
-    uint32_t tile, const uint32_t (&a)[ITEMS], const uint32_t (&b)[ITEMS],
-    const uint32_t (&w)[ITEMS], const uint32_t (&oid)[ITEMS],
-    const uint8_t (&cls)[ITEMS], uint32_t dropped_w, const EdgePassArgs& p) {
-  __shared__ uint32_t s_rank[NOUT * ITEMS * (kBlock / 32)];
-  __shared__ uint32_t s_tot[NOUT];
-  __shared__ uint64_t s_pre[NOUT];
-  uint32_t offs[ITEMS];
-#pragma unroll
-  for (int j = 0; j < ITEMS; ++j) offs[j] = 0;
-  tile_rank<NOUT, ITEMS, kBlock>(cls, offs, s_rank, s_tot);
-  const uint32_t warp = threadIdx.x >> 5;
-  if (warp < NOUT) {
-    const uint64_t pre = lookback(p.status[warp], tile, s_tot[warp], p.err);
-    if (lane_id() == 0) {
-      s_pre[warp] = pre;
-      if (s_tot[warp]) atomicAdd(&p.counts[warp], static_cast<unsigned long long>(s_tot[warp]));
-    }
-  }
-  // weight-dropped count (for the unmaterialised class)
-  const uint32_t dsum = warp_sum(dropped_w);
-  if (lane_id() == 0 && dsum) atomicAdd(&p.counts[kMaxOut], static_cast<unsigned long long>(dsum));
-  __syncthreads();
-#pragma unroll
-  for (int j = 0; j < ITEMS; ++j) {
-    if (cls[j] == 0xff) continue;
-    const uint64_t pos = s_pre[cls[j]] + offs[j];
-    if (pos >= p.cap[cls[j]]) {
-      atomicOr(p.err, kErrOverflow);
-      continue;
-    }
-    Rec r;
-    r.a = a[j];
-    r.b = b[j];
-    r.w = w[j];
-    r.oid = oid[j];
-    p.out[cls[j]][pos] = r;
-    if (cls[j] == 0 && p.minval != nullptr) {
-      const uint64_t v = (static_cast<uint64_t>(w[j]) << 32) | pos;
-      min_update(&p.minval[a[j]], v);
-      min_update(&p.minval[b[j]], v);
-    }
-  }
 }
 
 __device__ __forceinline__ uint32_t next_tile(uint32_t* ticket) {
@@ -109,116 +88,367 @@ __device__ __forceinline__ uint32_t next_tile(uint32_t* ticket) {
   return s_tile;
 }
 
-// Edge pass over the caller's directed input (12-byte records, (src,dst)
-// sorted, both directions).  Only src < dst copies are candidates; the
-// record's oid is its index in the input.  The tile is staged through shared
-// memory with 16-byte loads (coalesced), then read back per item.
-template <int NOUT>
-__global__ void __launch_bounds__(kBlock)
-    k_edge_pass_dir(const uint32_t* __restrict__ in, uint64_t m, EdgePassArgs p) {
-  constexpr int TILE = kItemsDir * kBlock;
-  __shared__ __align__(16) uint32_t s_words[TILE * 3];
-  for (;;) {
-    const uint32_t tile = next_tile(p.ticket);
-    if (tile >= p.ntiles) return;
-    const uint64_t base = static_cast<uint64_t>(tile) * TILE;
-    const uint32_t cnt = static_cast<uint32_t>(m - base < TILE ? m - base : TILE);
-    const uint32_t words = cnt * 3;
-    const uint32_t* src = in + base * 3;
-    if (p.aligned16) {
-      const uint32_t nvec = words >> 2;
-      const uint4* src4 = reinterpret_cast<const uint4*>(src);
-      uint4* dst4 = reinterpret_cast<uint4*>(s_words);
-      for (uint32_t i = threadIdx.x; i < nvec; i += kBlock) dst4[i] = __ldcs(src4 + i);
-      for (uint32_t i = (nvec << 2) + threadIdx.x; i < words; i += kBlock) s_words[i] = src[i];
-    } else {
-      for (uint32_t i = threadIdx.x; i < words; i += kBlock) s_words[i] = src[i];
-    }
-    __syncthreads();
-    uint32_t a[kItemsDir], b[kItemsDir], w[kItemsDir], oid[kItemsDir];
-    uint8_t cls[kItemsDir];
-    uint32_t dropped_w = 0;
+// Rank the tile's kept items (stable), append them to this CTA's output
+// segments and feed the fused minimum.  rec(t) returns tile item t from
+// shared memory.  run[] holds the CTA's running segment sizes (the same in
+// every thread).  Class loops are unrolled so no array is indexed at run
+// time.  Minimum updates of a checked pass first read all their current
+// values, then issue the reductions, so a thread waits for at most one
+// memory round trip per tile.
+template <int NOUT, int ITEMS, typename RecAt>
+__device__ __forceinline__ void seg_tile_finish(const uint8_t (&cls)[ITEMS], uint64_t (&run)[NOUT],
+                                                const PassArgs& p, RecAt rec) {
+  __shared__ uint32_t s_rank[NOUT * ITEMS * (kBlock / 32)];
+  __shared__ uint32_t s_tot[NOUT];
+  uint32_t offs[ITEMS];
 #pragma unroll
-    for (int j = 0; j < kItemsDir; ++j) {
-      const uint32_t t = j * kBlock + threadIdx.x;
-      cls[j] = 0xff;
-      a[j] = b[j] = w[j] = 0;
-      oid[j] = static_cast<uint32_t>(base + t);
-      if (t >= cnt) continue;
-      const uint32_t s = s_words[3 * t], d = s_words[3 * t + 1], wt = s_words[3 * t + 2];
-      if (p.validate) {
+  for (int j = 0; j < ITEMS; ++j) offs[j] = 0;
+  tile_rank<NOUT, ITEMS, kBlock>(cls, offs, s_rank, s_tot);
+  uint32_t min_mask = 0;  // class-0 items whose minimum must be fed
+#pragma unroll
+  for (int c = 0; c < NOUT; ++c) {
+    const uint64_t cap = p.out[c].cap;
+    Rec* const seg = p.out[c].base + static_cast<uint64_t>(blockIdx.x) * cap;
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) {
+      if (cls[j] != c) continue;
+      const uint64_t local = run[c] + offs[j];
+      if (local >= cap) {
+        atomicOr(p.err, kErrOverflow);
+        continue;
+      }
+      seg[local] = rec(j * kBlock + threadIdx.x);
+      if (c == 0) min_mask |= 1u << j;
+    }
+  }
+  if (p.minval != nullptr && min_mask) {
+    const uint64_t seg0 = static_cast<uint64_t>(blockIdx.x) * p.out[0].cap + run[0];
+    if (!p.min_checked) {
+#pragma unroll
+      for (int j = 0; j < ITEMS; ++j) {
+        if (!((min_mask >> j) & 1u)) continue;
+        const Rec r = rec(j * kBlock + threadIdx.x);
+        const uint64_t v = (static_cast<uint64_t>(r.w) << 32) | (seg0 + offs[j]);
+        red_min(&p.minval[r.a], v);
+        red_min(&p.minval[r.b], v);
+      }
+    } else {
+      constexpr int G = 4;  // items per batch of filter reads
+#pragma unroll
+      for (int g = 0; g < ITEMS; g += G) {
+        uint64_t cur[2 * G];
+#pragma unroll
+        for (int q = 0; q < G && g + q < ITEMS; ++q) {
+          if (!((min_mask >> (g + q)) & 1u)) continue;
+          const Rec r = rec((g + q) * kBlock + threadIdx.x);
+          cur[2 * q] = ld_weak(&p.minval[r.a]);
+          cur[2 * q + 1] = ld_weak(&p.minval[r.b]);
+        }
+#pragma unroll
+        for (int q = 0; q < G && g + q < ITEMS; ++q) {
+          if (!((min_mask >> (g + q)) & 1u)) continue;
+          const Rec r = rec((g + q) * kBlock + threadIdx.x);
+          const uint64_t v = (static_cast<uint64_t>(r.w) << 32) | (seg0 + offs[g + q]);
+          if (v < cur[2 * q]) red_min(&p.minval[r.a], v);
+          if (v < cur[2 * q + 1]) red_min(&p.minval[r.b], v);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < NOUT; ++c) run[c] += s_tot[c];
+}
+
+template <int NOUT>
+__device__ __forceinline__ void seg_pass_end(const uint64_t (&run)[NOUT], uint32_t dropped_w,
+                                             uint32_t cand, const PassArgs& p) {
+  __shared__ uint32_t s_red[2];
+  if (threadIdx.x < 2) s_red[threadIdx.x] = 0;
+  __syncthreads();
+  const uint32_t d = warp_sum(dropped_w), c = warp_sum(cand);
+  if (lane_id() == 0) {
+    if (d) atomicAdd(&s_red[0], d);
+    if (c) atomicAdd(&s_red[1], c);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (s_red[0]) atomicAdd(&p.counts[0], static_cast<unsigned long long>(s_red[0]));
+    if (s_red[1]) atomicAdd(&p.counts[1], static_cast<unsigned long long>(s_red[1]));
+  }
+  // unclamped: a count above cap tells the host the exact size to retry with
+  if (threadIdx.x < NOUT) p.out[threadIdx.x].count[blockIdx.x] = static_cast<uint32_t>(run[threadIdx.x]);
+}
+
+// Edge pass over the caller's directed input (12-byte records, (src,dst)
+// sorted, both directions).  Only src < dst copies are candidates; a
+// record's oid is its index in the input.  Copies need 16-byte multiples:
+// the last tile's ragged tail is read with plain loads; a source that is
+// not 16-byte aligned is read with plain loads throughout.  Striped layout:
+// item j of thread t is tile item j*kBlock + t, so consecutive lanes read
+// consecutive records (conflict-free) and write consecutive output slots.
+constexpr uint32_t kDirTile = kItemsDir * kBlock;
+constexpr uint32_t kDirStageWords = kDirTile * 3;
+constexpr size_t kDirDynSmem = 2 * kDirStageWords * sizeof(uint32_t);
+
+template <int NOUT>
+__global__ void __launch_bounds__(kBlock, 3)
+    k_pass_dir(const uint32_t* __restrict__ in, PassArgs p) {
+  extern __shared__ __align__(128) uint32_t s_words[];  // two stages
+  __shared__ __align__(8) uint64_t s_bar[2];
+  __shared__ uint32_t s_ok;
+  const uint64_t lo = static_cast<uint64_t>(blockIdx.x) * p.chunk;
+  const uint64_t hi = lo + p.chunk < p.total ? lo + p.chunk : p.total;
+  const uint32_t ntile = lo < hi ? static_cast<uint32_t>((hi - lo + kDirTile - 1) / kDirTile) : 0u;
+  const bool tma = p.aligned16 != 0;
+  auto tile_items = [&](uint32_t k) -> uint32_t {
+    const uint64_t b = lo + static_cast<uint64_t>(k) * kDirTile;
+    return static_cast<uint32_t>(hi - b < kDirTile ? hi - b : kDirTile);
+  };
+  auto issue = [&](uint32_t k, int stage) {  // thread 0 only
+    const uint32_t bytes16 = (tile_items(k) * 12u) & ~15u;
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(&s_bar[stage], bytes16);
+    if (bytes16)
+      bulk_load(s_words + stage * kDirStageWords,
+                in + (lo + static_cast<uint64_t>(k) * kDirTile) * 3, bytes16, &s_bar[stage]);
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(&s_bar[0], 1);
+    mbar_init(&s_bar[1], 1);
+    fence_mbar_init();
+    if (tma && ntile > 0) issue(0, 0);
+  }
+  __syncthreads();
+  uint64_t run[NOUT];
+#pragma unroll
+  for (int c = 0; c < NOUT; ++c) run[c] = 0;
+  uint32_t dropped_w = 0, cand = 0;
+  for (uint32_t k = 0; k < ntile; ++k) {
+    const int stage = k & 1;
+    uint32_t* words = s_words + stage * kDirStageWords;
+    const uint64_t base = lo + static_cast<uint64_t>(k) * kDirTile;
+    const uint32_t cnt = tile_items(k);
+    uint32_t first_plain = 0;
+    if (tma) {
+      if (threadIdx.x == 0) s_ok = mbar_wait(&s_bar[stage], (k >> 1) & 1u, p.err) ? 1u : 0u;
+      __syncthreads();  // also: every thread is done with tile k-1 and its stage
+      if (!s_ok) return;
+      if (threadIdx.x == 0 && k + 1 < ntile) issue(k + 1, stage ^ 1);
+      first_plain = ((cnt * 12u) & ~15u) / 4u;
+    } else {
+      __syncthreads();
+    }
+    if (first_plain < cnt * 3) {
+      for (uint32_t i = first_plain + threadIdx.x; i < cnt * 3; i += kBlock)
+        words[i] = in[base * 3 + i];
+      __syncthreads();
+    }
+    if (p.validate) {
+#pragma unroll 1
+      for (int j = 0; j < kItemsDir; ++j) {
+        const uint32_t t = j * kBlock + threadIdx.x;
+        if (t >= cnt) continue;
+        const uint32_t s = words[3 * t], d = words[3 * t + 1];
         if (s >= p.n || d >= p.n) atomicOr(p.err, kErrRange);
-        uint32_t ps, pd;
+        uint32_t ps = 0, pd = 0;
         bool have_prev = true;
         if (t > 0) {
-          ps = s_words[3 * (t - 1)];
-          pd = s_words[3 * (t - 1) + 1];
+          ps = words[3 * (t - 1)];
+          pd = words[3 * (t - 1) + 1];
         } else if (base > 0) {
           ps = in[(base - 1) * 3];
           pd = in[(base - 1) * 3 + 1];
         } else {
           have_prev = false;
-          ps = pd = 0;
         }
         if (have_prev && (s < ps || (s == ps && d <= pd))) atomicOr(p.err, kErrOrder);
       }
-      if (!(s < d) || d >= p.n) continue;
+    }
+    uint8_t cls[kItemsDir];
+#pragma unroll
+    for (int j = 0; j < kItemsDir; ++j) {
+      const uint32_t t = j * kBlock + threadIdx.x;
+      const uint32_t s = words[3 * t], d = words[3 * t + 1], wt = words[3 * t + 2];
+      cls[j] = 0xff;
+      if (t >= cnt || !(s < d) || d >= p.n) continue;
       if (wt < p.wmin || wt > p.wmax) {
         dropped_w += (wt > p.wmax) ? 1u : 0u;
         continue;
       }
-      const uint32_t la = p.map ? p.map[s] : s;
-      const uint32_t lb = p.map ? p.map[d] : d;
-      if (la == lb) continue;
-      a[j] = la;
-      b[j] = lb;
-      w[j] = wt;
+      ++cand;
+      if (p.map) {
+        const uint32_t la = p.map[s], lb = p.map[d];
+        if (la == lb) continue;
+        words[3 * t] = la;  // item t belongs to this thread alone
+        words[3 * t + 1] = lb;
+      }
       cls[j] = weight_class<NOUT>(wt, p);
     }
-    edge_pass_finish<NOUT, kItemsDir>(tile, a, b, w, oid, cls, dropped_w, p);
+    seg_tile_finish<NOUT, kItemsDir>(cls, run, p, [&](uint32_t t) {
+      Rec r;
+      r.a = words[3 * t];
+      r.b = words[3 * t + 1];
+      r.w = words[3 * t + 2];
+      r.oid = static_cast<uint32_t>(base + t);
+      return r;
+    });
   }
+  seg_pass_end<NOUT>(run, dropped_w, cand, p);
 }
 
-// Edge pass over a Rec list (kept in canonical order).
-template <int NOUT>
-__global__ void __launch_bounds__(kBlock)
-    k_edge_pass_rec(const Rec* __restrict__ in, uint64_t m, EdgePassArgs p) {
-  constexpr int TILE = kItemsRec * kBlock;
-  for (;;) {
-    const uint32_t tile = next_tile(p.ticket);
-    if (tile >= p.ntiles) return;
-    const uint64_t base = static_cast<uint64_t>(tile) * TILE;
-    uint32_t a[kItemsRec], b[kItemsRec], w[kItemsRec], oid[kItemsRec];
-    uint8_t cls[kItemsRec];
-    uint32_t dropped_w = 0;
-    Rec r[kItemsRec];
+// Edge pass over a segmented Rec list.  Tile k of a CTA covers logical
+// items [lo + k*T, ...); thread 0 maps them to physical runs (at most a few,
+// as segments hold thousands of records) and copies each run with one bulk
+// copy into the tile's stage.
+constexpr uint32_t kRecTile = kItemsRec * kBlock;
+constexpr size_t kRecDynSmem = 2 * kRecTile * sizeof(Rec);
+constexpr int kMaxRuns = 16;
+
+// prefix[s] = records in segments < s (shared memory), built by the block
+__device__ __forceinline__ void seg_prefix(const SegIn& in, uint64_t* prefix) {
+  __shared__ uint64_t s_part[kBlock / 32];
+  const uint32_t per = (in.nseg + kBlock - 1) / kBlock;  // <= kMaxSeg / kBlock
+  uint64_t loc = 0;
+  for (uint32_t i = 0; i < per; ++i) {
+    const uint32_t s = threadIdx.x * per + i;
+    if (s < in.nseg) loc += in.count[s];
+  }
+  uint64_t incl = loc;
 #pragma unroll
-    for (int j = 0; j < kItemsRec; ++j) {
-      const uint64_t i = base + j * kBlock + threadIdx.x;
-      if (i < m) r[j] = in[i];
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint64_t y = __shfl_up_sync(kFull, incl, o);
+    if (lane_id() >= static_cast<uint32_t>(o)) incl += y;
+  }
+  if (lane_id() == 31) s_part[threadIdx.x >> 5] = incl;
+  __syncthreads();
+  uint64_t wpre = 0;
+  for (uint32_t w = 0; w < (threadIdx.x >> 5); ++w) wpre += s_part[w];
+  uint64_t run = wpre + incl - loc;
+  for (uint32_t i = 0; i < per; ++i) {
+    const uint32_t s = threadIdx.x * per + i;
+    if (s < in.nseg) {
+      prefix[s] = run;
+      run += in.count[s];
     }
+  }
+  if (threadIdx.x == kBlock - 1) prefix[in.nseg] = run;
+  __syncthreads();
+}
+
+// first segment s with prefix[s+1] > x
+__device__ __forceinline__ uint32_t seg_find(const uint64_t* prefix, uint32_t nseg, uint64_t x) {
+  uint32_t lo = 0, hi = nseg;  // answer in [lo, hi)
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (prefix[mid] <= x) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+template <int NOUT>
+__global__ void __launch_bounds__(kBlock, 3)
+    k_pass_seg(SegIn in, PassArgs p) {
+  extern __shared__ __align__(128) Rec s_rec[];  // two stages
+  __shared__ uint64_t s_prefix[kMaxSeg + 1];
+  __shared__ __align__(8) uint64_t s_bar[2];
+  __shared__ uint32_t s_ok, s_plain[2];
+  seg_prefix(in, s_prefix);
+  const uint64_t lo = static_cast<uint64_t>(blockIdx.x) * p.chunk;
+  const uint64_t hi = lo + p.chunk < p.total ? lo + p.chunk : p.total;
+  const uint32_t ntile = lo < hi ? static_cast<uint32_t>((hi - lo + kRecTile - 1) / kRecTile) : 0u;
+  auto tile_items = [&](uint32_t k) -> uint32_t {
+    const uint64_t b = lo + static_cast<uint64_t>(k) * kRecTile;
+    return static_cast<uint32_t>(hi - b < kRecTile ? hi - b : kRecTile);
+  };
+  // thread 0: copy logical [b, b+cnt) into stage; falls back to plain loads
+  // (s_plain) when the range spans more than kMaxRuns segments
+  auto issue = [&](uint32_t k, int stage) {
+    const uint64_t b = lo + static_cast<uint64_t>(k) * kRecTile;
+    const uint32_t cnt = tile_items(k);
+    uint32_t s = seg_find(s_prefix, in.nseg, b);
+    uint32_t runs = 0;
+    {
+      uint64_t x = b, left = cnt;
+      uint32_t ss = s;
+      while (left > 0 && runs <= kMaxRuns) {
+        const uint64_t take0 = s_prefix[ss + 1] - x;
+        const uint64_t take = take0 < left ? take0 : left;
+        if (take) ++runs;
+        x += take;
+        left -= take;
+        ++ss;
+      }
+    }
+    s_plain[stage] = runs > kMaxRuns ? 1u : 0u;
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(&s_bar[stage], runs > kMaxRuns ? 0u : cnt * static_cast<uint32_t>(sizeof(Rec)));
+    if (runs > kMaxRuns) return;
+    uint64_t x = b, left = cnt;
+    Rec* dst = s_rec + stage * kRecTile;
+    while (left > 0) {
+      const uint64_t off = x - s_prefix[s];
+      const uint64_t take0 = s_prefix[s + 1] - x;
+      const uint64_t take = take0 < left ? take0 : left;
+      if (take) {
+        bulk_load(dst, in.base + static_cast<uint64_t>(s) * in.cap + off,
+                  static_cast<uint32_t>(take * sizeof(Rec)), &s_bar[stage]);
+        dst += take;
+      }
+      x += take;
+      left -= take;
+      ++s;
+    }
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(&s_bar[0], 1);
+    mbar_init(&s_bar[1], 1);
+    fence_mbar_init();
+    if (ntile > 0) issue(0, 0);
+  }
+  __syncthreads();
+  uint64_t run[NOUT];
+#pragma unroll
+  for (int c = 0; c < NOUT; ++c) run[c] = 0;
+  uint32_t dropped_w = 0, cand = 0;
+  for (uint32_t k = 0; k < ntile; ++k) {
+    const int stage = k & 1;
+    Rec* recs = s_rec + stage * kRecTile;
+    const uint64_t b = lo + static_cast<uint64_t>(k) * kRecTile;
+    const uint32_t cnt = tile_items(k);
+    if (threadIdx.x == 0) s_ok = mbar_wait(&s_bar[stage], (k >> 1) & 1u, p.err) ? 1u : 0u;
+    __syncthreads();  // also: every thread is done with tile k-1 and its stage
+    if (!s_ok) return;
+    if (threadIdx.x == 0 && k + 1 < ntile) issue(k + 1, stage ^ 1);
+    if (s_plain[stage]) {
+      for (uint32_t t = threadIdx.x; t < cnt; t += kBlock) {
+        const uint64_t x = b + t;
+        const uint32_t s = seg_find(s_prefix, in.nseg, x);
+        recs[t] = in.base[static_cast<uint64_t>(s) * in.cap + (x - s_prefix[s])];
+      }
+      __syncthreads();
+    }
+    uint8_t cls[kItemsRec];
 #pragma unroll
     for (int j = 0; j < kItemsRec; ++j) {
-      const uint64_t i = base + j * kBlock + threadIdx.x;
+      const uint32_t t = j * kBlock + threadIdx.x;
       cls[j] = 0xff;
-      a[j] = b[j] = w[j] = oid[j] = 0;
-      if (i >= m) continue;
-      const uint32_t wt = r[j].w;
-      if (wt < p.wmin || wt > p.wmax) {
-        dropped_w += (wt > p.wmax) ? 1u : 0u;
+      if (t >= cnt) continue;
+      const Rec r = recs[t];
+      if (r.w < p.wmin || r.w > p.wmax) {
+        dropped_w += (r.w > p.wmax) ? 1u : 0u;
         continue;
       }
-      const uint32_t la = p.map ? p.map[r[j].a] : r[j].a;
-      const uint32_t lb = p.map ? p.map[r[j].b] : r[j].b;
+      ++cand;
+      const uint32_t la = p.map ? p.map[r.a] : r.a;
+      const uint32_t lb = p.map ? p.map[r.b] : r.b;
       if (la == lb) continue;
-      a[j] = la;
-      b[j] = lb;
-      w[j] = wt;
-      oid[j] = r[j].oid;
-      cls[j] = weight_class<NOUT>(wt, p);
+      recs[t].a = la;
+      recs[t].b = lb;
+      cls[j] = weight_class<NOUT>(r.w, p);
     }
-    edge_pass_finish<NOUT, kItemsRec>(tile, a, b, w, oid, cls, dropped_w, p);
+    seg_tile_finish<NOUT, kItemsRec>(cls, run, p, [&](uint32_t t) { return recs[t]; });
   }
+  seg_pass_end<NOUT>(run, dropped_w, cand, p);
 }
 
 // ---------------------------------------------------------------------------
@@ -274,6 +504,31 @@ __global__ void k_jump(uint32_t n, uint32_t* parent, uint32_t* err) {
       ++steps;
       // a cycle (never produced by a correct hook) must not keep the device
       // busy: one thread reaching the cap stops all others within 1024 steps
+      if ((steps & 1023u) == 0 && (steps > kJumpCap || (ld_relaxed(err) & kErrJump))) {
+        atomicOr(err, kErrJump);
+        break;
+      }
+    }
+    st_relaxed(parent + v, p);
+  }
+}
+
+// Second pointer-jumping pass.  Path halving lets a thread overwrite another
+// vertex's finished root pointer with an older ancestor, so after k_jump some
+// entries may still point one or two levels below the root.  Here every
+// thread only reads other entries and writes its own, so when the kernel
+// ends every vertex points at its root.
+__global__ void k_jump_finish(uint32_t n, uint32_t* parent, uint32_t* err) {
+  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n;
+       v += gridDim.x * blockDim.x) {
+    uint32_t p = ld_relaxed(parent + v);
+    if (p == v) continue;
+    uint32_t steps = 0;
+    for (;;) {
+      const uint32_t gp = ld_relaxed(parent + p);
+      if (gp == p) break;
+      p = gp;
+      ++steps;
       if ((steps & 1023u) == 0 && (steps > kJumpCap || (ld_relaxed(err) & kErrJump))) {
         atomicOr(err, kErrJump);
         break;
@@ -517,12 +772,14 @@ __global__ void k_sample_weights(const uint32_t* __restrict__ in_words, uint64_t
   }
 }
 
-__global__ void k_sample_weights_rec(const Rec* __restrict__ in, uint64_t m,
+// Same over a segmented list; prefix[s] = records in segments < s.
+__global__ void k_sample_weights_seg(SegIn in, const uint64_t* __restrict__ prefix, uint64_t m,
                                      uint64_t seed, uint32_t count, uint32_t* out) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count;
        i += gridDim.x * blockDim.x) {
-    const uint64_t pos = __umul64hi(mix64(seed + i), m);
-    out[i] = in[pos].w;
+    const uint64_t x = __umul64hi(mix64(seed + i), m);
+    const uint32_t sg = seg_find(prefix, in.nseg, x);
+    out[i] = in.base[static_cast<uint64_t>(sg) * in.cap + (x - prefix[sg])].w;
   }
 }
 

@@ -9,13 +9,17 @@
 //   boruvka3            local_mst_respecting_cut_edges.hpp:101-207
 //       -> Solve::rounds(): hook, jump, renumber, map, relabel+compact.
 //   localMST::filter    mst_utils_filter.hpp:102-126
-//       -> Solve::edge_pass(): heavier classes are relabelled by the current
+//       -> Solve::contract(): heavier classes are relabelled by the current
 //          components and internal edges dropped on the way into rounds().
 //   boruvka_recursive   hybrid_boruvka_edgefilter.hpp:227-330
 //       -> Solve::filter_rec(): host recursion over device edge lists.
+//
+// Edge lists are segmented (see kernels.cuh): every edge pass writes one
+// segment per CTA, so no pass has a cross-CTA scan on its critical path.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "kernels.cuh"
@@ -58,15 +62,15 @@ void Arena::release() {
   off = 0;
 }
 
-#define KS_TRY(x)                          \
-  do {                                     \
-    const kamsta_status s_ = (x);          \
-    if (s_ != KAMSTA_OK) return s_;        \
+#define KS_TRY(x)                   \
+  do {                              \
+    const kamsta_status s_ = (x);   \
+    if (s_ != KAMSTA_OK) return s_; \
   } while (0)
-#define CU_TRY(x)                                        \
-  do {                                                   \
-    const cudaError_t e_ = (x);                          \
-    if (e_ != cudaSuccess) return cuda_status(e_, #x);   \
+#define CU_TRY(x)                                      \
+  do {                                                 \
+    const cudaError_t e_ = (x);                        \
+    if (e_ != cudaSuccess) return cuda_status(e_, #x); \
   } while (0)
 
 static inline size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -74,71 +78,116 @@ static inline uint32_t ceil_div(uint64_t a, uint64_t b) {
   return static_cast<uint32_t>((a + b - 1) / b);
 }
 
-constexpr uint32_t kTileDir = kItemsDir * kBlock;
-constexpr uint32_t kTileRec = kItemsRec * kBlock;
 constexpr uint32_t kTileVtx = kItemsVtx * kBlock;
 constexpr uint32_t kSamples = 4096;
 
-// Occupancy-derived persistent grid for the tile kernels.
 template <typename K>
-static int persistent_grid(K kernel, int sms, uint32_t ntiles) {
-  static int per_sm = 0;  // one cache per kernel type K
-  if (per_sm == 0) {
-    int v = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kernel, kBlock, 0);
-    per_sm = v < 1 ? 1 : v;
-  }
-  const uint64_t g = static_cast<uint64_t>(per_sm) * sms;
-  return static_cast<int>(std::max<uint64_t>(1, std::min<uint64_t>(g, ntiles)));
+static int blocks_per_sm(K kernel, size_t dyn_smem) {
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, dyn_smem);
+  return per_sm < 1 ? 1 : per_sm;
 }
+
+// A segmented edge list in pool memory (see kernels.cuh).
+struct SegList {
+  Rec* base = nullptr;
+  uint64_t cap = 0;  // records per segment
+  uint32_t nseg = 0;
+  uint32_t* d_count = nullptr;  // kMaxSeg entries, written by the pass
+  std::vector<uint32_t> h_count;
+  uint64_t total = 0;
+  void* mem = nullptr;
+  SegIn in() const { return SegIn{base, d_count, cap, nseg}; }
+};
 
 class Solve {
  public:
-  Solve(kamsta_ctx* ctx, cudaStream_t st, const kamsta_wedge* in, uint64_t md,
-        uint32_t n, const kamsta_cfg& cfg, kamsta_stats* stats)
-      : ctx_(ctx), st_(st), in_(reinterpret_cast<const uint32_t*>(in)), md_(md),
-        n_(n), cfg_(cfg), stats_(stats) {}
+  Solve(kamsta_ctx* ctx, cudaStream_t st, const kamsta_wedge* in, uint64_t md, uint32_t n,
+        const kamsta_cfg& cfg, kamsta_stats* stats)
+      : ctx_(ctx), st_(st), in_(reinterpret_cast<const uint32_t*>(in)), md_(md), n_(n),
+        cfg_(cfg), stats_(stats) {}
+  ~Solve() {
+    for (SegList* L : owned_) {
+      free_list(L);
+      delete L;
+    }
+  }
 
   kamsta_status run(Algo algo, kamsta_wedge* d_out, SolveOut* out);
 
  private:
+  // ---- memory
   kamsta_status alloc_fixed();
-  kamsta_status ensure_edges(uint64_t cap);
-  kamsta_status fetch_counters(int first, int count);
+  SegList* new_list() {
+    owned_.push_back(new SegList());
+    return owned_.back();
+  }
+  kamsta_status alloc_list(SegList* L, uint32_t nseg, uint64_t cap);
+  void free_list(SegList* L);
+  // ---- sync / errors
+  kamsta_status fetch_counters();
   kamsta_status check_err();
   void fill_inf(uint64_t* p, uint64_t count);
   int grid_for(uint64_t items) const {
     const uint64_t g = (items + kBlock - 1) / kBlock;
     return static_cast<int>(std::max<uint64_t>(1, std::min<uint64_t>(g, uint64_t(sms_) * 8)));
   }
-  // Edge passes.  Counts of the pass land in counts_[0..nout) (kept per class)
-  // and counts_[kMaxOut] (dropped above wmax).
+  // One edge pass (src == nullptr: the directed input).  frac[c] bounds the
+  // share of a chunk's items that can land in class c (1 = all); outputs are
+  // (re)allocated here and resized exactly once on overflow.  minval (with
+  // minval_n entries) receives the class-0 minimum.
   template <int NOUT>
-  kamsta_status pass_dir(uint64_t m, const uint32_t* map, uint32_t wmin, uint32_t wmax,
-                         const uint32_t* thr, Rec* const* out, const uint64_t* cap,
-                         uint64_t* minval, bool validate, uint64_t* counts);
-  template <int NOUT>
-  kamsta_status pass_rec(const Rec* in, uint64_t m, const uint32_t* map, uint32_t wmin,
-                         uint32_t wmax, const uint32_t* thr, Rec* const* out,
-                         const uint64_t* cap, uint64_t* minval, uint64_t* counts);
-  // Boruvka rounds on list L (m0 edges, dense labels in [0, nreps_),
-  // canonical order).  minA_ must hold the round-0 minima.
-  kamsta_status rounds(Rec* L, uint64_t m0);
+  kamsta_status pass(int phase, const SegList* src, const uint32_t* map, uint32_t wmin,
+                     uint32_t wmax, const uint32_t* thr, SegList* const* outs, const double* frac,
+                     uint64_t* minval, uint64_t minval_n, bool validate);
+  // Boruvka rounds on list L (dense labels in [0, nreps_)); minA_ holds the
+  // round-0 minima.  Frees L if `own` is set.
+  kamsta_status rounds(SegList* L, bool own);
   // Relabel `L` (or the directed input when L == nullptr, weights in
-  // [wmin, wmax]) into the current dense space and run rounds on the result.
-  kamsta_status contract_list(const Rec* L, uint64_t m, uint32_t wmin, uint32_t wmax);
+  // [wmin, wmax], a share `frac` of the entries) into the current dense
+  // labels, fuse the round-0 minimum and contract the result.
+  kamsta_status contract(const SegList* L, uint32_t wmin, uint32_t wmax, double frac);
   std::vector<uint32_t> plan_classes();
-  kamsta_status sample_weights(const Rec* L, uint64_t m, uint32_t count,
-                               std::vector<uint32_t>* out);
-  kamsta_status filter_rec(Rec* L, uint64_t m, bool stop, int depth);
+  kamsta_status sample_weights(const SegList* L, uint32_t count, std::vector<uint32_t>* out);
+  kamsta_status filter_rec(SegList* L, bool own, bool stop, int depth);
   kamsta_status run_boruvka();
   kamsta_status run_filter_boruvka();
+  // ---- debugging (KAMSTA_DEBUG_CHECKS=1): host-side invariant checks
+  kamsta_status debug_list(const char* where, const SegList& L, uint64_t nlabels);
+  kamsta_status debug_forest(const char* where, uint64_t count);
+
   void trace(uint64_t m, uint64_t n) {
     if (stats_ && (cfg_.flags & KAMSTA_FLAG_TRACE) && stats_->trace_len < KAMSTA_TRACE_MAX) {
       stats_->trace_m[stats_->trace_len] = m;
       stats_->trace_n[stats_->trace_len] = n;
       stats_->trace_len++;
     }
+  }
+  // phase timing: event pairs recorded on st_, resolved after each host sync
+  struct Pending {
+    int phase, ev_a, ev_b;
+  };
+  int tick() {
+    const int e = next_ev_;
+    next_ev_ = (next_ev_ + 1) % kTimerEvents;
+    cudaEventRecord(ctx_->tev[e], st_);
+    return e;
+  }
+  void tock(int phase, int ev_a) { pending_.push_back({phase, ev_a, tick()}); }
+  void resolve() {
+    for (const Pending& q : pending_) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, ctx_->tev[q.ev_a], ctx_->tev[q.ev_b]) == cudaSuccess)
+        phase_ms_[q.phase] += ms;
+    }
+    pending_.clear();
+    cudaGetLastError();
+  }
+  void account(int phase, uint64_t bytes, uint32_t launches) {
+    phase_bytes_[phase] += bytes;
+    phase_launches_[phase] += launches;
+    alg_bytes_ += bytes;
+    launches_ += launches;
   }
 
   kamsta_ctx* ctx_;
@@ -149,48 +198,45 @@ class Solve {
   kamsta_cfg cfg_;
   kamsta_stats* stats_;
   int sms_ = 1;
-  uint32_t launches_ = 0;
-  uint32_t rounds_ = 0;
-  uint32_t levels_ = 0;
+  bool aligned16_ = false;
+  bool debug_ = false;
+  bool tolerate_overflow_ = false;
+  uint32_t launches_ = 0, rounds_ = 0, levels_ = 0;
   uint64_t alg_bytes_ = 0;
+  double phase_ms_[KAMSTA_PHASES] = {};
+  uint64_t phase_bytes_[KAMSTA_PHASES] = {};
+  uint32_t phase_launches_[KAMSTA_PHASES] = {};
+  std::vector<Pending> pending_;
+  int next_ev_ = 0;
+  std::vector<SegList*> owned_;
 
   // vertex-side buffers (n_ entries unless noted)
   uint32_t *P_ = nullptr, *D_ = nullptr, *V_ = nullptr, *Vn_ = nullptr;
   uint32_t *dense_of_ = nullptr, *parent_ = nullptr, *msfoid_ = nullptr, *newid_ = nullptr;
   uint32_t *Rbuf_ = nullptr, *Obuf_ = nullptr, *msf_ = nullptr, *samples_ = nullptr;
-  uint64_t *minA_ = nullptr, *minB_ = nullptr;
-  uint64_t* status_[6] = {};
-  uint32_t status_words_ = 0;  // capacity of each status array (tiles)
-  Rec* C_[kMaxOut] = {};       // materialised weight classes
-  uint64_t Ccap_[kMaxOut] = {};
-  Rec *E1_ = nullptr, *E2_ = nullptr;
-  uint64_t Ecap_ = 0;
+  uint64_t *minA_ = nullptr, *minB_ = nullptr, *prefix_ = nullptr;
+  uint64_t* status_[3] = {};  // vertex-scan look-back words
   uint32_t nreps_ = 0;
   uint64_t msf_count_ = 0;
-  bool aligned16_ = false;
   std::vector<uint32_t> bounds_;        // ascending weight-class bounds
   std::vector<uint32_t> samples_host_;  // sorted weight sample of the input
-  bool tolerate_overflow_ = false;  // first pass: overflow means "resize"
-  static constexpr kamsta_status kRetry = 1000;
 };
+
+// ---------------------------------------------------------------------------
+// memory
 
 kamsta_status Solve::alloc_fixed() {
   const uint64_t n = n_;
-  const uint64_t mu = md_ / 2 + 1;
-  const uint32_t tiles = std::max({ceil_div(md_, kTileDir), ceil_div(mu, kTileRec),
-                                   ceil_div(n, kTileVtx), 1u});
-  status_words_ = tiles;
+  const uint32_t vtiles = std::max(ceil_div(n, kTileVtx), 1u);
   size_t bytes = 0;
   auto add = [&](uint64_t count, size_t sz) { bytes += round_up(count * sz, 256); };
-  for (int i = 0; i < 9; ++i) add(n + 1, 4);        // P D V Vn dense parent msfoid newid msf
-  add(2 * n + 64, 4);                               // Rbuf
-  add(n + 64, 4);                                   // Obuf
+  for (int i = 0; i < 9; ++i) add(n + 1, 4);  // P D V Vn dense parent msfoid newid msf
+  add(2 * n + 64, 4);                         // Rbuf
+  add(n + 64, 4);                             // Obuf
   add(n + 1, 8);
-  add(n + 1, 8);                                    // minA minB
-  for (int i = 0; i < 6; ++i) add(tiles, 8);
-  // class lists are estimated later; reserve a generous first guess here
-  // and grow (re-run) if the first pass overflows.
-  for (int i = 0; i < kMaxOut; ++i) add(Ccap_[i], sizeof(Rec));
+  add(n + 1, 8);  // minA minB
+  add(kMaxSeg + 1, 8);
+  for (int i = 0; i < 3; ++i) add(vtiles, 8);
   CU_TRY(ctx_->fixed.reserve(bytes + 4096));
   Arena& A = ctx_->fixed;
   P_ = A.take<uint32_t>(n + 1);
@@ -206,24 +252,45 @@ kamsta_status Solve::alloc_fixed() {
   Obuf_ = A.take<uint32_t>(n + 64);
   minA_ = A.take<uint64_t>(n + 1);
   minB_ = A.take<uint64_t>(n + 1);
-  for (int i = 0; i < 6; ++i) status_[i] = A.take<uint64_t>(tiles);
-  for (int i = 0; i < kMaxOut; ++i) C_[i] = Ccap_[i] ? A.take<Rec>(Ccap_[i]) : nullptr;
-  if (!status_[5]) {
+  prefix_ = A.take<uint64_t>(kMaxSeg + 1);
+  for (int i = 0; i < 3; ++i) status_[i] = A.take<uint64_t>(vtiles);
+  if (!status_[2]) {
     set_error("internal: fixed arena too small");
     return KAMSTA_E_OOM;
   }
   return KAMSTA_OK;
 }
 
-kamsta_status Solve::ensure_edges(uint64_t cap) {
+kamsta_status Solve::alloc_list(SegList* L, uint32_t nseg, uint64_t cap) {
+  free_list(L);
   cap = std::max<uint64_t>(cap, 1);
-  const size_t bytes = 2 * round_up(cap * sizeof(Rec), 256) + 1024;
-  CU_TRY(ctx_->edges.reserve(bytes));
-  E1_ = ctx_->edges.take<Rec>(cap);
-  E2_ = ctx_->edges.take<Rec>(cap);
-  Ecap_ = cap;
+  const size_t cnt_bytes = round_up(sizeof(uint32_t) * kMaxSeg, 256);
+  const size_t bytes = cnt_bytes + static_cast<size_t>(nseg) * cap * sizeof(Rec);
+  void* mem = nullptr;
+  CU_TRY(cudaMallocFromPoolAsync(&mem, bytes, ctx_->pool, st_));
+  L->mem = mem;
+  L->d_count = static_cast<uint32_t*>(mem);
+  L->base = reinterpret_cast<Rec*>(static_cast<char*>(mem) + cnt_bytes);
+  L->cap = cap;
+  L->nseg = nseg;
+  L->h_count.assign(nseg, 0);
+  L->total = 0;
   return KAMSTA_OK;
 }
+
+void Solve::free_list(SegList* L) {
+  if (L && L->mem) cudaFreeAsync(L->mem, st_);
+  if (L) {
+    L->mem = nullptr;
+    L->base = nullptr;
+    L->d_count = nullptr;
+    L->total = 0;
+    L->nseg = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// sync, errors, debugging
 
 kamsta_status Solve::check_err() {
   uint32_t e = *ctx_->h_err;
@@ -249,116 +316,168 @@ kamsta_status Solve::check_err() {
   return KAMSTA_E_CUDA;
 }
 
-kamsta_status Solve::fetch_counters(int first, int count) {
-  CU_TRY(cudaMemcpyAsync(ctx_->h_counters + first, ctx_->d_counters + first,
-                         sizeof(DevCounters) * count, cudaMemcpyDeviceToHost, st_));
-  CU_TRY(cudaMemcpyAsync(ctx_->h_err, ctx_->d_err, sizeof(uint32_t),
+kamsta_status Solve::fetch_counters() {
+  CU_TRY(cudaMemcpyAsync(ctx_->h_counters, ctx_->d_counters, sizeof(DevCounters) * kCSlots,
                          cudaMemcpyDeviceToHost, st_));
+  CU_TRY(cudaMemcpyAsync(ctx_->h_err, ctx_->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st_));
   CU_TRY(cudaStreamSynchronize(st_));
+  resolve();
   return check_err();
 }
 
+kamsta_status Solve::debug_list(const char* where, const SegList& L, uint64_t nlabels) {
+  if (!debug_ || L.total == 0) return KAMSTA_OK;
+  uint32_t prev = 0;
+  bool first = true;
+  for (uint32_t s = 0; s < L.nseg; ++s) {
+    const uint32_t c = L.h_count[s];
+    if (!c) continue;
+    std::vector<Rec> h(c);
+    CU_TRY(cudaMemcpyAsync(h.data(), L.base + s * L.cap, c * sizeof(Rec), cudaMemcpyDeviceToHost,
+                           st_));
+    CU_TRY(cudaStreamSynchronize(st_));
+    for (uint32_t i = 0; i < c; ++i) {
+      const bool ok = (first || h[i].oid > prev) && h[i].a < nlabels && h[i].b < nlabels &&
+                      h[i].a != h[i].b;
+      if (!ok) {
+        fprintf(stderr,
+                "[kamsta debug] %s: bad record seg %u idx %u: a=%u b=%u w=%u oid=%u prev=%u "
+                "nlabels=%llu\n",
+                where, s, i, h[i].a, h[i].b, h[i].w, h[i].oid, prev, (unsigned long long)nlabels);
+        set_error(std::string("debug check failed: ") + where);
+        return KAMSTA_E_CUDA;
+      }
+      prev = h[i].oid;
+      first = false;
+    }
+  }
+  return KAMSTA_OK;
+}
+
+kamsta_status Solve::debug_forest(const char* where, uint64_t count) {
+  if (!debug_ || count == 0) return KAMSTA_OK;
+  std::vector<uint32_t> h(count);
+  CU_TRY(cudaMemcpyAsync(h.data(), msf_, count * 4, cudaMemcpyDeviceToHost, st_));
+  CU_TRY(cudaStreamSynchronize(st_));
+  std::sort(h.begin(), h.end());
+  for (size_t i = 1; i < h.size(); ++i)
+    if (h[i] == h[i - 1]) {
+      fprintf(stderr, "[kamsta debug] %s: forest edge id %u appears twice\n", where, h[i]);
+      set_error(std::string("debug check failed: ") + where);
+      return KAMSTA_E_CUDA;
+    }
+  return KAMSTA_OK;
+}
+
 void Solve::fill_inf(uint64_t* p, uint64_t count) {
+  if (!count) return;
   k_fill64<<<grid_for(count), kBlock, 0, st_>>>(count, p, kInf64);
-  launches_++;
+  account(KAMSTA_PHASE_FINALIZE, count * 8, 1);
 }
+
+// ---------------------------------------------------------------------------
+// edge passes
 
 template <int NOUT>
-kamsta_status Solve::pass_dir(uint64_t m, const uint32_t* map, uint32_t wmin, uint32_t wmax,
-                              const uint32_t* thr, Rec* const* out, const uint64_t* cap,
-                              uint64_t* minval, bool validate, uint64_t* counts) {
-  const uint32_t ntiles = ceil_div(m, kTileDir);
-  if (ntiles == 0) {
-    for (int c = 0; c <= kMaxOut; ++c) counts[c] = 0;
-    return KAMSTA_OK;
-  }
-  DevCounters* dc = ctx_->d_counters + kCEdge;
-  CU_TRY(cudaMemsetAsync(dc, 0, sizeof(DevCounters), st_));
-  for (int c = 0; c < NOUT; ++c)
-    CU_TRY(cudaMemsetAsync(status_[c], 0, sizeof(uint64_t) * ntiles, st_));
-  EdgePassArgs a{};
-  a.map = map;
-  a.wmin = wmin;
-  a.wmax = wmax;
-  for (int c = 0; c < NOUT - 1; ++c) a.thr[c] = thr[c];
+kamsta_status Solve::pass(int phase, const SegList* src, const uint32_t* map, uint32_t wmin,
+                          uint32_t wmax, const uint32_t* thr, SegList* const* outs,
+                          const double* frac, uint64_t* minval, uint64_t minval_n,
+                          bool validate) {
+  const bool dir = src == nullptr;
+  const uint64_t total = dir ? md_ : src->total;
+  const uint32_t tile = dir ? kDirTile : kRecTile;
+  const size_t dyn = dir ? kDirDynSmem : kRecDynSmem;
+  const int per_sm =
+      dir ? blocks_per_sm(k_pass_dir<NOUT>, dyn) : blocks_per_sm(k_pass_seg<NOUT>, dyn);
+  const uint64_t gmax = std::min<uint64_t>(kMaxSeg, uint64_t(per_sm) * sms_);
+  uint64_t chunk = std::max<uint64_t>(1, (total + gmax - 1) / gmax);
+  chunk = round_up(chunk, tile);
+  const uint32_t G = std::max<uint32_t>(1, ceil_div(total, chunk));
+  uint64_t cap[kMaxOut];
   for (int c = 0; c < NOUT; ++c) {
-    a.out[c] = out[c];
-    a.cap[c] = cap[c];
-    a.status[c] = status_[c];
+    const double f = std::min(1.0, std::max(0.0, frac ? frac[c] : 1.0));
+    const double est = f * chunk * 1.1 + 6.0 * std::sqrt(f * chunk) + tile;
+    cap[c] = std::min<uint64_t>(chunk, static_cast<uint64_t>(est));
   }
-  a.minval = minval;
-  a.counts = dc->cnt;
-  a.ticket = &dc->ticket;
-  a.err = ctx_->d_err;
-  a.n = n_;
-  a.validate = validate ? 1 : 0;
-  a.aligned16 = aligned16_ ? 1 : 0;
-  a.ntiles = ntiles;
-  const int grid = persistent_grid(k_edge_pass_dir<NOUT>, sms_, ntiles);
-  k_edge_pass_dir<NOUT><<<grid, kBlock, 0, st_>>>(in_, m, a);
-  launches_++;
-  CU_TRY(cudaGetLastError());
-  KS_TRY(fetch_counters(kCEdge, 1));
-  const DevCounters& h = ctx_->h_counters[kCEdge];
-  uint64_t kept = 0;
-  for (int c = 0; c <= kMaxOut; ++c) counts[c] = (c < NOUT || c == kMaxOut) ? h.cnt[c] : 0;
-  for (int c = 0; c < NOUT; ++c) kept += counts[c];
-  alg_bytes_ += m * 12 + kept * sizeof(Rec) + (map ? kept * 8 : 0) + (minval ? counts[0] * 16 : 0);
-  return KAMSTA_OK;
+  if (!dir && src->nseg > static_cast<uint32_t>(kMaxSeg)) {
+    set_error("internal: too many segments");
+    return KAMSTA_E_CUDA;
+  }
+  for (int attempt = 0;; ++attempt) {
+    for (int c = 0; c < NOUT; ++c) KS_TRY(alloc_list(outs[c], G, cap[c]));
+    if (total == 0) return KAMSTA_OK;
+    CU_TRY(cudaMemsetAsync(ctx_->d_counters + kCEdge, 0, sizeof(DevCounters), st_));
+    PassArgs a{};
+    a.map = map;
+    a.wmin = wmin;
+    a.wmax = wmax;
+    for (int c = 0; c < NOUT - 1; ++c) a.thr[c] = thr[c];
+    for (int c = 0; c < NOUT; ++c) a.out[c] = SegOut{outs[c]->base, cap[c], outs[c]->d_count};
+    a.minval = minval;
+    // original ids (no map): few updates per address, reductions go straight
+    // out; relabelled lists have hub components, so updates are filtered
+    a.min_checked = map != nullptr ? 1u : 0u;
+    a.total = total;
+    a.chunk = chunk;
+    a.counts = ctx_->d_counters[kCEdge].cnt;
+    a.err = ctx_->d_err;
+    a.n = n_;
+    a.validate = validate ? 1 : 0;
+    a.aligned16 = aligned16_ ? 1 : 0;
+    const int t0 = tick();
+    if (dir)
+      k_pass_dir<NOUT><<<G, kBlock, dyn, st_>>>(in_, a);
+    else
+      k_pass_seg<NOUT><<<G, kBlock, dyn, st_>>>(src->in(), a);
+    tock(phase, t0);
+    CU_TRY(cudaGetLastError());
+    for (int c = 0; c < NOUT; ++c)
+      CU_TRY(cudaMemcpyAsync(outs[c]->h_count.data(), outs[c]->d_count, sizeof(uint32_t) * G,
+                             cudaMemcpyDeviceToHost, st_));
+    tolerate_overflow_ = true;
+    const kamsta_status fs = fetch_counters();
+    tolerate_overflow_ = false;
+    KS_TRY(fs);
+    bool overflow = false;
+    uint64_t kept = 0;
+    for (int c = 0; c < NOUT; ++c) {
+      uint64_t sum = 0, mx = 0;
+      for (uint32_t s = 0; s < G; ++s) {
+        sum += outs[c]->h_count[s];
+        mx = std::max<uint64_t>(mx, outs[c]->h_count[s]);
+      }
+      outs[c]->total = sum;
+      kept += sum;
+      if (mx > cap[c]) {
+        overflow = true;
+        cap[c] = mx;
+      }
+    }
+    const DevCounters& h = ctx_->h_counters[kCEdge];
+    // read every item, two label gathers per candidate, write kept records,
+    // one 8-byte minimum per endpoint of a class-0 record
+    account(phase,
+            total * (dir ? 12 : sizeof(Rec)) + (map ? h.cnt[1] * 8 : 0) + kept * sizeof(Rec) +
+                (minval ? outs[0]->total * 16 : 0),
+            1);
+    if (!overflow) return KAMSTA_OK;
+    if (attempt > 0) {
+      set_error("internal: edge-pass output overflow after exact resize");
+      return KAMSTA_E_CUDA;
+    }
+    CU_TRY(cudaMemsetAsync(ctx_->d_err, 0, sizeof(uint32_t), st_));
+    if (minval) fill_inf(minval, minval_n);  // the failed attempt fed stale positions
+  }
 }
 
-template <int NOUT>
-kamsta_status Solve::pass_rec(const Rec* in, uint64_t m, const uint32_t* map, uint32_t wmin,
-                              uint32_t wmax, const uint32_t* thr, Rec* const* out,
-                              const uint64_t* cap, uint64_t* minval, uint64_t* counts) {
-  const uint32_t ntiles = ceil_div(m, kTileRec);
-  if (ntiles == 0) {
-    for (int c = 0; c <= kMaxOut; ++c) counts[c] = 0;
-    return KAMSTA_OK;
-  }
-  DevCounters* dc = ctx_->d_counters + kCEdge;
-  CU_TRY(cudaMemsetAsync(dc, 0, sizeof(DevCounters), st_));
-  for (int c = 0; c < NOUT; ++c)
-    CU_TRY(cudaMemsetAsync(status_[c], 0, sizeof(uint64_t) * ntiles, st_));
-  EdgePassArgs a{};
-  a.map = map;
-  a.wmin = wmin;
-  a.wmax = wmax;
-  for (int c = 0; c < NOUT - 1; ++c) a.thr[c] = thr[c];
-  for (int c = 0; c < NOUT; ++c) {
-    a.out[c] = out[c];
-    a.cap[c] = cap[c];
-    a.status[c] = status_[c];
-  }
-  a.minval = minval;
-  a.counts = dc->cnt;
-  a.ticket = &dc->ticket;
-  a.err = ctx_->d_err;
-  a.n = n_;
-  a.ntiles = ntiles;
-  const int grid = persistent_grid(k_edge_pass_rec<NOUT>, sms_, ntiles);
-  k_edge_pass_rec<NOUT><<<grid, kBlock, 0, st_>>>(in, m, a);
-  launches_++;
-  CU_TRY(cudaGetLastError());
-  KS_TRY(fetch_counters(kCEdge, 1));
-  const DevCounters& h = ctx_->h_counters[kCEdge];
-  uint64_t kept = 0;
-  for (int c = 0; c <= kMaxOut; ++c) counts[c] = (c < NOUT || c == kMaxOut) ? h.cnt[c] : 0;
-  for (int c = 0; c < NOUT; ++c) kept += counts[c];
-  alg_bytes_ += m * sizeof(Rec) + kept * sizeof(Rec) + (map ? m * 8 : 0) +
-                (minval ? counts[0] * 16 : 0);
-  return KAMSTA_OK;
-}
-
-// Boruvka rounds (boruvka3).  One host read per round: the new edge count,
-// vertex count and forest-edge count.
-kamsta_status Solve::rounds(Rec* L, uint64_t m0) {
+// ---------------------------------------------------------------------------
+// Boruvka rounds (boruvka3).  One host read per round: the new edge, vertex
+// and forest-edge counts.
+kamsta_status Solve::rounds(SegList* L, bool own) {
   levels_++;
   const uint32_t n0 = nreps_;
-  Rec* cur = L;
-  Rec* bufs[2] = {E1_, E2_};
-  int nb = (cur == E1_) ? 1 : 0;
-  uint64_t m = m0;
+  SegList* cur = L;
+  bool cur_owned = own;
   uint32_t nr = n0;
   uint64_t* minv = minA_;
   uint64_t* minn = minB_;
@@ -368,19 +487,22 @@ kamsta_status Solve::rounds(Rec* L, uint64_t m0) {
   size_t roff = 0, ooff = 0;
   uint32_t r = 0;
   const uint32_t* orig_cur = V_;
-  while (m > 0) {
+  while (cur->total > 0) {
     if (r >= static_cast<uint32_t>(kMaxRounds)) {
       set_error("round cap reached");
       return KAMSTA_E_NOCONVERGE;
     }
-    trace(m, nr);
-    CU_TRY(cudaMemsetAsync(ctx_->d_counters + kCVertex, 0, 2 * sizeof(DevCounters), st_));
+    trace(cur->total, nr);
+    const uint64_t m = cur->total;
+    CU_TRY(cudaMemsetAsync(ctx_->d_counters + kCVertex, 0, sizeof(DevCounters), st_));
     const int gv = grid_for(nr);
-    k_hook<<<gv, kBlock, 0, st_>>>(nr, minv, cur, parent_, msfoid_, ctx_->d_err);
+    const int tv = tick();
+    k_hook<<<gv, kBlock, 0, st_>>>(nr, minv, cur->base, parent_, msfoid_, ctx_->d_err);
     k_jump<<<gv, kBlock, 0, st_>>>(nr, parent_, ctx_->d_err);
+    k_jump_finish<<<gv, kBlock, 0, st_>>>(nr, parent_, ctx_->d_err);
     const uint32_t ntv = ceil_div(nr, kTileVtx);
-    CU_TRY(cudaMemsetAsync(status_[3], 0, sizeof(uint64_t) * ntv, st_));
-    CU_TRY(cudaMemsetAsync(status_[4], 0, sizeof(uint64_t) * ntv, st_));
+    CU_TRY(cudaMemsetAsync(status_[0], 0, sizeof(uint64_t) * ntv, st_));
+    CU_TRY(cudaMemsetAsync(status_[1], 0, sizeof(uint64_t) * ntv, st_));
     uint32_t* onext = Obuf_ + ooff;
     VertexScanArgs va{};
     va.n = nr;
@@ -394,42 +516,38 @@ kamsta_status Solve::rounds(Rec* L, uint64_t m0) {
     va.msf_out = msf_ + msf_count_;
     va.msf_cap = (n_ + 1) - msf_count_;
     va.orig_cap = std::min<uint64_t>((n_ + 64) - ooff, n_ + 1);
-    va.status[0] = status_[3];
-    va.status[1] = status_[4];
+    va.status[0] = status_[0];
+    va.status[1] = status_[1];
     va.counts = ctx_->d_counters[kCVertex].cnt;
     va.ticket = &ctx_->d_counters[kCVertex].ticket;
     va.err = ctx_->d_err;
     va.ntiles = ntv;
-    k_vertex_scan<<<persistent_grid(k_vertex_scan, sms_, ntv), kBlock, 0, st_>>>(va);
+    k_vertex_scan<<<std::min<int>(ntv, blocks_per_sm(k_vertex_scan, 0) * sms_), kBlock, 0, st_>>>(
+        va);
     uint32_t* R = Rbuf_ + roff;
     k_map<<<gv, kBlock, 0, st_>>>(nr, minv, parent_, newid_, R);
-    launches_ += 4;
+    tock(KAMSTA_PHASE_ROUND_VERTS, tv);
     // relabel + self-loop removal + compaction + next-round minimum
-    const uint32_t ntiles = ceil_div(m, kTileRec);
-    CU_TRY(cudaMemsetAsync(status_[0], 0, sizeof(uint64_t) * ntiles, st_));
-    Rec* nxt = bufs[nb];
-    EdgePassArgs a{};
-    a.map = R;
-    a.wmin = 0;
-    a.wmax = 0xffffffffu;
-    a.out[0] = nxt;
-    a.cap[0] = Ecap_;
-    a.status[0] = status_[0];
-    a.minval = minn;
-    a.counts = ctx_->d_counters[kCEdge].cnt;
-    a.ticket = &ctx_->d_counters[kCEdge].ticket;
-    a.err = ctx_->d_err;
-    a.ntiles = ntiles;
-    k_edge_pass_rec<1><<<persistent_grid(k_edge_pass_rec<1>, sms_, ntiles), kBlock, 0, st_>>>(
-        cur, m, a);
-    launches_++;
-    CU_TRY(cudaGetLastError());
-    KS_TRY(fetch_counters(kCVertex, 2));
+    SegList* nxt = new_list();
+    SegList* outs[1] = {nxt};
+    KS_TRY(pass<1>(KAMSTA_PHASE_ROUND_EDGES, cur, R, 0, 0xffffffffu, nullptr, outs, nullptr, minn,
+                   0, false));
     const uint64_t n_next = ctx_->h_counters[kCVertex].cnt[0];
     const uint64_t added = ctx_->h_counters[kCVertex].cnt[1];
-    const uint64_t m_next = ctx_->h_counters[kCEdge].cnt[0];
-    alg_bytes_ += uint64_t(nr) * (40 + 8 + 16 + 20) + n_next * 16 + added * 4;
-    alg_bytes_ += m * (sizeof(Rec) + 8) + m_next * (sizeof(Rec) + 16);
+    // hook: minimum, record gather, partner minimum, parent + edge id;
+    // jump: parent reads/writes; scan: parent, minimum, orig per vertex and
+    // id/orig/minimum per root, edge id per hooked vertex; map: 3 reads + 1 write
+    account(KAMSTA_PHASE_ROUND_VERTS,
+            uint64_t(nr) * ((8 + 16 + 8 + 8) + 16 + (4 + 8 + 4) + (8 + 4 + 4)) + n_next * 16 +
+                added * 8,
+            6);
+    if (debug_) {
+      fprintf(stderr, "[kamsta debug] round %u: m=%llu n=%u -> m'=%llu n'=%llu forest+=%llu\n", r,
+              (unsigned long long)m, nr, (unsigned long long)nxt->total,
+              (unsigned long long)n_next, (unsigned long long)added);
+      KS_TRY(debug_forest("after vertex scan", msf_count_ + added));
+      KS_TRY(debug_list("after relabel pass", *nxt, n_next));
+    }
     msf_count_ += added;
     if (msf_count_ > n_) {
       set_error("internal: forest larger than n-1");
@@ -440,59 +558,73 @@ kamsta_status Solve::rounds(Rec* L, uint64_t m0) {
     roff += nr;
     ooff += n_next;
     orig_cur = onext;
+    if (cur_owned) free_list(cur);
     cur = nxt;
-    nb ^= 1;
-    m = m_next;
+    cur_owned = true;
     nr = static_cast<uint32_t>(n_next);
     std::swap(minv, minn);
     ++r;
   }
+  if (cur_owned) free_list(cur);
   rounds_ += r;
   if (r == 0) return KAMSTA_OK;  // nothing contracted; labels unchanged
   ca.rounds = r;
   ca.P = P_;
   ca.err = ctx_->d_err;
+  const int tf = tick();
   k_chase<<<grid_for(n0), kBlock, 0, st_>>>(ca);
   const uint32_t ntv = ceil_div(n0, kTileVtx);
   CU_TRY(cudaMemsetAsync(ctx_->d_counters + kCRep, 0, sizeof(DevCounters), st_));
-  CU_TRY(cudaMemsetAsync(status_[5], 0, sizeof(uint64_t) * ntv, st_));
+  CU_TRY(cudaMemsetAsync(status_[2], 0, sizeof(uint64_t) * ntv, st_));
   RepScanArgs ra{};
   ra.n = n0;
   ra.V = V_;
   ra.P = P_;
   ra.Vout = Vn_;
   ra.dense_of = dense_of_;
-  ra.status = status_[5];
+  ra.status = status_[2];
   ra.counts = ctx_->d_counters[kCRep].cnt;
   ra.ticket = &ctx_->d_counters[kCRep].ticket;
   ra.err = ctx_->d_err;
   ra.ntiles = ntv;
-  k_rep_scan<<<persistent_grid(k_rep_scan, sms_, ntv), kBlock, 0, st_>>>(ra);
+  k_rep_scan<<<std::min<int>(ntv, blocks_per_sm(k_rep_scan, 0) * sms_), kBlock, 0, st_>>>(ra);
   k_relabel_all<<<grid_for(n_), kBlock, 0, st_>>>(n_, P_, dense_of_, D_);
-  launches_ += 3;
+  tock(KAMSTA_PHASE_FINALIZE, tf);
   CU_TRY(cudaGetLastError());
-  KS_TRY(fetch_counters(kCRep, 1));
-  alg_bytes_ += uint64_t(n0) * (4 * r + 12) + uint64_t(n0) * 16 + uint64_t(n_) * 16;
+  KS_TRY(fetch_counters());
+  account(KAMSTA_PHASE_FINALIZE,
+          uint64_t(n0) * (4 * r + 12) + uint64_t(n0) * 16 + uint64_t(n_) * 16, 3);
   nreps_ = static_cast<uint32_t>(ctx_->h_counters[kCRep].cnt[0]);
   std::swap(V_, Vn_);
   return KAMSTA_OK;
 }
 
-kamsta_status Solve::sample_weights(const Rec* L, uint64_t m, uint32_t count,
-                                    std::vector<uint32_t>* out) {
+// ---------------------------------------------------------------------------
+// sampling and planning
+
+kamsta_status Solve::sample_weights(const SegList* L, uint32_t count, std::vector<uint32_t>* out) {
   out->clear();
+  const uint64_t m = L ? L->total : md_;
   if (m == 0) return KAMSTA_OK;
   count = std::min<uint32_t>(count, kSamples);
   const int g = grid_for(count);
-  if (L)
-    k_sample_weights_rec<<<g, kBlock, 0, st_>>>(L, m, cfg_.seed, count, samples_);
-  else
+  const int tp = tick();
+  if (L) {
+    std::vector<uint64_t> pre(L->nseg + 1, 0);
+    for (uint32_t s = 0; s < L->nseg; ++s) pre[s + 1] = pre[s] + L->h_count[s];
+    CU_TRY(cudaMemcpyAsync(prefix_, pre.data(), sizeof(uint64_t) * (L->nseg + 1),
+                           cudaMemcpyHostToDevice, st_));
+    k_sample_weights_seg<<<g, kBlock, 0, st_>>>(L->in(), prefix_, m, cfg_.seed, count, samples_);
+  } else {
     k_sample_weights<<<g, kBlock, 0, st_>>>(in_, m, cfg_.seed, count, samples_);
-  launches_++;
+  }
+  tock(KAMSTA_PHASE_PLAN, tp);
+  account(KAMSTA_PHASE_PLAN, uint64_t(count) * 8, 1);
   out->resize(count);
-  CU_TRY(cudaMemcpyAsync(out->data(), samples_, count * sizeof(uint32_t),
-                         cudaMemcpyDeviceToHost, st_));
+  CU_TRY(cudaMemcpyAsync(out->data(), samples_, count * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                         st_));
   CU_TRY(cudaStreamSynchronize(st_));
+  resolve();
   std::sort(out->begin(), out->end());
   return KAMSTA_OK;
 }
@@ -505,14 +637,14 @@ std::vector<uint32_t> Solve::plan_classes() {
   std::vector<uint32_t> thr;
   if (cfg_.local_preprocessing == KAMSTA_NO_PREPROCESSING) return thr;
   std::vector<uint32_t>& s = samples_host_;
-  if (sample_weights(nullptr, md_, kSamples, &s) != KAMSTA_OK) return thr;
+  if (sample_weights(nullptr, kSamples, &s) != KAMSTA_OK) return thr;
   double m_est = static_cast<double>(md_) / 2.0;
   const double nv = static_cast<double>(n_);
   size_t len = s.size();
   while (m_est > 3.0 * nv && len >= 16) {
     const uint32_t pivot = s[static_cast<size_t>(len * 0.25)];
-    const size_t light = static_cast<size_t>(
-        std::upper_bound(s.begin(), s.begin() + len, pivot) - s.begin());
+    const size_t light =
+        static_cast<size_t>(std::upper_bound(s.begin(), s.begin() + len, pivot) - s.begin());
     const double frac = static_cast<double>(light) / static_cast<double>(len);
     if (std::abs(0.5 - (1.0 - frac)) > 0.4) break;  // is_unbalanced
     if (!thr.empty() && pivot >= thr.back()) break;
@@ -523,20 +655,25 @@ std::vector<uint32_t> Solve::plan_classes() {
   return thr;
 }
 
-// Relabel a list (or the directed input) into the current dense labels with
-// the next minimum fused in, then contract it.
-kamsta_status Solve::contract_list(const Rec* L, uint64_t m, uint32_t wmin, uint32_t wmax) {
-  if (m == 0 || nreps_ <= 1) return KAMSTA_OK;
+static double sample_share(const std::vector<uint32_t>& s, uint32_t lo, uint32_t hi) {
+  if (s.empty()) return 1.0;
+  const double k = static_cast<double>(std::upper_bound(s.begin(), s.end(), hi) -
+                                       std::lower_bound(s.begin(), s.end(), lo));
+  return k / static_cast<double>(s.size()) + 4.0 / static_cast<double>(s.size());
+}
+
+// ---------------------------------------------------------------------------
+// contraction drivers
+
+kamsta_status Solve::contract(const SegList* L, uint32_t wmin, uint32_t wmax, double frac) {
+  if ((L && L->total == 0) || nreps_ <= 1) return KAMSTA_OK;
   fill_inf(minA_, nreps_);
-  uint64_t counts[kMaxOut + 1];
-  Rec* out[1] = {E1_};
-  const uint64_t cap[1] = {Ecap_};
-  if (L)
-    KS_TRY(pass_rec<1>(L, m, D_, wmin, wmax, nullptr, out, cap, minA_, counts));
-  else
-    KS_TRY(pass_dir<1>(md_, D_, wmin, wmax, nullptr, out, cap, minA_, false, counts));
-  if (counts[0] == 0) return KAMSTA_OK;
-  return rounds(E1_, counts[0]);
+  SegList* E = new_list();
+  SegList* outs[1] = {E};
+  const double f[1] = {frac};
+  KS_TRY(pass<1>(KAMSTA_PHASE_CLASS_PASS, L, D_, wmin, wmax, nullptr, outs, f, minA_, nreps_,
+                 false));
+  return rounds(E, true);
 }
 
 kamsta_status Solve::run_boruvka() {
@@ -547,51 +684,91 @@ kamsta_status Solve::run_boruvka() {
   // first pass: classes 0..nmat-1, class 0 with identity labels and the
   // round-0 minimum fused in
   fill_inf(minA_, n_);
-  uint64_t counts[kMaxOut + 1];
+  SegList* C[kMaxOut] = {new_list(), new_list(), new_list()};
+  double frac[kMaxOut] = {1.0, 1.0, 1.0};
+  if (K > 0)
+    for (int c = 0; c < nmat; ++c)
+      frac[c] = sample_share(samples_host_, c == 0 ? 0u : b[c - 1] + 1, b[c]);
   const bool validate = (cfg_.flags & KAMSTA_FLAG_VALIDATE) != 0;
-  tolerate_overflow_ = true;
   switch (nmat) {
     case 1:
-      KS_TRY(pass_dir<1>(md_, nullptr, 0, wmax0, nullptr, C_, Ccap_, minA_, validate, counts));
+      KS_TRY(pass<1>(KAMSTA_PHASE_FIRST_PASS, nullptr, nullptr, 0, wmax0, nullptr, C, frac, minA_,
+                     n_, validate));
       break;
     case 2:
-      KS_TRY(pass_dir<2>(md_, nullptr, 0, wmax0, b.data(), C_, Ccap_, minA_, validate, counts));
+      KS_TRY(pass<2>(KAMSTA_PHASE_FIRST_PASS, nullptr, nullptr, 0, wmax0, b.data(), C, frac,
+                     minA_, n_, validate));
       break;
     default:
-      KS_TRY(pass_dir<3>(md_, nullptr, 0, wmax0, b.data(), C_, Ccap_, minA_, validate, counts));
+      KS_TRY(pass<3>(KAMSTA_PHASE_FIRST_PASS, nullptr, nullptr, 0, wmax0, b.data(), C, frac,
+                     minA_, n_, validate));
       break;
   }
-  tolerate_overflow_ = false;
-  bool overflow = false;
-  for (int c = 0; c < nmat; ++c) overflow |= counts[c] > Ccap_[c];
-  if (overflow) {  // the sample under-estimated a class: rerun with exact sizes
-    for (int c = 0; c < nmat; ++c) Ccap_[c] = counts[c];
-    return kRetry;
+  for (int c = 0; c < nmat; ++c) KS_TRY(debug_list("after first pass", *C[c], n_));
+  KS_TRY(rounds(C[0], true));
+  for (int c = 1; c < nmat; ++c) {
+    KS_TRY(contract(C[c], 0, 0xffffffffu, 1.0));
+    free_list(C[c]);
   }
-  uint64_t ecap = counts[kMaxOut];
-  for (int c = 0; c < nmat; ++c) ecap = std::max(ecap, counts[c]);
-  KS_TRY(ensure_edges(ecap));
-  KS_TRY(rounds(C_[0], counts[0]));
-  for (int c = 1; c < nmat; ++c)
-    KS_TRY(contract_list(C_[c], counts[c], 0, 0xffffffffu));
   for (int c = nmat; c <= K; ++c) {
     const uint32_t lo = b[c - 1] + 1;
     const uint32_t hi = c < K ? b[c] : 0xffffffffu;
-    KS_TRY(contract_list(nullptr, md_, lo, hi));
+    KS_TRY(contract(nullptr, lo, hi, sample_share(samples_host_, lo, hi)));
   }
   return KAMSTA_OK;
 }
 
-kamsta_status Solve::filter_rec(Rec* L, uint64_t m, bool stop, int depth) {
-  (void)L;
-  (void)m;
-  (void)stop;
-  (void)depth;
-  set_error("filter_boruvka: not built yet");
-  return KAMSTA_E_UNSUPPORTED;
+// filter_boruvka's recursion (boruvka_recursive, hybrid_boruvka_edgefilter.hpp:
+// 227-330): contract directly when the average degree is at most
+// filter_threshold, the recursion was told to stop, or the graph is small;
+// otherwise split at the median sampled weight (select_pivot,
+// distributed_partitioning.hpp:91-119), recurse on the light part, relabel
+// the heavy part by the components found and drop its internal edges
+// (boruvka_recursive_setup, :173-225), recurse on what is left.  A light
+// share above 85% stops the next level (partition_edges,
+// filter_helpers.hpp:130-133).  L == nullptr is the directed input.
+kamsta_status Solve::filter_rec(SegList* L, bool own, bool stop, int depth) {
+  const uint64_t m_und = L ? L->total : md_ / 2;  // the input holds m_directed/2 edges
+  if (m_und == 0 || nreps_ <= 1) {
+    if (own) free_list(L);
+    return KAMSTA_OK;
+  }
+  const double avg_degree = 2.0 * static_cast<double>(m_und) / static_cast<double>(n_);
+  if (avg_degree <= static_cast<double>(cfg_.filter_threshold) || stop || 2 * m_und <= 1000 ||
+      depth >= 48) {
+    KS_TRY(contract(L, 0, 0xffffffffu, 1.0));
+    if (own) free_list(L);
+    return KAMSTA_OK;
+  }
+  std::vector<uint32_t> s;
+  KS_TRY(sample_weights(L, kSamples, &s));
+  const uint32_t pivot = s[s.size() / 2];
+  SegList* light = new_list();
+  SegList* heavy = new_list();
+  SegList* outs[2] = {light, heavy};
+  const double frac[2] = {sample_share(s, 0, pivot), 1.0};
+  const uint32_t thr[1] = {pivot};
+  KS_TRY(pass<2>(KAMSTA_PHASE_CLASS_PASS, L, nullptr, 0, 0xffffffffu, thr, outs, frac, nullptr, 0,
+                 false));
+  if (own) free_list(L);
+  const uint64_t tot = light->total + heavy->total;
+  const bool stop_next = tot == 0 || static_cast<double>(light->total) / tot > 0.85;
+  KS_TRY(filter_rec(light, true, stop_next, depth + 1));
+  if (nreps_ <= 1 || heavy->total == 0) {
+    free_list(heavy);
+    return KAMSTA_OK;
+  }
+  SegList* kept = new_list();
+  SegList* kouts[1] = {kept};
+  KS_TRY(pass<1>(KAMSTA_PHASE_CLASS_PASS, heavy, P_, 0, 0xffffffffu, nullptr, kouts, nullptr,
+                 nullptr, 0, false));
+  free_list(heavy);
+  return filter_rec(kept, true, false, depth + 1);
 }
 
-kamsta_status Solve::run_filter_boruvka() { return filter_rec(nullptr, md_ / 2, false, 0); }
+kamsta_status Solve::run_filter_boruvka() { return filter_rec(nullptr, false, false, 0); }
+
+// ---------------------------------------------------------------------------
 
 kamsta_status Solve::run(Algo algo, kamsta_wedge* d_out, SolveOut* out) {
   out->count = 0;
@@ -606,60 +783,51 @@ kamsta_status Solve::run(Algo algo, kamsta_wedge* d_out, SolveOut* out) {
   CU_TRY(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
   aligned16_ = (reinterpret_cast<uintptr_t>(in_) & 15u) == 0;
   samples_ = ctx_->d_samples;
+  {
+    const char* dbg = std::getenv("KAMSTA_DEBUG_CHECKS");
+    debug_ = dbg && dbg[0] == '1';
+  }
+  {  // per device context; cheap
+    const int dd = static_cast<int>(kDirDynSmem), dr = static_cast<int>(kRecDynSmem);
+    CU_TRY(cudaFuncSetAttribute(k_pass_dir<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, dd));
+    CU_TRY(cudaFuncSetAttribute(k_pass_dir<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, dd));
+    CU_TRY(cudaFuncSetAttribute(k_pass_dir<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, dd));
+    CU_TRY(cudaFuncSetAttribute(k_pass_seg<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, dr));
+    CU_TRY(cudaFuncSetAttribute(k_pass_seg<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, dr));
+    CU_TRY(cudaFuncSetAttribute(k_pass_seg<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, dr));
+  }
+  KS_TRY(alloc_fixed());
   CU_TRY(cudaEventRecord(ctx_->ev0, st_));
-  const uint64_t mu = md_ / 2 + 1;
+  // filter_boruvka runs the local contraction first when local preprocessing
+  // is requested (filter_boruvka_setup_and_preprocessing,
+  // hybrid_boruvka_edgefilter.hpp:375-418); on one device that contraction
+  // covers every edge, so the distributed recursion has nothing left.
+  if (algo == Algo::kFilterBoruvka && cfg_.local_preprocessing != KAMSTA_NO_PREPROCESSING)
+    algo = Algo::kBoruvka;
   if (algo == Algo::kBoruvka) {
-    // class bounds (ascending) and class-list capacities from the sample
     std::vector<uint32_t> thr_desc = plan_classes();
     bounds_.assign(thr_desc.rbegin(), thr_desc.rend());
-    const int K = static_cast<int>(bounds_.size());
-    const int nmat = std::max(1, std::min(K, kMaxOut));
-    for (int c = 0; c < kMaxOut; ++c) Ccap_[c] = 0;
-    if (K == 0) {
-      Ccap_[0] = mu;
-    } else {
-      const double S = static_cast<double>(std::max<size_t>(samples_host_.size(), 1));
-      for (int c = 0; c < nmat; ++c) {
-        const uint32_t lo = c == 0 ? 0u : bounds_[c - 1] + 1;
-        const uint32_t hi = bounds_[c];
-        const double k = static_cast<double>(
-            std::upper_bound(samples_host_.begin(), samples_host_.end(), hi) -
-            std::lower_bound(samples_host_.begin(), samples_host_.end(), lo));
-        const double f = k / S;
-        const double est = f + 6.0 * std::sqrt(f * (1.0 - f) / S + 1.0 / (S * S)) + 4.0 / S;
-        Ccap_[c] = std::min<uint64_t>(mu, static_cast<uint64_t>(est * static_cast<double>(mu)) + 4096);
-      }
-    }
   }
-  for (int attempt = 0;; ++attempt) {
-    KS_TRY(alloc_fixed());
-    k_iota<<<grid_for(n_), kBlock, 0, st_>>>(n_, P_);
-    k_iota<<<grid_for(n_), kBlock, 0, st_>>>(n_, V_);
-    k_iota<<<grid_for(n_), kBlock, 0, st_>>>(n_, D_);
-    launches_ += 3;
-    nreps_ = n_;
-    msf_count_ = 0;
-    CU_TRY(cudaMemsetAsync(ctx_->d_err, 0, sizeof(uint32_t), st_));
-    const kamsta_status s = algo == Algo::kBoruvka ? run_boruvka() : run_filter_boruvka();
-    if (s == kRetry && attempt == 0) continue;
-    if (s == kRetry) {
-      set_error("internal: class buffer overflow after resize");
-      return KAMSTA_E_CUDA;
-    }
-    KS_TRY(s);
-    break;
-  }
+  k_iota<<<grid_for(n_), kBlock, 0, st_>>>(n_, P_);
+  k_iota<<<grid_for(n_), kBlock, 0, st_>>>(n_, V_);
+  k_iota<<<grid_for(n_), kBlock, 0, st_>>>(n_, D_);
+  account(KAMSTA_PHASE_FINALIZE, uint64_t(n_) * 12, 3);
+  nreps_ = n_;
+  msf_count_ = 0;
+  CU_TRY(cudaMemsetAsync(ctx_->d_err, 0, sizeof(uint32_t), st_));
+  KS_TRY(algo == Algo::kBoruvka ? run_boruvka() : run_filter_boruvka());
   // forest output
   CU_TRY(cudaMemsetAsync(ctx_->d_counters + kCMisc, 0, sizeof(DevCounters), st_));
   if (msf_count_ > 0) {
-    k_emit<<<grid_for(msf_count_), kBlock, 0, st_>>>(
-        msf_count_, msf_, in_, reinterpret_cast<uint32_t*>(d_out),
-        &ctx_->d_counters[kCMisc].weight);
-    launches_++;
+    const int tm = tick();
+    k_emit<<<grid_for(msf_count_), kBlock, 0, st_>>>(msf_count_, msf_, in_,
+                                                      reinterpret_cast<uint32_t*>(d_out),
+                                                      &ctx_->d_counters[kCMisc].weight);
+    tock(KAMSTA_PHASE_EMIT, tm);
+    account(KAMSTA_PHASE_EMIT, msf_count_ * (4 + 12 + 12), 1);
   }
   CU_TRY(cudaEventRecord(ctx_->ev1, st_));
-  KS_TRY(fetch_counters(kCMisc, 1));
-  alg_bytes_ += msf_count_ * (4 + 12 + 12);
+  KS_TRY(fetch_counters());
   out->count = msf_count_;
   out->weight = ctx_->h_counters[kCMisc].weight;
   if (stats_) {
@@ -672,6 +840,11 @@ kamsta_status Solve::run(Algo algo, kamsta_wedge* d_out, SolveOut* out) {
     stats_->gpu_launches = launches_;
     stats_->device_ms = ms;
     stats_->alg_bytes = alg_bytes_;
+    for (int k = 0; k < KAMSTA_PHASES; ++k) {
+      stats_->phase_ms[k] = phase_ms_[k];
+      stats_->phase_bytes[k] = phase_bytes_[k];
+      stats_->phase_launches[k] = phase_launches_[k];
+    }
   }
   return KAMSTA_OK;
 }
@@ -680,9 +853,7 @@ kamsta_status solve_device(kamsta_ctx* ctx, Algo algo, const kamsta_wedge* d_in,
                            uint64_t m_directed, uint32_t n, const kamsta_cfg& cfg,
                            kamsta_wedge* d_out, SolveOut* out, kamsta_stats* st,
                            cudaStream_t stream) {
-  if (st) {
-    std::memset(st, 0, sizeof(*st));
-  }
+  if (st) std::memset(st, 0, sizeof(*st));
   Solve s(ctx, stream ? stream : ctx->stream, d_in, m_directed, n, cfg, st);
   return s.run(algo, d_out, out);
 }

@@ -44,20 +44,23 @@ static_assert(sizeof(DevCounters) == 128, "counter block size");
 
 enum CounterSlot : int { kCVertex = 0, kCEdge = 1, kCRep = 2, kCMisc = 3, kCSlots = 4 };
 constexpr uint32_t kSampleCap = 4096;
+constexpr int kTimerEvents = 64;
 
 }  // namespace kamsta
 
 struct kamsta_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
-  kamsta::Arena fixed;   // vertex arrays, class lists, status words
-  kamsta::Arena edges;   // round ping-pong lists (sized after the first pass)
+  kamsta::Arena fixed;   // vertex arrays and look-back words
+  cudaMemPool_t pool = nullptr;  // edge lists (stream-ordered, cached between calls)
   kamsta::DevCounters* d_counters = nullptr;  // kCSlots blocks
   uint32_t* d_samples = nullptr;               // weight samples (kSampleCap)
   uint32_t* d_err = nullptr;
   kamsta::DevCounters* h_counters = nullptr;  // pinned mirror
   uint32_t* h_err = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t tev[kamsta::kTimerEvents] = {};  // per-phase timing events
+  kamsta::Arena io;      // host-buffer entry points: device copies of in/out
   std::mutex mu;
 };
 

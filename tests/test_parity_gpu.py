@@ -23,10 +23,12 @@ def _configs(K):
     return {
         "boruvka_plain": (K.boruvka, K.AlgorithmConfig(local_preprocessing=LP.NO_PREPROCESSING)),
         "boruvka_local": (K.boruvka, K.AlgorithmConfig(local_preprocessing=LP.MODIFIED_BORUVKA)),
+        "filter_boruvka": (K.filter_boruvka, K.AlgorithmConfig()),
+        "filter_boruvka_t1": (K.filter_boruvka, K.AlgorithmConfig(filter_threshold=1)),
     }
 
 
-ALGOS = ["boruvka_plain", "boruvka_local"]
+ALGOS = ["boruvka_plain", "boruvka_local", "filter_boruvka", "filter_boruvka_t1"]
 
 
 def _triples(mst):
@@ -182,7 +184,7 @@ def test_device_generator_matches_oracle(kamsta, oracle, n, m):
     assert np.array_equal(host, oracle.gen_gnm(n, m, 5))
 
 
-@pytest.mark.parametrize("algo", ALGOS)
+@pytest.mark.parametrize("algo", ["boruvka_plain", "boruvka_local", "filter_boruvka"])
 def test_exactness_n22_m26(kamsta, oracle, algo):
     """The bit-exact check size of the large configuration: G(n=2^22, m=2^26)."""
     fn, cfg = _configs(kamsta)[algo]
