@@ -211,8 +211,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 // Bounded wait for phase `parity` of `bar`; false (and kErrSpin) on timeout.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t* err) {
-  for (uint32_t i = 0; i < kSpinCap; ++i)
+  for (uint32_t i = 0; i < kSpinCap; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
+  }
   atomicOr(err, kErrSpin);
   return false;
 }

@@ -57,6 +57,11 @@ struct SegOut {
 // minimum (minval) with the value (w << 32 | position).
 struct PassArgs {
   const uint32_t* map;  // label map; nullptr = identity
+  // Optional membership bitmap of the largest component (bit x set iff
+  // map[x] == big_label): an edge with both endpoints inside is dropped
+  // without gathering map[], and one inside endpoint needs no gather.
+  const uint32_t* big;
+  uint32_t big_label;
   uint32_t wmin, wmax;
   uint32_t thr[kMaxOut];
   SegOut out[kMaxOut];
@@ -70,6 +75,22 @@ struct PassArgs {
   uint32_t validate;  // check id range and (src,dst) order (directed source)
   uint32_t aligned16; // directed source base is 16-byte aligned
 };
+
+// Relabel both endpoints; false when they land in the same component.
+__device__ __forceinline__ bool relabel(const PassArgs& p, uint32_t s, uint32_t d, uint32_t& la,
+                                        uint32_t& lb) {
+  if (p.big) {
+    const bool bs = (__ldg(p.big + (s >> 5)) >> (s & 31)) & 1u;
+    const bool bd = (__ldg(p.big + (d >> 5)) >> (d & 31)) & 1u;
+    if (bs && bd) return false;
+    la = bs ? p.big_label : p.map[s];
+    lb = bd ? p.big_label : p.map[d];
+  } else {
+    la = p.map[s];
+    lb = p.map[d];
+  }
+  return la != lb;
+}
 
 template <int NOUT>
 __device__ __forceinline__ uint8_t weight_class(uint32_t w, const PassArgs& p) {
@@ -277,8 +298,8 @@ __global__ void __launch_bounds__(kBlock, 3)
       }
       ++cand;
       if (p.map) {
-        const uint32_t la = p.map[s], lb = p.map[d];
-        if (la == lb) continue;
+        uint32_t la, lb;
+        if (!relabel(p, s, d, la, lb)) continue;
         words[3 * t] = la;  // item t belongs to this thread alone
         words[3 * t + 1] = lb;
       }
@@ -439,9 +460,8 @@ __global__ void __launch_bounds__(kBlock, 3)
         continue;
       }
       ++cand;
-      const uint32_t la = p.map ? p.map[r.a] : r.a;
-      const uint32_t lb = p.map ? p.map[r.b] : r.b;
-      if (la == lb) continue;
+      uint32_t la = r.a, lb = r.b;
+      if (p.map && !relabel(p, r.a, r.b, la, lb)) continue;
       recs[t].a = la;
       recs[t].b = lb;
       cls[j] = weight_class<NOUT>(r.w, p);
@@ -539,11 +559,15 @@ __global__ void k_jump_finish(uint32_t n, uint32_t* parent, uint32_t* err) {
 }
 
 // Renumbering and forest-edge emission (compactify_vertices +
-// add_new_mst_edges_to_mst_array).  Class 0: live roots -> dense new ids,
-// carry their original representative and reset the next minimum.  Class 1:
-// hooked vertices -> append the edge id of their minimum edge to the forest.
+// add_new_mst_edges_to_mst_array), without a cross-CTA scan: CTA c owns the
+// vertex chunk [c*chunk, (c+1)*chunk).  k_vertex_count counts its live roots
+// (class 0: dense new ids, original representative carried, next minimum
+// reset) and hooked vertices (class 1: forest edge appended); k_vertex_write
+// sums the counts of the CTAs before it and writes, in vertex order, so ids
+// and the forest order are deterministic.
 struct VertexScanArgs {
   uint32_t n;
+  uint32_t chunk;  // vertices per CTA (multiple of kBlock)
   const uint32_t* parent;
   const uint64_t* minval;
   const uint32_t* msfoid;
@@ -551,70 +575,106 @@ struct VertexScanArgs {
   uint32_t* orig_next;
   uint32_t* newid;
   uint64_t* minval_next;
-  uint32_t* msf_out;  // already offset by the forest edges found so far
-  uint64_t msf_cap;   // entries available at msf_out
-  uint64_t orig_cap;  // entries available at orig_next / minval_next
-  uint64_t* status[2];
-  unsigned long long* counts;  // [0] roots, [1] forest edges
-  uint32_t* ticket;
+  uint32_t* msf_out;   // already offset by the forest edges found so far
+  uint64_t msf_cap;    // entries available at msf_out
+  uint64_t orig_cap;   // entries available at orig_next / minval_next
+  uint32_t* cta_counts;  // 2 per CTA: roots, hooked
+  unsigned long long* counts;  // [0] roots, [1] forest edges (totals)
   uint32_t* err;
-  uint32_t ntiles;
 };
 
-__global__ void __launch_bounds__(kBlock) k_vertex_scan(VertexScanArgs p) {
-  constexpr int TILE = kItemsVtx * kBlock;
-  __shared__ uint32_t s_rank[2 * kItemsVtx * (kBlock / 32)];
-  __shared__ uint32_t s_tot[2];
-  __shared__ uint64_t s_pre[2];
-  for (;;) {
-    const uint32_t tile = next_tile(p.ticket);
-    if (tile >= p.ntiles) return;
-    const uint64_t base = static_cast<uint64_t>(tile) * TILE;
-    uint8_t cls[kItemsVtx];
-    uint32_t offs[kItemsVtx];
-#pragma unroll
-    for (int j = 0; j < kItemsVtx; ++j) {
-      const uint64_t v = base + j * kBlock + threadIdx.x;
-      cls[j] = 0xff;
-      offs[j] = 0;
-      if (v >= p.n) continue;
-      const uint32_t par = p.parent[v];
-      if (par != v)
-        cls[j] = 1;
-      else if (p.minval[v] != kInf64)
-        cls[j] = 0;
+__device__ __forceinline__ uint32_t vertex_class(const VertexScanArgs& p, uint32_t v) {
+  if (v >= p.n) return 2;
+  const uint32_t par = p.parent[v];
+  if (par != v) return 1;
+  return p.minval[v] != kInf64 ? 0u : 2u;
+}
+
+__global__ void __launch_bounds__(kBlock) k_vertex_count(VertexScanArgs p) {
+  const uint32_t lo = blockIdx.x * p.chunk;
+  const uint32_t hi = min(lo + p.chunk, p.n);
+  uint32_t c0 = 0, c1 = 0;
+  for (uint32_t v = lo + threadIdx.x; v < hi; v += kBlock) {
+    const uint32_t c = vertex_class(p, v);
+    c0 += c == 0;
+    c1 += c == 1;
+  }
+  __shared__ uint32_t s_c[2];
+  if (threadIdx.x < 2) s_c[threadIdx.x] = 0;
+  __syncthreads();
+  c0 = warp_sum(c0);
+  c1 = warp_sum(c1);
+  if (lane_id() == 0) {
+    if (c0) atomicAdd(&s_c[0], c0);
+    if (c1) atomicAdd(&s_c[1], c1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    p.cta_counts[2 * blockIdx.x] = s_c[0];
+    p.cta_counts[2 * blockIdx.x + 1] = s_c[1];
+    if (s_c[0]) atomicAdd(&p.counts[0], static_cast<unsigned long long>(s_c[0]));
+    if (s_c[1]) atomicAdd(&p.counts[1], static_cast<unsigned long long>(s_c[1]));
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_vertex_write(VertexScanArgs p) {
+  __shared__ uint32_t s_base[2];
+  __shared__ uint32_t s_w[2][kBlock / 32];
+  if (threadIdx.x < 32) {  // bases: counts of the CTAs before this one
+    uint32_t b0 = 0, b1 = 0;
+    for (uint32_t c = threadIdx.x; c < blockIdx.x; c += 32) {
+      b0 += p.cta_counts[2 * c];
+      b1 += p.cta_counts[2 * c + 1];
     }
-    tile_rank<2, kItemsVtx, kBlock>(cls, offs, s_rank, s_tot);
-    const uint32_t warp = threadIdx.x >> 5;
-    if (warp < 2) {
-      const uint64_t pre = lookback(p.status[warp], tile, s_tot[warp], p.err);
-      if (lane_id() == 0) {
-        s_pre[warp] = pre;
-        if (s_tot[warp]) atomicAdd(&p.counts[warp], static_cast<unsigned long long>(s_tot[warp]));
-      }
+    b0 = warp_sum(b0);
+    b1 = warp_sum(b1);
+    if (threadIdx.x == 0) {
+      s_base[0] = b0;
+      s_base[1] = b1;
+    }
+  }
+  __syncthreads();
+  const uint32_t lo = blockIdx.x * p.chunk;
+  const uint32_t hi = min(lo + p.chunk, p.n);
+  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5, lt = lanemask_lt();
+  uint32_t run0 = s_base[0], run1 = s_base[1];
+  for (uint32_t v0 = lo; v0 < hi; v0 += kBlock) {  // rows of kBlock vertices, in order
+    const uint32_t v = v0 + threadIdx.x;
+    const uint32_t c = v < hi ? vertex_class(p, v) : 2u;
+    const uint32_t b0 = __ballot_sync(kFull, c == 0), b1 = __ballot_sync(kFull, c == 1);
+    if (lane == 0) {
+      s_w[0][warp] = __popc(b0);
+      s_w[1][warp] = __popc(b1);
     }
     __syncthreads();
+    uint32_t pre0 = run0, pre1 = run1, tot0 = 0, tot1 = 0;
 #pragma unroll
-    for (int j = 0; j < kItemsVtx; ++j) {
-      const uint64_t v = base + j * kBlock + threadIdx.x;
-      if (cls[j] == 0) {
-        const uint64_t id = s_pre[0] + offs[j];
-        if (id >= p.orig_cap) {
-          atomicOr(p.err, kErrOverflow);
-          continue;
-        }
-        p.newid[v] = static_cast<uint32_t>(id);
+    for (int w = 0; w < kBlock / 32; ++w) {
+      const uint32_t x0 = s_w[0][w], x1 = s_w[1][w];
+      pre0 += static_cast<uint32_t>(w) < warp ? x0 : 0u;
+      pre1 += static_cast<uint32_t>(w) < warp ? x1 : 0u;
+      tot0 += x0;
+      tot1 += x1;
+    }
+    __syncthreads();
+    if (c == 0) {
+      const uint32_t id = pre0 + __popc(b0 & lt);
+      if (id < p.orig_cap) {
+        p.newid[v] = id;
         p.orig_next[id] = p.orig_cur[v];
         p.minval_next[id] = kInf64;
-      } else if (cls[j] == 1) {
-        const uint64_t k = s_pre[1] + offs[j];
-        if (k >= p.msf_cap) {
-          atomicOr(p.err, kErrOverflow);
-          continue;
-        }
-        p.msf_out[k] = p.msfoid[v];
+      } else {
+        atomicOr(p.err, kErrOverflow);
       }
+    } else if (c == 1) {
+      const uint32_t k = pre1 + __popc(b1 & lt);
+      if (k < p.msf_cap)
+        p.msf_out[k] = p.msfoid[v];
+      else
+        atomicOr(p.err, kErrOverflow);
     }
+    run0 += tot0;
+    run1 += tot1;
   }
 }
 
@@ -661,58 +721,94 @@ __global__ void k_chase(ChaseArgs p) {
 }
 
 // New representative list of the call (V' = {v in V : P[v] == v}, stable)
-// and the dense numbering of those representatives.
+// and the dense numbering of those representatives; count + write kernels
+// over per-CTA chunks as for the vertex scan.
 struct RepScanArgs {
   uint32_t n;
+  uint32_t chunk;
   const uint32_t* V;
   const uint32_t* P;
   uint32_t* Vout;
   uint32_t* dense_of;
-  uint64_t* status;
+  uint32_t* cta_counts;
   unsigned long long* counts;
-  uint32_t* ticket;
   uint32_t* err;
-  uint32_t ntiles;
 };
 
-__global__ void __launch_bounds__(kBlock) k_rep_scan(RepScanArgs p) {
-  constexpr int TILE = kItemsVtx * kBlock;
-  __shared__ uint32_t s_rank[kItemsVtx * (kBlock / 32)];
-  __shared__ uint32_t s_tot[1];
-  __shared__ uint64_t s_pre;
-  for (;;) {
-    const uint32_t tile = next_tile(p.ticket);
-    if (tile >= p.ntiles) return;
-    const uint64_t base = static_cast<uint64_t>(tile) * TILE;
-    uint8_t cls[kItemsVtx];
-    uint32_t offs[kItemsVtx], val[kItemsVtx];
+__global__ void __launch_bounds__(kBlock) k_rep_count(RepScanArgs p) {
+  const uint32_t lo = blockIdx.x * p.chunk;
+  const uint32_t hi = min(lo + p.chunk, p.n);
+  uint32_t c0 = 0;
+  for (uint32_t i = lo + threadIdx.x; i < hi; i += kBlock) {
+    const uint32_t v = p.V[i];
+    c0 += p.P[v] == v;
+  }
+  __shared__ uint32_t s_c;
+  if (threadIdx.x == 0) s_c = 0;
+  __syncthreads();
+  c0 = warp_sum(c0);
+  if (lane_id() == 0 && c0) atomicAdd(&s_c, c0);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    p.cta_counts[blockIdx.x] = s_c;
+    if (s_c) atomicAdd(&p.counts[0], static_cast<unsigned long long>(s_c));
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_rep_write(RepScanArgs p) {
+  __shared__ uint32_t s_base;
+  __shared__ uint32_t s_w[kBlock / 32];
+  if (threadIdx.x < 32) {
+    uint32_t b = 0;
+    for (uint32_t c = threadIdx.x; c < blockIdx.x; c += 32) b += p.cta_counts[c];
+    b = warp_sum(b);
+    if (threadIdx.x == 0) s_base = b;
+  }
+  __syncthreads();
+  const uint32_t lo = blockIdx.x * p.chunk;
+  const uint32_t hi = min(lo + p.chunk, p.n);
+  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5, lt = lanemask_lt();
+  uint32_t run = s_base;
+  for (uint32_t i0 = lo; i0 < hi; i0 += kBlock) {
+    const uint32_t i = i0 + threadIdx.x;
+    const uint32_t v = i < hi ? p.V[i] : 0u;
+    const bool keep = i < hi && p.P[v] == v;
+    const uint32_t b = __ballot_sync(kFull, keep);
+    if (lane == 0) s_w[warp] = __popc(b);
+    __syncthreads();
+    uint32_t pre = run, tot = 0;
 #pragma unroll
-    for (int j = 0; j < kItemsVtx; ++j) {
-      const uint64_t i = base + j * kBlock + threadIdx.x;
-      cls[j] = 0xff;
-      offs[j] = 0;
-      val[j] = 0;
-      if (i >= p.n) continue;
-      val[j] = p.V[i];
-      if (p.P[val[j]] == val[j]) cls[j] = 0;
-    }
-    tile_rank<1, kItemsVtx, kBlock>(cls, offs, s_rank, s_tot);
-    if ((threadIdx.x >> 5) == 0) {
-      const uint64_t pre = lookback(p.status, tile, s_tot[0], p.err);
-      if (lane_id() == 0) {
-        s_pre = pre;
-        if (s_tot[0]) atomicAdd(&p.counts[0], static_cast<unsigned long long>(s_tot[0]));
-      }
+    for (int w = 0; w < kBlock / 32; ++w) {
+      pre += static_cast<uint32_t>(w) < warp ? s_w[w] : 0u;
+      tot += s_w[w];
     }
     __syncthreads();
-#pragma unroll
-    for (int j = 0; j < kItemsVtx; ++j) {
-      if (cls[j] != 0) continue;
-      const uint32_t k = static_cast<uint32_t>(s_pre + offs[j]);
-      p.Vout[k] = val[j];
-      p.dense_of[val[j]] = k;
+    if (keep) {
+      const uint32_t k = pre + __popc(b & lt);
+      p.Vout[k] = v;
+      p.dense_of[v] = k;
     }
+    run += tot;
   }
+}
+
+// Membership bitmap of component `g`: bit x set iff D[x] == g.
+__global__ void k_big_bitmap(uint32_t n, const uint32_t* __restrict__ D, uint32_t g,
+                             uint32_t* __restrict__ bits) {
+  const uint32_t words = (n + 31) / 32;
+  for (uint32_t wi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; wi < words;
+       wi += (gridDim.x * blockDim.x) >> 5) {
+    const uint32_t x = wi * 32 + lane_id();
+    const uint32_t b = __ballot_sync(kFull, x < n && D[x] == g);
+    if (lane_id() == 0) bits[wi] = b;
+  }
+}
+
+// D at `count` pseudo-random vertices (for picking the largest component).
+__global__ void k_sample_labels(uint32_t n, const uint32_t* __restrict__ D, uint64_t seed,
+                                uint32_t count, uint32_t* out) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+    out[i] = D[__umul64hi(mix64(seed ^ (0x9e3779b97f4a7c15ull * (i + 1))), n)];
 }
 
 // Shortcut every original vertex to its new representative and compute its

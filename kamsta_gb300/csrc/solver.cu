@@ -78,7 +78,6 @@ static inline uint32_t ceil_div(uint64_t a, uint64_t b) {
   return static_cast<uint32_t>((a + b - 1) / b);
 }
 
-constexpr uint32_t kTileVtx = kItemsVtx * kBlock;
 constexpr uint32_t kSamples = 4096;
 
 template <typename K>
@@ -147,6 +146,12 @@ class Solve {
   // [wmin, wmax], a share `frac` of the entries) into the current dense
   // labels, fuse the round-0 minimum and contract the result.
   kamsta_status contract(const SegList* L, uint32_t wmin, uint32_t wmax, double frac);
+  // Largest current component (mode of sampled labels); when it holds at
+  // least half the vertices, its membership bitmap is built into big_ and
+  // the next D-relabelling pass skips gathers for edges inside it.
+  kamsta_status pick_big(uint32_t* label, bool* use);
+  bool use_big_ = false;
+  uint32_t big_label_ = 0;
   std::vector<uint32_t> plan_classes();
   kamsta_status sample_weights(const SegList* L, uint32_t count, std::vector<uint32_t>* out);
   kamsta_status filter_rec(SegList* L, bool own, bool stop, int depth);
@@ -215,7 +220,8 @@ class Solve {
   uint32_t *dense_of_ = nullptr, *parent_ = nullptr, *msfoid_ = nullptr, *newid_ = nullptr;
   uint32_t *Rbuf_ = nullptr, *Obuf_ = nullptr, *msf_ = nullptr, *samples_ = nullptr;
   uint64_t *minA_ = nullptr, *minB_ = nullptr, *prefix_ = nullptr;
-  uint64_t* status_[3] = {};  // vertex-scan look-back words
+  uint32_t* cta_counts_ = nullptr;  // per-CTA counts of the vertex scans
+  uint32_t* big_ = nullptr;         // membership bitmap of the largest component
   uint32_t nreps_ = 0;
   uint64_t msf_count_ = 0;
   std::vector<uint32_t> bounds_;        // ascending weight-class bounds
@@ -227,7 +233,6 @@ class Solve {
 
 kamsta_status Solve::alloc_fixed() {
   const uint64_t n = n_;
-  const uint32_t vtiles = std::max(ceil_div(n, kTileVtx), 1u);
   size_t bytes = 0;
   auto add = [&](uint64_t count, size_t sz) { bytes += round_up(count * sz, 256); };
   for (int i = 0; i < 9; ++i) add(n + 1, 4);  // P D V Vn dense parent msfoid newid msf
@@ -236,7 +241,8 @@ kamsta_status Solve::alloc_fixed() {
   add(n + 1, 8);
   add(n + 1, 8);  // minA minB
   add(kMaxSeg + 1, 8);
-  for (int i = 0; i < 3; ++i) add(vtiles, 8);
+  add(2 * kMaxSeg, 4);
+  add(n / 32 + 2, 4);
   CU_TRY(ctx_->fixed.reserve(bytes + 4096));
   Arena& A = ctx_->fixed;
   P_ = A.take<uint32_t>(n + 1);
@@ -253,8 +259,9 @@ kamsta_status Solve::alloc_fixed() {
   minA_ = A.take<uint64_t>(n + 1);
   minB_ = A.take<uint64_t>(n + 1);
   prefix_ = A.take<uint64_t>(kMaxSeg + 1);
-  for (int i = 0; i < 3; ++i) status_[i] = A.take<uint64_t>(vtiles);
-  if (!status_[2]) {
+  cta_counts_ = A.take<uint32_t>(2 * kMaxSeg);
+  big_ = A.take<uint32_t>(n / 32 + 2);
+  if (!big_) {
     set_error("internal: fixed arena too small");
     return KAMSTA_E_OOM;
   }
@@ -409,6 +416,10 @@ kamsta_status Solve::pass(int phase, const SegList* src, const uint32_t* map, ui
     CU_TRY(cudaMemsetAsync(ctx_->d_counters + kCEdge, 0, sizeof(DevCounters), st_));
     PassArgs a{};
     a.map = map;
+    if (use_big_ && map == D_) {
+      a.big = big_;
+      a.big_label = big_label_;
+    }
     a.wmin = wmin;
     a.wmax = wmax;
     for (int c = 0; c < NOUT - 1; ++c) a.thr[c] = thr[c];
@@ -500,12 +511,15 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
     k_hook<<<gv, kBlock, 0, st_>>>(nr, minv, cur->base, parent_, msfoid_, ctx_->d_err);
     k_jump<<<gv, kBlock, 0, st_>>>(nr, parent_, ctx_->d_err);
     k_jump_finish<<<gv, kBlock, 0, st_>>>(nr, parent_, ctx_->d_err);
-    const uint32_t ntv = ceil_div(nr, kTileVtx);
-    CU_TRY(cudaMemsetAsync(status_[0], 0, sizeof(uint64_t) * ntv, st_));
-    CU_TRY(cudaMemsetAsync(status_[1], 0, sizeof(uint64_t) * ntv, st_));
     uint32_t* onext = Obuf_ + ooff;
     VertexScanArgs va{};
     va.n = nr;
+    {
+      const uint32_t g = std::max<uint32_t>(
+          1, std::min<uint32_t>(ceil_div(nr, kBlock * 8u), static_cast<uint32_t>(sms_) * 4));
+      va.chunk = static_cast<uint32_t>(round_up(ceil_div(nr, g), kBlock));
+    }
+    const uint32_t gvs = std::max<uint32_t>(1, ceil_div(nr, va.chunk));
     va.parent = parent_;
     va.minval = minv;
     va.msfoid = msfoid_;
@@ -516,14 +530,11 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
     va.msf_out = msf_ + msf_count_;
     va.msf_cap = (n_ + 1) - msf_count_;
     va.orig_cap = std::min<uint64_t>((n_ + 64) - ooff, n_ + 1);
-    va.status[0] = status_[0];
-    va.status[1] = status_[1];
+    va.cta_counts = cta_counts_;
     va.counts = ctx_->d_counters[kCVertex].cnt;
-    va.ticket = &ctx_->d_counters[kCVertex].ticket;
     va.err = ctx_->d_err;
-    va.ntiles = ntv;
-    k_vertex_scan<<<std::min<int>(ntv, blocks_per_sm(k_vertex_scan, 0) * sms_), kBlock, 0, st_>>>(
-        va);
+    k_vertex_count<<<gvs, kBlock, 0, st_>>>(va);
+    k_vertex_write<<<gvs, kBlock, 0, st_>>>(va);
     uint32_t* R = Rbuf_ + roff;
     k_map<<<gv, kBlock, 0, st_>>>(nr, minv, parent_, newid_, R);
     tock(KAMSTA_PHASE_ROUND_VERTS, tv);
@@ -540,7 +551,7 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
     account(KAMSTA_PHASE_ROUND_VERTS,
             uint64_t(nr) * ((8 + 16 + 8 + 8) + 16 + (4 + 8 + 4) + (8 + 4 + 4)) + n_next * 16 +
                 added * 8,
-            6);
+            7);
     if (debug_) {
       fprintf(stderr, "[kamsta debug] round %u: m=%llu n=%u -> m'=%llu n'=%llu forest+=%llu\n", r,
               (unsigned long long)m, nr, (unsigned long long)nxt->total,
@@ -573,27 +584,30 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
   ca.err = ctx_->d_err;
   const int tf = tick();
   k_chase<<<grid_for(n0), kBlock, 0, st_>>>(ca);
-  const uint32_t ntv = ceil_div(n0, kTileVtx);
   CU_TRY(cudaMemsetAsync(ctx_->d_counters + kCRep, 0, sizeof(DevCounters), st_));
-  CU_TRY(cudaMemsetAsync(status_[2], 0, sizeof(uint64_t) * ntv, st_));
   RepScanArgs ra{};
   ra.n = n0;
+  {
+    const uint32_t g = std::max<uint32_t>(
+        1, std::min<uint32_t>(ceil_div(n0, kBlock * 8u), static_cast<uint32_t>(sms_) * 4));
+    ra.chunk = static_cast<uint32_t>(round_up(ceil_div(n0, g), kBlock));
+  }
+  const uint32_t gr = std::max<uint32_t>(1, ceil_div(n0, ra.chunk));
   ra.V = V_;
   ra.P = P_;
   ra.Vout = Vn_;
   ra.dense_of = dense_of_;
-  ra.status = status_[2];
+  ra.cta_counts = cta_counts_;
   ra.counts = ctx_->d_counters[kCRep].cnt;
-  ra.ticket = &ctx_->d_counters[kCRep].ticket;
   ra.err = ctx_->d_err;
-  ra.ntiles = ntv;
-  k_rep_scan<<<std::min<int>(ntv, blocks_per_sm(k_rep_scan, 0) * sms_), kBlock, 0, st_>>>(ra);
+  k_rep_count<<<gr, kBlock, 0, st_>>>(ra);
+  k_rep_write<<<gr, kBlock, 0, st_>>>(ra);
   k_relabel_all<<<grid_for(n_), kBlock, 0, st_>>>(n_, P_, dense_of_, D_);
   tock(KAMSTA_PHASE_FINALIZE, tf);
   CU_TRY(cudaGetLastError());
   KS_TRY(fetch_counters());
   account(KAMSTA_PHASE_FINALIZE,
-          uint64_t(n0) * (4 * r + 12) + uint64_t(n0) * 16 + uint64_t(n_) * 16, 3);
+          uint64_t(n0) * (4 * r + 12) + uint64_t(n0) * 16 + uint64_t(n_) * 16, 4);
   nreps_ = static_cast<uint32_t>(ctx_->h_counters[kCRep].cnt[0]);
   std::swap(V_, Vn_);
   return KAMSTA_OK;
@@ -665,14 +679,46 @@ static double sample_share(const std::vector<uint32_t>& s, uint32_t lo, uint32_t
 // ---------------------------------------------------------------------------
 // contraction drivers
 
+kamsta_status Solve::pick_big(uint32_t* label, bool* use) {
+  *use = false;
+  if (n_ < (1u << 16) || nreps_ <= 1) return KAMSTA_OK;
+  const uint32_t count = kSamples;
+  k_sample_labels<<<grid_for(count), kBlock, 0, st_>>>(n_, D_, cfg_.seed ^ launches_, count,
+                                                       samples_);
+  std::vector<uint32_t> h(count);
+  CU_TRY(cudaMemcpyAsync(h.data(), samples_, count * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                         st_));
+  CU_TRY(cudaStreamSynchronize(st_));
+  std::sort(h.begin(), h.end());
+  uint32_t best = 0, best_len = 0;
+  for (size_t i = 0; i < h.size();) {
+    size_t j = i;
+    while (j < h.size() && h[j] == h[i]) ++j;
+    if (j - i > best_len) {
+      best_len = static_cast<uint32_t>(j - i);
+      best = h[i];
+    }
+    i = j;
+  }
+  if (best_len * 2 < count) return KAMSTA_OK;  // no dominant component
+  k_big_bitmap<<<grid_for(n_), kBlock, 0, st_>>>(n_, D_, best, big_);
+  account(KAMSTA_PHASE_CLASS_PASS, uint64_t(n_) * 4 + n_ / 8 + count * 8, 2);
+  *label = best;
+  *use = true;
+  return KAMSTA_OK;
+}
+
 kamsta_status Solve::contract(const SegList* L, uint32_t wmin, uint32_t wmax, double frac) {
   if ((L && L->total == 0) || nreps_ <= 1) return KAMSTA_OK;
   fill_inf(minA_, nreps_);
+  KS_TRY(pick_big(&big_label_, &use_big_));
   SegList* E = new_list();
   SegList* outs[1] = {E};
   const double f[1] = {frac};
-  KS_TRY(pass<1>(KAMSTA_PHASE_CLASS_PASS, L, D_, wmin, wmax, nullptr, outs, f, minA_, nreps_,
-                 false));
+  const kamsta_status s = pass<1>(KAMSTA_PHASE_CLASS_PASS, L, D_, wmin, wmax, nullptr, outs, f,
+                                  minA_, nreps_, false);
+  use_big_ = false;
+  KS_TRY(s);
   return rounds(E, true);
 }
 
