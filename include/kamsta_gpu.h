@@ -186,6 +186,22 @@ kamsta_status kamsta_mst_filter_boruvka_dev(kamsta_ctx* ctx,
                                             kamsta_stats* stats,
                                             kamsta_stream stream);
 
+/* ---- single-graph solve without any allocation -------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory (code inside another framework's fixed memory budget, allocator-
+ * less runtimes, plugins handed only a stream and buffers): same result as
+ * kamsta_mst_boruvka_dev, computed by one kernel whose scratch is a fixed
+ * array inside the library (about 5 MB, held by every device that loads the
+ * library until exit).  Limits: n <= 32768 and m_directed <= 262144, larger
+ * graphs are rejected with KAMSTA_E_INPUT.  d_edges / d_out are device
+ * pointers, out_count / total_weight host pointers; the call returns after
+ * the result is known.  The first call on a device looks up the array's
+ * device address, so make it before any stream capture.  Calls share the
+ * array: calls that overlap on the GPU race and must be serialised. */
+kamsta_status kamsta_mst_boruvka_noalloc(const kamsta_wedge* d_edges, uint64_t m_directed,
+                                         uint32_t n, kamsta_wedge* d_out, uint64_t* out_count,
+                                         uint64_t* total_weight, kamsta_stream stream);
+
 /* ---- device graph generators (seeded; identical to the oracle's CPU
  * generators).  d_out must hold 2*m entries; *m_directed_out receives the
  * number written.  Stand-ins for KaGen's get_gnm / get_rgg2D / get_rhg

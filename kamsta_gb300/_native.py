@@ -88,6 +88,7 @@ SIGNATURES = {
     "kamsta_mst_filter_boruvka_dev": (I32, [P, P, U64, U32, C.POINTER(Cfg), P, C.POINTER(U64),
                                             C.POINTER(Stats), P]),
     "kamsta_gen_gnm_dev": (I32, [P, U32, U64, U64, U32, P, C.POINTER(U64), P]),
+    "kamsta_mst_boruvka_noalloc": (I32, [P, U64, U32, P, C.POINTER(U64), C.POINTER(U64), P]),
 }
 
 
