@@ -267,10 +267,10 @@ def main():
     bytes_per_launch = fp["bytes"] / max(fp["launches"], 1)
     achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9 if launch_ms > 0 else 0.0
     peak, peak_src = load_peak()
-    traffic, traffic_src = load_traffic("k_edge_pass_dir")
+    traffic, traffic_src = load_traffic("k_pass_dir")
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic,
-                "kernel": "k_edge_pass_dir (first pass over the directed input)",
+                "kernel": "k_pass_dir (first pass over the directed input)",
                 "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
                 else "fallback 6.8 TB/s",
                 "alg_bytes_per_launch": bytes_per_launch, "launch_ms": launch_ms,
