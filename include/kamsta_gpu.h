@@ -86,6 +86,7 @@ typedef struct kamsta_wedge64 {
 #define KAMSTA_FLAG_DEDUPE_NEVER 0x4u /* never remove parallel edges          */
 #define KAMSTA_FLAG_DEDUPE_ALWAYS 0x8u/* remove parallel edges every round   */
 #define KAMSTA_FLAG_TRACE 0x10u       /* record per-round (m_r, n_r) in stats  */
+#define KAMSTA_FLAG_FILTER 0x20u      /* batch / serving: run filter_boruvka   */
 
 /* AlgorithmConfig (algorithm_configurations.hpp:27-34) plus GPU knobs. */
 typedef struct kamsta_cfg {
@@ -202,6 +203,105 @@ kamsta_status kamsta_mst_boruvka_noalloc(const kamsta_wedge* d_edges, uint64_t m
                                          uint32_t n, kamsta_wedge* d_out, uint64_t* out_count,
                                          uint64_t* total_weight, kamsta_stream stream);
 
+/* ---- batched solve ------------------------------------------------------
+ * No counterpart in the reference, whose benchmark solves one graph per job
+ * (benchmarks/mst.cpp:215-228).  Graphs are solved in waves; each wave is the
+ * disjoint union of consecutive graphs whose estimated device footprint fits
+ * `budget_bytes` (0 = 32 GiB), solved as one graph, and the forest is split
+ * back per graph.  Per graph the result equals kamsta_mst_boruvka (or
+ * kamsta_mst_filter_boruvka with KAMSTA_FLAG_FILTER) on that graph alone,
+ * with the forest sorted by (src, dst).  A graph whose ids are >= n (or, with
+ * KAMSTA_FLAG_VALIDATE, whose entries are not (src,dst)-sorted) gets status
+ * KAMSTA_E_INPUT without affecting the others. */
+typedef struct kamsta_graph_desc {
+  const kamsta_wedge* edges; /* in: m_directed entries, same contract as above */
+  uint64_t m_directed;       /* in                                           */
+  uint32_t n;                /* in: vertex count (< 2^31)                    */
+  kamsta_status status;      /* out: KAMSTA_OK / KAMSTA_E_INPUT              */
+  kamsta_wedge* out;         /* in: capacity >= max(n-1, 1) entries          */
+  uint64_t out_count;        /* out: forest edges written                    */
+  uint64_t total_weight;     /* out: forest weight                           */
+} kamsta_graph_desc;
+
+typedef struct kamsta_batch_stats {
+  uint32_t graphs;           /* graphs in the call                           */
+  uint32_t waves;            /* union solves                                 */
+  uint32_t gpu_launches;     /* kernels launched                             */
+  uint32_t pad_;
+  uint64_t entries;          /* directed input entries over all graphs       */
+  uint64_t vertices;         /* vertices over all graphs                     */
+  uint64_t forest_edges;     /* forest edges over all graphs                 */
+  double device_ms;          /* device time of the whole call (CUDA events)  */
+  double solve_ms;           /* of which in the union solves                 */
+} kamsta_batch_stats;
+
+/* Device buffers: edges / out of every descriptor are device pointers; the
+ * descriptors themselves are host memory. */
+kamsta_status kamsta_mst_batch_dev(kamsta_ctx* ctx, kamsta_graph_desc* graphs,
+                                   uint32_t count, const kamsta_cfg* cfg,
+                                   uint64_t budget_bytes, kamsta_batch_stats* stats,
+                                   kamsta_stream stream);
+/* Host buffers (the library copies in and out; pinned memory is faster). */
+kamsta_status kamsta_mst_batch(kamsta_ctx* ctx, kamsta_graph_desc* graphs, uint32_t count,
+                               const kamsta_cfg* cfg, uint64_t budget_bytes,
+                               kamsta_batch_stats* stats);
+
+/* ---- serving loop -------------------------------------------------------
+ * No counterpart in the reference.  A continuous-batching request loop:
+ * clients submit jobs whose edge arrays already sit in device memory (their
+ * writes complete before the submit); worker threads (each with its own
+ * context and stream) repeatedly take the queued jobs in arrival order while
+ * their estimated device footprint fits the memory budget, and solve them as
+ * one batch wave.  Jobs arriving while a wave runs join the next one; with
+ * two or more workers, waves overlap on the device.  Each job's result is
+ * the batch result of that graph alone (forest sorted by (src, dst)). */
+typedef struct kamsta_server kamsta_server;
+
+typedef struct kamsta_server_cfg {
+  uint64_t budget_bytes;     /* admission budget, device bytes (0 = 64 GiB)   */
+  uint32_t max_batch;        /* jobs per wave at most (0 = 4096)              */
+  uint32_t workers;          /* worker threads / streams (1..8, default 2)   */
+  kamsta_cfg solver;         /* solver options for every job (FILTER flag    */
+                             /* selects filter_boruvka)                      */
+} kamsta_server_cfg;
+
+typedef struct kamsta_request {
+  const kamsta_wedge* d_edges; /* device, m_directed entries (input contract) */
+  uint64_t m_directed;
+  uint32_t n;
+  uint32_t pad_;
+  kamsta_wedge* d_out;         /* device, capacity >= max(n-1, 1)           */
+  uint64_t user_tag;           /* returned in the completion                 */
+} kamsta_request;
+
+typedef struct kamsta_completion {
+  uint64_t ticket;             /* from kamsta_server_submit                  */
+  uint64_t user_tag;
+  kamsta_status status;        /* KAMSTA_OK / KAMSTA_E_INPUT / solver error  */
+  uint32_t batch_size;         /* jobs in the wave that solved this one      */
+  uint64_t out_count;
+  uint64_t total_weight;
+  double submit_us;            /* steady-clock microseconds since create     */
+  double start_us;             /* wave start                                 */
+  double finish_us;            /* wave end (output written)                  */
+} kamsta_completion;
+
+kamsta_status kamsta_server_cfg_default(kamsta_server_cfg* cfg);
+kamsta_status kamsta_server_create(int device, const kamsta_server_cfg* cfg,
+                                   kamsta_server** out);
+/* KAMSTA_E_BUDGET if the job alone exceeds the budget. */
+kamsta_status kamsta_server_submit(kamsta_server* server, const kamsta_request* req,
+                                   uint64_t* ticket);
+/* Up to `cap` completions; waits up to timeout_us for the first one.
+ * KAMSTA_E_NOTREADY (count 0) when none finished in time. */
+kamsta_status kamsta_server_poll(kamsta_server* server, kamsta_completion* out,
+                                 uint32_t cap, uint32_t* count, uint32_t timeout_us);
+kamsta_status kamsta_server_stats(kamsta_server* server, uint64_t* queued,
+                                  uint64_t* in_flight, uint64_t* bytes_in_use,
+                                  uint64_t* waves);
+/* Finishes every queued job, then stops the workers and frees the server. */
+kamsta_status kamsta_server_destroy(kamsta_server* server);
+
 /* ---- device graph generators (seeded; identical to the oracle's CPU
  * generators).  d_out must hold 2*m entries; *m_directed_out receives the
  * number written.  Stand-ins for KaGen's get_gnm / get_rgg2D / get_rhg
@@ -210,6 +310,16 @@ kamsta_status kamsta_gen_gnm_dev(kamsta_ctx* ctx, uint32_t n, uint64_t m,
                                  uint64_t seed, uint32_t max_weight,
                                  kamsta_wedge* d_out, uint64_t* m_directed_out,
                                  kamsta_stream stream);
+/* 2-D random geometric graph on the unit square (radius in [0, 1]; for an
+ * expected degree d away from the border, radius = sqrt(d / (pi n))).  The
+ * edge count is data dependent: with d_out == NULL the call only counts
+ * (*m_directed_out = entries needed); with capacity < that count it returns
+ * KAMSTA_E_INPUT and the count.  Stand-in for get_rgg2D
+ * (benchmarks/mst_benchmarks.hpp:134-142). */
+kamsta_status kamsta_gen_rgg2d_dev(kamsta_ctx* ctx, uint32_t n, double radius,
+                                   uint64_t seed, uint32_t max_weight,
+                                   kamsta_wedge* d_out, uint64_t capacity,
+                                   uint64_t* m_directed_out, kamsta_stream stream);
 
 #ifdef __cplusplus
 } /* extern "C" */

@@ -22,12 +22,13 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _native
-from ._native import (FLAG_DEDUPE_ALWAYS, FLAG_DEDUPE_NEVER, FLAG_SORT_OUTPUT, FLAG_TRACE,
-                      FLAG_VALIDATE, WEDGE, WEDGE64, KamstaError, Stats, check, lib)
+from ._native import (FLAG_DEDUPE_ALWAYS, FLAG_DEDUPE_NEVER, FLAG_FILTER, FLAG_SORT_OUTPUT,
+                      FLAG_TRACE, FLAG_VALIDATE, WEDGE, WEDGE64, BatchStats, GraphDesc,
+                      KamstaError, Stats, check, lib)
 
 __all__ = ["LocalPreprocessing", "Compression", "AlgorithmConfig", "boruvka", "filter_boruvka",
            "boruvka_wedge64", "Context", "WEDGE", "WEDGE64", "KamstaError", "Stats",
-           "as_wedges", "mst_weight", "version"]
+           "as_wedges", "mst_weight", "version", "batch", "GraphDesc", "BatchStats", "Server"]
 
 
 class LocalPreprocessing(enum.IntEnum):
@@ -53,6 +54,7 @@ class AlgorithmConfig:
     dedupe_ratio: int = 0
     trace: bool = False
     seed: int | None = None
+    filter: bool = False        # batch / serving: filter_boruvka instead of boruvka
 
     def to_c(self) -> _native.Cfg:
         c = _native.default_cfg()
@@ -66,6 +68,8 @@ class AlgorithmConfig:
             flags |= FLAG_SORT_OUTPUT
         if self.trace:
             flags |= FLAG_TRACE
+        if self.filter:
+            flags |= FLAG_FILTER
         if self.dedupe == "never":
             flags |= FLAG_DEDUPE_NEVER
         elif self.dedupe == "always":
@@ -150,6 +154,93 @@ def boruvka_wedge64(input_edges: np.ndarray, config: AlgorithmConfig | None = No
     return out[: cnt.value].copy()
 
 
+def batch(graphs, config: AlgorithmConfig | None = None, budget_bytes: int = 0,
+          stats: dict | None = None, context: "Context | None" = None):
+    """kamsta_mst_batch over host arrays: `graphs` is a list of (edges, n).
+
+    Returns one (status, forest) pair per graph; each forest is sorted by
+    (src, dst) and equals boruvka() on that graph alone.
+    """
+    es = [as_wedges(e) for e, _ in graphs]
+    outs = [np.empty(max(int(n), 1), WEDGE) for _, n in graphs]
+    descs = (GraphDesc * max(len(graphs), 1))()
+    for i, ((_, n), e, o) in enumerate(zip(graphs, es, outs)):
+        descs[i].edges = e.ctypes.data if len(e) else None
+        descs[i].m_directed = len(e)
+        descs[i].n = int(n)
+        descs[i].out = o.ctypes.data
+    cfg = (config or AlgorithmConfig()).to_c()
+    st = BatchStats()
+    h = context.handle if context is not None else None
+    check(lib().kamsta_mst_batch(h, descs, len(graphs), C.byref(cfg), int(budget_bytes),
+                                 C.byref(st)))
+    if stats is not None:
+        stats.update(st.as_dict())
+    return [(int(descs[i].status), outs[i][: descs[i].out_count].copy())
+            for i in range(len(graphs))]
+
+
+class Server:
+    """Continuous-batching MST request loop on one device (kamsta_server).
+
+    submit() takes device pointers (edges already written); poll() returns
+    finished jobs as dicts with ticket, tag, status, out_count, total_weight,
+    batch_size and the submit / start / finish times in microseconds.
+    """
+
+    def __init__(self, device: int = 0, budget_bytes: int = 0, max_batch: int = 0,
+                 workers: int = 2, config: AlgorithmConfig | None = None):
+        c = _native.ServerCfg()
+        check(lib().kamsta_server_cfg_default(C.byref(c)))
+        if budget_bytes:
+            c.budget_bytes = int(budget_bytes)
+        if max_batch:
+            c.max_batch = int(max_batch)
+        c.workers = int(workers)
+        c.solver = (config or AlgorithmConfig()).to_c()
+        h = C.c_void_p()
+        check(lib().kamsta_server_create(int(device), C.byref(c), C.byref(h)))
+        self._h = h
+        self._buf = (_native.Completion * 4096)()
+
+    def submit(self, d_edges: int, m_directed: int, n: int, d_out: int, tag: int = 0) -> int:
+        r = _native.Request(C.c_void_p(d_edges or None), int(m_directed), int(n), 0,
+                            C.c_void_p(d_out or None), int(tag))
+        t = C.c_uint64(0)
+        check(lib().kamsta_server_submit(self._h, C.byref(r), C.byref(t)))
+        return int(t.value)
+
+    def poll(self, timeout_us: int = 0) -> list:
+        cnt = C.c_uint32(0)
+        s = lib().kamsta_server_poll(self._h, self._buf, len(self._buf), C.byref(cnt),
+                                     int(timeout_us))
+        if s == _native.E_NOTREADY:
+            return []
+        check(s)
+        return [{"ticket": c.ticket, "tag": c.user_tag, "status": c.status,
+                 "batch_size": c.batch_size, "out_count": c.out_count,
+                 "total_weight": c.total_weight, "submit_us": c.submit_us,
+                 "start_us": c.start_us, "finish_us": c.finish_us}
+                for c in self._buf[: cnt.value]]
+
+    def stats(self) -> dict:
+        q, f, b, w = C.c_uint64(), C.c_uint64(), C.c_uint64(), C.c_uint64()
+        check(lib().kamsta_server_stats(self._h, C.byref(q), C.byref(f), C.byref(b), C.byref(w)))
+        return {"queued": q.value, "in_flight": f.value, "bytes_in_use": b.value,
+                "waves": w.value}
+
+    def close(self):
+        if self._h:
+            check(lib().kamsta_server_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Context:
     """A solver context on one device: scratch pool + stream (kamsta_ctx).
 
@@ -204,10 +295,31 @@ class Context:
         return self._dev(lib().kamsta_mst_filter_boruvka_dev, d_edges, m, n, d_out, config,
                          stream, stats)
 
+    def batch_dev(self, descs, config=None, budget_bytes: int = 0, stream=0,
+                  stats: dict | None = None):
+        """kamsta_mst_batch_dev over a ctypes GraphDesc array (device pointers)."""
+        cfg = (config or AlgorithmConfig()).to_c()
+        st = BatchStats()
+        check(lib().kamsta_mst_batch_dev(self._h, descs, len(descs), C.byref(cfg),
+                                         int(budget_bytes), C.byref(st), C.c_void_p(stream or 0)))
+        if stats is not None:
+            stats.update(st.as_dict())
+        return descs
+
     def gen_gnm_dev(self, n: int, m: int, seed: int, max_weight: int, d_out: int,
                     stream=0) -> int:
         """Device G(n,m) generator; d_out needs 2*m entries.  Returns 2*m."""
         cnt = C.c_uint64(0)
         check(lib().kamsta_gen_gnm_dev(self._h, int(n), int(m), int(seed), int(max_weight),
                                        C.c_void_p(d_out), C.byref(cnt), C.c_void_p(stream or 0)))
+        return int(cnt.value)
+
+    def gen_rgg2d_dev(self, n: int, radius: float, seed: int, max_weight: int, d_out: int = 0,
+                      capacity: int = 0, stream=0) -> int:
+        """Device 2-D random geometric graph.  With d_out == 0 it only counts;
+        returns the number of directed entries."""
+        cnt = C.c_uint64(0)
+        check(lib().kamsta_gen_rgg2d_dev(self._h, int(n), float(radius), int(seed),
+                                         int(max_weight), C.c_void_p(d_out or 0), int(capacity),
+                                         C.byref(cnt), C.c_void_p(stream or 0)))
         return int(cnt.value)

@@ -23,6 +23,7 @@ FLAG_SORT_OUTPUT = 0x2
 FLAG_DEDUPE_NEVER = 0x4
 FLAG_DEDUPE_ALWAYS = 0x8
 FLAG_TRACE = 0x10
+FLAG_FILTER = 0x20
 TRACE_MAX = 128
 PHASES = ["plan", "first_pass", "round_edges", "round_verts", "class_pass", "finalize", "emit",
           "dedupe"]
@@ -65,6 +66,39 @@ class Stats(C.Structure):
         return d
 
 
+class GraphDesc(C.Structure):
+    _fields_ = [("edges", C.c_void_p), ("m_directed", C.c_uint64), ("n", C.c_uint32),
+                ("status", C.c_int32), ("out", C.c_void_p), ("out_count", C.c_uint64),
+                ("total_weight", C.c_uint64)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("graphs", C.c_uint32), ("waves", C.c_uint32), ("gpu_launches", C.c_uint32),
+                ("pad_", C.c_uint32), ("entries", C.c_uint64), ("vertices", C.c_uint64),
+                ("forest_edges", C.c_uint64), ("device_ms", C.c_double),
+                ("solve_ms", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad_"}
+
+
+class ServerCfg(C.Structure):
+    _fields_ = [("budget_bytes", C.c_uint64), ("max_batch", C.c_uint32),
+                ("workers", C.c_uint32), ("solver", Cfg)]
+
+
+class Request(C.Structure):
+    _fields_ = [("d_edges", C.c_void_p), ("m_directed", C.c_uint64), ("n", C.c_uint32),
+                ("pad_", C.c_uint32), ("d_out", C.c_void_p), ("user_tag", C.c_uint64)]
+
+
+class Completion(C.Structure):
+    _fields_ = [("ticket", C.c_uint64), ("user_tag", C.c_uint64), ("status", C.c_int32),
+                ("batch_size", C.c_uint32), ("out_count", C.c_uint64),
+                ("total_weight", C.c_uint64), ("submit_us", C.c_double),
+                ("start_us", C.c_double), ("finish_us", C.c_double)]
+
+
 _lib = None
 
 # Every symbol declared in include/kamsta_gpu.h, with its ctypes signature.
@@ -87,8 +121,20 @@ SIGNATURES = {
                                      C.POINTER(Stats), P]),
     "kamsta_mst_filter_boruvka_dev": (I32, [P, P, U64, U32, C.POINTER(Cfg), P, C.POINTER(U64),
                                             C.POINTER(Stats), P]),
+    "kamsta_server_cfg_default": (I32, [C.POINTER(ServerCfg)]),
+    "kamsta_server_create": (I32, [C.c_int, C.POINTER(ServerCfg), C.POINTER(P)]),
+    "kamsta_server_submit": (I32, [P, C.POINTER(Request), C.POINTER(U64)]),
+    "kamsta_server_poll": (I32, [P, C.POINTER(Completion), U32, C.POINTER(U32), U32]),
+    "kamsta_server_stats": (I32, [P, C.POINTER(U64), C.POINTER(U64), C.POINTER(U64),
+                                  C.POINTER(U64)]),
+    "kamsta_server_destroy": (I32, [P]),
     "kamsta_gen_gnm_dev": (I32, [P, U32, U64, U64, U32, P, C.POINTER(U64), P]),
+    "kamsta_gen_rgg2d_dev": (I32, [P, U32, C.c_double, U64, U32, P, U64, C.POINTER(U64), P]),
     "kamsta_mst_boruvka_noalloc": (I32, [P, U64, U32, P, C.POINTER(U64), C.POINTER(U64), P]),
+    "kamsta_mst_batch_dev": (I32, [P, C.POINTER(GraphDesc), U32, C.POINTER(Cfg), U64,
+                                   C.POINTER(BatchStats), P]),
+    "kamsta_mst_batch": (I32, [P, C.POINTER(GraphDesc), U32, C.POINTER(Cfg), U64,
+                               C.POINTER(BatchStats)]),
 }
 
 

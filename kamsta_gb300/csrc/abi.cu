@@ -5,6 +5,7 @@
 #include <string>
 #include <vector>
 
+#include "batch.cuh"
 #include "solver.cuh"
 
 namespace kamsta {
@@ -124,6 +125,34 @@ kamsta_status solve_dev(Algo algo, kamsta_ctx* ctx, const kamsta_wedge* d_edges,
                    static_cast<cudaStream_t>(stream));
   if (cur != ctx->device) cudaSetDevice(cur);
   *out_count = so.count;
+  return s;
+}
+
+kamsta_status batch_call(kamsta_ctx* ctx, kamsta_graph_desc* graphs, uint32_t count,
+                         const kamsta_cfg* cfg, uint64_t budget, kamsta_batch_stats* stats,
+                         bool host_buffers, kamsta_stream stream) {
+  if (count && !graphs) {
+    set_error("null pointer argument");
+    return KAMSTA_E_INPUT;
+  }
+  kamsta_status s = check_cfg(cfg);
+  if (s != KAMSTA_OK) return s;
+  kamsta_cfg c = cfg_or_default(cfg);
+  if (!ctx) {
+    s = g_default.get(&ctx);
+    if (s != KAMSTA_OK) return s;
+  }
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  int cur = 0;
+  cudaGetDevice(&cur);
+  if (cur != ctx->device) {
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return cuda_status(e, "cudaSetDevice");
+  }
+  const Algo algo = (c.flags & KAMSTA_FLAG_FILTER) ? Algo::kFilterBoruvka : Algo::kBoruvka;
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  s = solve_batch(ctx, algo, graphs, count, c, budget, host_buffers, stats, st);
+  if (cur != ctx->device) cudaSetDevice(cur);
   return s;
 }
 
@@ -291,6 +320,22 @@ kamsta_status kamsta_mst_filter_boruvka_dev(kamsta_ctx* ctx, const kamsta_wedge*
                                             kamsta_stats* stats, kamsta_stream stream) {
   return solve_dev(Algo::kFilterBoruvka, ctx, d_edges, m, n, cfg, d_out, out_count, stats,
                    stream);
+}
+
+kamsta_status kamsta_mst_batch_dev(kamsta_ctx* ctx, kamsta_graph_desc* graphs, uint32_t count,
+                                   const kamsta_cfg* cfg, uint64_t budget_bytes,
+                                   kamsta_batch_stats* stats, kamsta_stream stream) {
+  if (!ctx) {
+    set_error("null context");
+    return KAMSTA_E_INPUT;
+  }
+  return batch_call(ctx, graphs, count, cfg, budget_bytes, stats, false, stream);
+}
+
+kamsta_status kamsta_mst_batch(kamsta_ctx* ctx, kamsta_graph_desc* graphs, uint32_t count,
+                               const kamsta_cfg* cfg, uint64_t budget_bytes,
+                               kamsta_batch_stats* stats) {
+  return batch_call(ctx, graphs, count, cfg, budget_bytes, stats, true, nullptr);
 }
 
 }  // extern "C"

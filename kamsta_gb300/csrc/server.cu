@@ -1,0 +1,279 @@
+// server.cu -- continuous-batching request loop for MST jobs.
+//
+// Clients submit jobs (device edge arrays, device output buffers) at any
+// time; worker threads, each with its own context and stream, repeatedly
+// take whatever is queued, in arrival order, as long as the summed device
+// footprint of the admitted jobs stays under the memory budget, and solve
+// them as one wave (batch.cu: disjoint union -> one solve -> per-graph
+// split).  A job that arrives while a wave is on the GPU joins the next wave
+// of the first worker that frees up, so with two or more workers waves
+// overlap on the device.  Completions carry submit / start / finish times
+// (steady clock) for latency accounting.
+//
+// The reference has no serving loop (its benchmark runs one graph per MPI
+// job, benchmarks/mst.cpp:215-228); per job the result equals the batch
+// entry point on that graph alone.
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "batch.cuh"
+#include "solver.cuh"
+
+struct kamsta_server {
+  struct Job {
+    kamsta_request req;
+    uint64_t ticket;
+    uint64_t bytes;
+    double submit_us;
+  };
+  int device = 0;
+  kamsta_server_cfg cfg{};
+  kamsta_cfg scfg{};
+  std::chrono::steady_clock::time_point t0;
+  std::mutex mu;
+  std::condition_variable cv_work;  // jobs queued / stop
+  std::condition_variable cv_done;  // completions / memory freed
+  std::deque<Job> queue;
+  std::deque<kamsta_completion> done;
+  uint64_t next_ticket = 1;
+  uint64_t bytes_in_use = 0;
+  uint64_t in_flight = 0;
+  uint64_t waves = 0;
+  bool stop = false;
+  std::vector<std::thread> workers;
+  std::vector<kamsta_ctx*> ctxs;
+
+  double now_us() const {
+    return std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - t0)
+        .count();
+  }
+  void worker(int w);
+};
+
+namespace kamsta {
+namespace {
+constexpr uint64_t kServerDefaultBudget = 64ull << 30;
+constexpr uint32_t kServerDefaultMaxBatch = 4096;
+}  // namespace
+}  // namespace kamsta
+
+void kamsta_server::worker(int w) {
+  using namespace kamsta;
+  cudaSetDevice(device);
+  kamsta_ctx* ctx = ctxs[w];
+  const Algo algo = (scfg.flags & KAMSTA_FLAG_FILTER) ? Algo::kFilterBoruvka : Algo::kBoruvka;
+  std::vector<Job> batch;
+  std::vector<kamsta_graph_desc> descs;
+  for (;;) {
+    batch.clear();
+    uint64_t bytes = 0;
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      cv_work.wait(lk, [&] {
+        if (stop && queue.empty()) return true;
+        // admit the queue head once its footprint fits the free budget
+        return !queue.empty() && bytes_in_use + queue.front().bytes <= cfg.budget_bytes;
+      });
+      if (queue.empty()) return;  // stop requested and drained
+      // take jobs in arrival order while they fit
+      while (!queue.empty() && batch.size() < cfg.max_batch &&
+             bytes_in_use + bytes + queue.front().bytes <= cfg.budget_bytes) {
+        bytes += queue.front().bytes;
+        batch.push_back(queue.front());
+        queue.pop_front();
+      }
+      bytes_in_use += bytes;
+      in_flight += batch.size();
+      ++waves;
+    }
+    if (!queue.empty()) cv_work.notify_one();  // more work for another worker
+    const double start = now_us();
+    descs.resize(batch.size());
+    for (size_t i = 0; i < batch.size(); ++i) {
+      descs[i] = kamsta_graph_desc{};
+      descs[i].edges = batch[i].req.d_edges;
+      descs[i].m_directed = batch[i].req.m_directed;
+      descs[i].n = batch[i].req.n;
+      descs[i].out = batch[i].req.d_out;
+    }
+    BatchWaveStats ws;
+    kamsta_status s;
+    {
+      std::lock_guard<std::mutex> clk(ctx->mu);
+      s = solve_wave(ctx, algo, descs.data(), static_cast<uint32_t>(descs.size()), scfg, false,
+                     ctx->stream, &ws);
+    }
+    const double finish = now_us();
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      for (size_t i = 0; i < batch.size(); ++i) {
+        kamsta_completion c{};
+        c.ticket = batch[i].ticket;
+        c.user_tag = batch[i].req.user_tag;
+        c.status = s != KAMSTA_OK ? s : descs[i].status;
+        c.out_count = s == KAMSTA_OK ? descs[i].out_count : 0;
+        c.total_weight = s == KAMSTA_OK ? descs[i].total_weight : 0;
+        c.batch_size = static_cast<uint32_t>(batch.size());
+        c.submit_us = batch[i].submit_us;
+        c.start_us = start;
+        c.finish_us = finish;
+        done.push_back(c);
+      }
+      bytes_in_use -= bytes;
+      in_flight -= batch.size();
+    }
+    cv_done.notify_all();
+    cv_work.notify_all();
+  }
+}
+
+using namespace kamsta;
+
+extern "C" {
+
+kamsta_status kamsta_server_cfg_default(kamsta_server_cfg* cfg) {
+  if (!cfg) {
+    set_error("null pointer argument");
+    return KAMSTA_E_INPUT;
+  }
+  std::memset(cfg, 0, sizeof(*cfg));
+  cfg->budget_bytes = kServerDefaultBudget;
+  cfg->max_batch = kServerDefaultMaxBatch;
+  cfg->workers = 2;
+  kamsta_cfg_default(&cfg->solver);
+  return KAMSTA_OK;
+}
+
+kamsta_status kamsta_server_create(int device, const kamsta_server_cfg* cfg,
+                                   kamsta_server** out) {
+  if (!out) {
+    set_error("null pointer argument");
+    return KAMSTA_E_INPUT;
+  }
+  *out = nullptr;
+  kamsta_server_cfg c;
+  kamsta_server_cfg_default(&c);
+  if (cfg) c = *cfg;
+  if (c.budget_bytes == 0) c.budget_bytes = kServerDefaultBudget;
+  if (c.max_batch == 0) c.max_batch = kServerDefaultMaxBatch;
+  if (c.workers == 0) c.workers = 1;
+  if (c.workers > 8) {
+    set_error("server: at most 8 workers");
+    return KAMSTA_E_INPUT;
+  }
+  if (c.solver.compression != KAMSTA_NO_COMPRESSION) {
+    set_error("compression: only NO_COMPRESSION is implemented");
+    return KAMSTA_E_UNSUPPORTED;
+  }
+  auto* s = new kamsta_server();
+  s->device = device;
+  s->cfg = c;
+  s->scfg = c.solver;
+  s->scfg.flags &= ~KAMSTA_FLAG_SORT_OUTPUT;
+  s->t0 = std::chrono::steady_clock::now();
+  for (uint32_t w = 0; w < c.workers; ++w) {
+    kamsta_ctx* ctx = nullptr;
+    const kamsta_status st = kamsta_ctx_create(device, &ctx);
+    if (st != KAMSTA_OK) {
+      for (auto* p : s->ctxs) kamsta_ctx_destroy(p);
+      delete s;
+      return st;
+    }
+    // cached pool memory above the worker's share of the budget goes back
+    // to the device at the wave's synchronisation points
+    uint64_t keep = c.budget_bytes / c.workers;
+    cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    s->ctxs.push_back(ctx);
+  }
+  for (uint32_t w = 0; w < c.workers; ++w)
+    s->workers.emplace_back([s, w] { s->worker(static_cast<int>(w)); });
+  *out = s;
+  return KAMSTA_OK;
+}
+
+kamsta_status kamsta_server_submit(kamsta_server* s, const kamsta_request* req,
+                                   uint64_t* ticket) {
+  if (!s || !req || (req->m_directed && !req->d_edges) || (req->n > 1 && !req->d_out)) {
+    set_error("null pointer argument");
+    return KAMSTA_E_INPUT;
+  }
+  if (req->n >= kBatchMaxVertices) {
+    set_error("server: n too large");
+    return KAMSTA_E_INPUT;
+  }
+  const uint64_t bytes = batch_graph_bytes(req->m_directed, req->n);
+  if (bytes > s->cfg.budget_bytes) {
+    set_error("server: request needs more device memory than the whole budget");
+    return KAMSTA_E_BUDGET;
+  }
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->stop) {
+      set_error("server: shutting down");
+      return KAMSTA_E_INPUT;
+    }
+    kamsta_server::Job j{*req, s->next_ticket++, bytes, s->now_us()};
+    if (ticket) *ticket = j.ticket;
+    s->queue.push_back(j);
+  }
+  s->cv_work.notify_one();
+  return KAMSTA_OK;
+}
+
+kamsta_status kamsta_server_poll(kamsta_server* s, kamsta_completion* out, uint32_t cap,
+                                 uint32_t* count, uint32_t timeout_us) {
+  if (!s || !count || (cap && !out)) {
+    set_error("null pointer argument");
+    return KAMSTA_E_INPUT;
+  }
+  *count = 0;
+  std::unique_lock<std::mutex> lk(s->mu);
+  if (s->done.empty() && timeout_us)
+    s->cv_done.wait_for(lk, std::chrono::microseconds(timeout_us),
+                        [&] { return !s->done.empty(); });
+  uint32_t k = 0;
+  while (k < cap && !s->done.empty()) {
+    out[k++] = s->done.front();
+    s->done.pop_front();
+  }
+  *count = k;
+  if (k == 0) {
+    set_error("server: nothing finished yet");
+    return KAMSTA_E_NOTREADY;
+  }
+  return KAMSTA_OK;
+}
+
+kamsta_status kamsta_server_stats(kamsta_server* s, uint64_t* queued, uint64_t* in_flight,
+                                  uint64_t* bytes_in_use, uint64_t* waves) {
+  if (!s) {
+    set_error("null pointer argument");
+    return KAMSTA_E_INPUT;
+  }
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (queued) *queued = s->queue.size();
+  if (in_flight) *in_flight = s->in_flight;
+  if (bytes_in_use) *bytes_in_use = s->bytes_in_use;
+  if (waves) *waves = s->waves;
+  return KAMSTA_OK;
+}
+
+kamsta_status kamsta_server_destroy(kamsta_server* s) {
+  if (!s) return KAMSTA_OK;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+  }
+  s->cv_work.notify_all();
+  for (auto& t : s->workers) t.join();
+  for (auto* c : s->ctxs) kamsta_ctx_destroy(c);
+  delete s;
+  return KAMSTA_OK;
+}
+
+}  // extern "C"

@@ -9,6 +9,7 @@
 //   candidate order; w = 1 + hi64(mix64(wseed ^ (min << 32 | max)) * max_weight),
 //   wseed = mix64(seed ^ 0x6a09e667f3bcc909); both directions, (src,dst) sorted.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "radix_sort.cuh"
@@ -164,16 +165,40 @@ __global__ void k_gnm_unpack(const uint64_t* dkeys, uint64_t md, uint32_t b, uin
   }
 }
 
+// Generator scratch: stream-ordered allocations from the context's pool when
+// a generator runs with a context (set by PoolScope), plain cudaMalloc
+// otherwise.
+struct GenPool {
+  cudaMemPool_t pool = nullptr;
+  cudaStream_t st = nullptr;
+};
+thread_local GenPool g_gen_pool;
+
+struct PoolScope {
+  GenPool saved;
+  PoolScope(kamsta_ctx* ctx, cudaStream_t st) : saved(g_gen_pool) {
+    g_gen_pool = ctx ? GenPool{ctx->pool, st} : GenPool{};
+  }
+  ~PoolScope() { g_gen_pool = saved; }
+};
+
 struct Tmp {
   void* p = nullptr;
+  GenPool gp = g_gen_pool;
   ~Tmp() { reset(); }
   void reset() {
-    if (p) cudaFree(p);
+    if (p) {
+      if (gp.pool) cudaFreeAsync(p, gp.st);
+      else cudaFree(p);
+    }
     p = nullptr;
   }
   template <typename T>
   cudaError_t alloc(T** out, uint64_t count) {
-    cudaError_t e = cudaMalloc(&p, std::max<uint64_t>(count, 1) * sizeof(T));
+    reset();
+    const size_t bytes = std::max<uint64_t>(count, 1) * sizeof(T);
+    cudaError_t e = gp.pool ? cudaMallocFromPoolAsync(&p, bytes, gp.pool, gp.st)
+                            : cudaMalloc(&p, bytes);
     *out = static_cast<T*>(p);
     return e;
   }
@@ -189,6 +214,7 @@ struct Tmp {
 kamsta_status gen_gnm(kamsta_ctx* ctx, uint32_t n, uint64_t m, uint64_t seed, uint32_t max_weight,
                       kamsta_wedge* d_out, uint64_t* m_out, cudaStream_t st) {
   *m_out = 0;
+  PoolScope scope(ctx, st);
   const uint64_t pairs = static_cast<uint64_t>(n) * (n - 1ull) / 2;
   if (m == 0) return KAMSTA_OK;
   if (n < 2 || m > pairs || max_weight == 0) {
@@ -217,6 +243,7 @@ kamsta_status gen_gnm(kamsta_ctx* ctx, uint32_t n, uint64_t m, uint64_t seed, ui
   GEN_TRY(tsmall.alloc(&d_small, 8));
   uint32_t* d_ticket = reinterpret_cast<uint32_t*>(d_small + 4);
   uint32_t* d_err = reinterpret_cast<uint32_t*>(d_small + 5);
+  GEN_TRY(cudaMemsetAsync(d_small, 0, 8 * sizeof(unsigned long long), st));
   for (int attempt = 0; attempt < 64; ++attempt) {
     if (K >= (1ull << 32) - kRsTile) {
       set_error("gen_gnm: candidate stream too long (graph too dense)");
@@ -305,7 +332,216 @@ kamsta_status gen_gnm(kamsta_ctx* ctx, uint32_t n, uint64_t m, uint64_t seed, ui
   return KAMSTA_E_NOCONVERGE;
 }
 
+// ---------------------------------------------------------------------------
+// 2-D random geometric graph.  Stand-in for KaGen's get_rgg2D
+// (benchmarks/mst_benchmarks.hpp:134-142); the definition is shared with the
+// oracle's CPU generator (oracle/oracle.cpp):
+//   base = mix64(seed ^ 0x5247473244); point i: x = mix64(base + 2i) >> 33,
+//   y = mix64(base + 2i + 1) >> 33 (31-bit integers); R = floor(radius * 2^31);
+//   u ~ v iff u != v and dx^2 + dy^2 <= R^2 (exact 64-bit arithmetic);
+//   G = min(floor(2^31 / R), isqrt(n), 65536) >= 1 cells per side;
+//   vertex ids = ranks of the points sorted by (cell, i); GNM weights.
+// Device steps: cell keys -> radix sort -> per-cell first rank -> per-vertex
+// degree over the 3x3 cell block -> scan -> write.  Each vertex's neighbours
+// come out in id order because cells are visited in row-major order and ids
+// follow the cells.
+
+__device__ __forceinline__ uint32_t rgg_coord(uint64_t base, uint64_t k) {
+  return static_cast<uint32_t>(mix64(base + k) >> 33);
+}
+
+__global__ void k_rgg_keys(uint32_t n, uint64_t base, uint64_t G, uint64_t* keys) {
+  for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    const uint64_t x = rgg_coord(base, 2 * i), y = rgg_coord(base, 2 * i + 1);
+    const uint64_t cell = ((y * G) >> 31) * G + ((x * G) >> 31);
+    keys[i] = (cell << 32) | i;
+  }
+}
+
+__global__ void k_rgg_place(const uint64_t* keys, uint32_t n, uint64_t base, uint32_t* px,
+                            uint32_t* py) {
+  for (uint64_t j = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; j < n;
+       j += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    const uint64_t i = keys[j] & 0xffffffffull;
+    px[j] = rgg_coord(base, 2 * i);
+    py[j] = rgg_coord(base, 2 * i + 1);
+  }
+}
+
+// cbeg[c] = first rank in cell c (c in [0, cells])
+__global__ void k_rgg_cells(const uint64_t* keys, uint32_t n, uint64_t cells, uint32_t* cbeg) {
+  for (uint64_t c = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; c <= cells;
+       c += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    const uint64_t x = c << 32;
+    uint64_t lo = 0, hi = n;
+    while (lo < hi) {
+      const uint64_t mid = (lo + hi) >> 1;
+      if (keys[mid] < x) lo = mid + 1; else hi = mid;
+    }
+    cbeg[c] = static_cast<uint32_t>(lo);
+  }
+}
+
+template <bool WRITE>
+__global__ void k_rgg_edges(uint32_t n, const uint32_t* __restrict__ px,
+                            const uint32_t* __restrict__ py, const uint32_t* __restrict__ cbeg,
+                            uint64_t G, uint64_t R2, uint32_t* __restrict__ deg,
+                            const uint32_t* __restrict__ off, uint64_t wseed, uint32_t max_weight,
+                            uint32_t* __restrict__ out) {
+  for (uint64_t j = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; j < n;
+       j += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    const uint64_t xj = px[j], yj = py[j];
+    const uint64_t cx = (xj * G) >> 31, cy = (yj * G) >> 31;
+    uint64_t o = WRITE ? off[j] : 0;
+    uint32_t d = 0;
+    const uint64_t y0 = cy ? cy - 1 : 0, y1 = min(cy + 1, G - 1);
+    const uint64_t x0 = cx ? cx - 1 : 0, x1 = min(cx + 1, G - 1);
+    for (uint64_t ny = y0; ny <= y1; ++ny) {
+      // cells (ny, x0..x1) are contiguous: one rank range
+      const uint32_t kb = cbeg[ny * G + x0], ke = cbeg[ny * G + x1 + 1];
+      for (uint32_t k = kb; k < ke; ++k) {
+        if (k == j) continue;
+        const uint64_t xk = px[k], yk = py[k];
+        const uint64_t dx = xj > xk ? xj - xk : xk - xj;
+        const uint64_t dy = yj > yk ? yj - yk : yk - yj;
+        if (dx * dx + dy * dy <= R2) {
+          if (WRITE) {
+            const uint64_t lo = j < k ? j : k, hi = j < k ? k : j;
+            const uint64_t canon = (lo << 32) | hi;
+            out[3 * o] = static_cast<uint32_t>(j);
+            out[3 * o + 1] = k;
+            out[3 * o + 2] = 1u + static_cast<uint32_t>(__umul64hi(mix64(wseed ^ canon),
+                                                                   max_weight));
+            ++o;
+          }
+          ++d;
+        }
+      }
+    }
+    if (!WRITE) deg[j] = d;
+  }
+}
+
+__global__ void k_sum_u32(const uint32_t* v, uint64_t n, unsigned long long* out) {
+  uint64_t s = 0;
+  for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+    s += v[i];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, static_cast<unsigned long long>(s));
+}
+
+static uint64_t isqrt64(uint64_t n) {
+  uint64_t s = static_cast<uint64_t>(std::sqrt(static_cast<double>(n)));
+  while (s * s > n) --s;
+  while ((s + 1) * (s + 1) <= n) ++s;
+  return s;
+}
+
+kamsta_status gen_rgg2d(kamsta_ctx* ctx, uint32_t n, double radius, uint64_t seed,
+                        uint32_t max_weight, kamsta_wedge* d_out, uint64_t capacity,
+                        uint64_t* m_out, cudaStream_t st) {
+  *m_out = 0;
+  if (max_weight == 0) {
+    set_error("gen_rgg2d: max_weight must be >= 1");
+    return KAMSTA_E_INPUT;
+  }
+  if (n == 0) return KAMSTA_OK;
+  PoolScope scope(ctx, st);
+  uint64_t R = 0;
+  if (!(radius > 0)) R = 0;
+  else if (radius >= 1) R = 1ull << 31;
+  else R = static_cast<uint64_t>(radius * 2147483648.0);
+  const uint64_t cap = std::min<uint64_t>(std::max<uint64_t>(isqrt64(n), 1), 65536);
+  const uint64_t G = R == 0 ? cap : std::max<uint64_t>(1, std::min<uint64_t>((1ull << 31) / R, cap));
+  const uint64_t cells = G * G;
+  const uint64_t base = mix64(seed ^ 0x5247473244ull);
+  const uint64_t wseed = mix64(seed ^ 0x6a09e667f3bcc909ull);
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int grid = sms * 8;
+  Tmp tsmall, tk, tk2, tx, ty, tcb, tdeg, toff, tcnt, tst;
+  unsigned long long* d_small = nullptr;
+  uint64_t *keys, *keys2, *status;
+  uint32_t *px, *py, *cbeg, *deg, *off, *counts;
+  GEN_TRY(tsmall.alloc(&d_small, 8));
+  uint32_t* d_ticket = reinterpret_cast<uint32_t*>(d_small + 4);
+  uint32_t* d_err = reinterpret_cast<uint32_t*>(d_small + 5);
+  GEN_TRY(cudaMemsetAsync(d_small, 0, 8 * sizeof(unsigned long long), st));
+  GEN_TRY(tk.alloc(&keys, n));
+  GEN_TRY(tk2.alloc(&keys2, n));
+  const RadixScratch rs = radix_scratch_bytes(n);
+  GEN_TRY(tcnt.alloc(&counts, std::max<uint64_t>(rs.counts, n)));
+  GEN_TRY(tst.alloc(&status, std::max<uint64_t>(rs.status, cdiv(n, kScanTile) + 1)));
+  k_rgg_keys<<<grid, 256, 0, st>>>(n, base, G, keys);
+  int alt = 0;
+  uint32_t cbits = 1;
+  while (cbits < 32 && (1ull << cbits) < cells) ++cbits;
+  GEN_TRY(radix_sort_keys(st, keys, keys2, n, 32 + static_cast<int>(cbits), counts, status,
+                          d_ticket, d_err, &alt, sms));
+  if (alt) std::swap(keys, keys2);
+  GEN_TRY(tx.alloc(&px, n));
+  GEN_TRY(ty.alloc(&py, n));
+  GEN_TRY(tcb.alloc(&cbeg, cells + 1));
+  k_rgg_place<<<grid, 256, 0, st>>>(keys, n, base, px, py);
+  k_rgg_cells<<<grid, 256, 0, st>>>(keys, n, cells, cbeg);
+  tk.reset();
+  tk2.reset();
+  GEN_TRY(tdeg.alloc(&deg, n));
+  GEN_TRY(toff.alloc(&off, n));
+  k_rgg_edges<false><<<grid, 256, 0, st>>>(n, px, py, cbeg, G, R * R, deg, nullptr, wseed,
+                                           max_weight, nullptr);
+  const uint32_t nst = cdiv(n, kScanTile);
+  GEN_TRY(cudaMemsetAsync(status, 0, sizeof(uint64_t) * nst, st));
+  GEN_TRY(cudaMemsetAsync(d_ticket, 0, sizeof(uint32_t), st));
+  k_scan_u32<<<std::min<uint32_t>(nst, sms * 4), kRsBlock, 0, st>>>(deg, off, n, status,
+                                                                     d_ticket, nst, d_err);
+  // exact 64-bit degree sum (the u32 prefix is only valid below 2^32)
+  k_sum_u32<<<grid, 256, 0, st>>>(deg, n, d_small);
+  unsigned long long h_total = 0;
+  uint32_t h_err = 0;
+  GEN_TRY(cudaMemcpyAsync(&h_total, d_small, sizeof(h_total), cudaMemcpyDeviceToHost, st));
+  GEN_TRY(cudaMemcpyAsync(&h_err, d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  GEN_TRY(cudaStreamSynchronize(st));
+  if (h_err) {
+    set_error("gen_rgg2d: device scan wait cap reached");
+    return KAMSTA_E_NOCONVERGE;
+  }
+  const uint64_t total = h_total;
+  if (total >= (1ull << 32)) {
+    set_error("gen_rgg2d: more than 2^32 directed entries");
+    return KAMSTA_E_INPUT;
+  }
+  *m_out = total;
+  if (!d_out || total > capacity) {
+    if (d_out) {
+      set_error("gen_rgg2d: output capacity too small (required count in m_directed_out)");
+      return KAMSTA_E_INPUT;
+    }
+    return KAMSTA_OK;
+  }
+  k_rgg_edges<true><<<grid, 256, 0, st>>>(n, px, py, cbeg, G, R * R, deg, off, wseed,
+                                          max_weight, reinterpret_cast<uint32_t*>(d_out));
+  GEN_TRY(cudaGetLastError());
+  GEN_TRY(cudaStreamSynchronize(st));
+  return KAMSTA_OK;
+}
+
 }  // namespace kamsta
+
+extern "C" kamsta_status kamsta_gen_rgg2d_dev(kamsta_ctx* ctx, uint32_t n, double radius,
+                                              uint64_t seed, uint32_t max_weight,
+                                              kamsta_wedge* d_out, uint64_t capacity,
+                                              uint64_t* m_directed_out, kamsta_stream stream) {
+  if (!m_directed_out) {
+    kamsta::set_error("null pointer argument");
+    return KAMSTA_E_INPUT;
+  }
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : (ctx ? ctx->stream : nullptr);
+  return kamsta::gen_rgg2d(ctx, n, radius, seed, max_weight, d_out, capacity, m_directed_out, st);
+}
 
 extern "C" kamsta_status kamsta_gen_gnm_dev(kamsta_ctx* ctx, uint32_t n, uint64_t m, uint64_t seed,
                                             uint32_t max_weight, kamsta_wedge* d_out,

@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <numeric>
@@ -464,5 +465,108 @@ extern "C" int oracle_gen_gnm(uint32_t n, uint64_t m, uint64_t seed,
     out[lo_cur[v]++] = kamsta_wedge{v, u, w};
   }
   *m_directed_out = 2 * sel.size();
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Seeded 2-D random geometric graph (stand-in for KaGen's get_rgg2D,
+// benchmarks/mst_benchmarks.hpp:134-142, which the reference tree does not
+// vendor).  The definition, shared with the device generator
+// kamsta_gen_rgg2d_dev:
+//   base = mix64(seed ^ 0x5247473244ull); point i (i < n) has 31-bit integer
+//   coordinates x = mix64(base + 2i) >> 33, y = mix64(base + 2i + 1) >> 33;
+//   R = floor(radius * 2^31) (radius clamped to [0, 1]); u ~ v iff u != v and
+//   dx^2 + dy^2 <= R^2 (exact in 64-bit integers);
+//   G = cells per side = min(floor(2^31 / R), isqrt(n), 65536), at least 1
+//   (cells at least R wide); cell = (y*G >> 31) * G + (x*G >> 31);
+//   vertex ids = ranks of the points sorted by (cell, i);
+//   weights as in the G(n,m) generator, both directions, (src,dst) sorted.
+namespace gen {
+
+struct RggParams {
+  uint64_t R;
+  uint64_t G;
+};
+
+inline uint64_t isqrt64(uint64_t n) {
+  uint64_t s = static_cast<uint64_t>(std::sqrt(static_cast<double>(n)));
+  while (s * s > n) --s;
+  while ((s + 1) * (s + 1) <= n) ++s;
+  return s;
+}
+
+inline RggParams rgg_params(uint32_t n, double radius) {
+  RggParams p;
+  if (!(radius > 0)) p.R = 0;
+  else if (radius >= 1) p.R = 1ull << 31;
+  else p.R = static_cast<uint64_t>(radius * 2147483648.0);
+  uint64_t cap = std::min<uint64_t>(std::max<uint64_t>(isqrt64(n), 1), 65536);
+  p.G = p.R == 0 ? cap : std::max<uint64_t>(1, std::min<uint64_t>((1ull << 31) / p.R, cap));
+  return p;
+}
+
+}  // namespace gen
+
+extern "C" int oracle_gen_rgg2d(uint32_t n, double radius, uint64_t seed, uint32_t max_weight,
+                                kamsta_wedge* out, uint64_t capacity,
+                                uint64_t* m_directed_out) {
+  using namespace gen;
+  *m_directed_out = 0;
+  if (max_weight == 0) return 1;
+  if (n == 0) return 0;
+  const RggParams P = rgg_params(n, radius);
+  const uint64_t base = mix64(seed ^ 0x5247473244ull);
+  const uint64_t wseed = mix64(seed ^ 0x6a09e667f3bcc909ull);
+  const uint64_t G = P.G, R2 = P.R * P.R;
+  std::vector<uint64_t> key(n);
+#pragma omp parallel for schedule(static)
+  for (uint64_t i = 0; i < n; ++i) {
+    const uint64_t x = mix64(base + 2 * i) >> 33, y = mix64(base + 2 * i + 1) >> 33;
+    const uint64_t cell = ((y * G) >> 31) * G + ((x * G) >> 31);
+    key[i] = (cell << 32) | i;
+  }
+  std::sort(key.begin(), key.end());
+  std::vector<uint64_t> px(n), py(n);
+  const uint64_t cells = G * G;
+  std::vector<uint64_t> cbeg(cells + 1, 0);
+  for (uint64_t j = 0; j < n; ++j) {
+    const uint64_t i = key[j] & 0xffffffffull;
+    px[j] = mix64(base + 2 * i) >> 33;
+    py[j] = mix64(base + 2 * i + 1) >> 33;
+    cbeg[(key[j] >> 32) + 1]++;
+  }
+  for (uint64_t c = 0; c < cells; ++c) cbeg[c + 1] += cbeg[c];
+  auto visit = [&](uint64_t j, auto&& emit) {
+    const uint64_t cx = (px[j] * G) >> 31, cy = (py[j] * G) >> 31;
+    for (uint64_t ny = cy ? cy - 1 : 0; ny <= std::min(cy + 1, G - 1); ++ny)
+      for (uint64_t nx = cx ? cx - 1 : 0; nx <= std::min(cx + 1, G - 1); ++nx) {
+        const uint64_t c = ny * G + nx;
+        for (uint64_t k = cbeg[c]; k < cbeg[c + 1]; ++k) {
+          if (k == j) continue;
+          const uint64_t dx = px[j] > px[k] ? px[j] - px[k] : px[k] - px[j];
+          const uint64_t dy = py[j] > py[k] ? py[j] - py[k] : py[k] - py[j];
+          if (dx * dx + dy * dy <= R2) emit(k);
+        }
+      }
+  };
+  std::vector<uint64_t> off(static_cast<uint64_t>(n) + 1, 0);
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (uint64_t j = 0; j < n; ++j) {
+    uint64_t d = 0;
+    visit(j, [&](uint64_t) { ++d; });
+    off[j + 1] = d;
+  }
+  for (uint64_t j = 0; j < n; ++j) off[j + 1] += off[j];
+  *m_directed_out = off[n];
+  if (off[n] > capacity) return 2;
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (uint64_t j = 0; j < n; ++j) {
+    uint64_t o = off[j];
+    visit(j, [&](uint64_t k) {
+      const uint64_t canon = (std::min(j, k) << 32) | std::max(j, k);
+      const uint32_t w = 1 + static_cast<uint32_t>(hi64(mix64(wseed ^ canon), max_weight));
+      out[o++] = kamsta_wedge{static_cast<uint32_t>(j), static_cast<uint32_t>(k), w};
+    });
+  }
   return 0;
 }

@@ -18,6 +18,8 @@
  *                              "reference CPU" baseline (kind "port").
  *   oracle_gen_gnm          -- seeded G(n,m) generator; bit-identical to the
  *                              device generator kamsta_gen_gnm_dev.
+ *   oracle_gen_rgg2d        -- seeded 2-D random geometric graph; bit-identical
+ *                              to kamsta_gen_rgg2d_dev.
  *
  * Parity status: the reference ships no golden vectors (its only test,
  * tests/test_sets.sh, checks the MSF weight against this same Kruskal).
@@ -52,6 +54,14 @@ int oracle_boruvka_filter(const kamsta_wedge* edges, uint64_t m_directed,
  * n(n-1)/2. */
 int oracle_gen_gnm(uint32_t n, uint64_t m, uint64_t seed, uint32_t max_weight,
                    kamsta_wedge* out, uint64_t* m_directed_out);
+
+/* Seeded 2-D random geometric graph (unit square, integer coordinates,
+ * radius in [0, 1]); definition in oracle.cpp, bit-identical to the device
+ * generator kamsta_gen_rgg2d_dev.  *m_directed_out receives the number of
+ * directed entries; returns 0, 2 if it exceeds `capacity` (nothing written),
+ * 1 on bad arguments. */
+int oracle_gen_rgg2d(uint32_t n, double radius, uint64_t seed, uint32_t max_weight,
+                     kamsta_wedge* out, uint64_t capacity, uint64_t* m_directed_out);
 
 /* Number of OpenMP threads the oracle uses when threads == 0. */
 int oracle_max_threads(void);

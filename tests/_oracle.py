@@ -26,6 +26,7 @@ def lib():
         L.oracle_boruvka_filter.argtypes = [P, U64, U32, C.c_int, P, C.POINTER(U64),
                                             C.POINTER(U64), C.POINTER(U32)]
         L.oracle_gen_gnm.argtypes = [U32, U64, U64, U32, P, C.POINTER(U64)]
+        L.oracle_gen_rgg2d.argtypes = [U32, C.c_double, U64, U32, P, U64, C.POINTER(U64)]
         L.oracle_max_threads.restype = C.c_int
         _lib = L
     return _lib
@@ -38,6 +39,24 @@ def gen_gnm(n: int, m: int, seed: int, max_weight: int = 254) -> np.ndarray:
     if rc != 0:
         raise ValueError("oracle_gen_gnm: m exceeds n(n-1)/2")
     return out[: cnt.value]
+
+
+def gen_rgg2d(n: int, radius: float, seed: int, max_weight: int = 254) -> np.ndarray:
+    cnt = C.c_uint64()
+    rc = lib().oracle_gen_rgg2d(n, radius, seed, max_weight, None, 0, C.byref(cnt))
+    if rc not in (0, 2):
+        raise ValueError("oracle_gen_rgg2d: bad arguments")
+    out = np.empty(max(cnt.value, 1), WEDGE)
+    rc = lib().oracle_gen_rgg2d(n, radius, seed, max_weight, out.ctypes.data, cnt.value,
+                                C.byref(cnt))
+    assert rc == 0
+    return out[: cnt.value]
+
+
+def rgg_radius(n: int, avg_degree: float) -> float:
+    """Radius giving an expected degree `avg_degree` away from the border."""
+    import math
+    return math.sqrt(avg_degree / (math.pi * n))
 
 
 def kruskal(edges: np.ndarray, n: int):

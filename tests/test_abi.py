@@ -39,9 +39,11 @@ def test_struct_layouts_match_header(kamsta, tmp_path):
     from kamsta_gb300 import _native
     prog = tmp_path / "sz.c"
     prog.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "kamsta_gpu.h"\n'
-                    'int main(){printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(kamsta_cfg),'
+                    'int main(){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(kamsta_cfg),'
                     'sizeof(kamsta_stats), sizeof(kamsta_wedge), sizeof(kamsta_wedge64),'
-                    'offsetof(kamsta_stats, trace_m), offsetof(kamsta_cfg, seed));}\n')
+                    'offsetof(kamsta_stats, trace_m), offsetof(kamsta_cfg, seed),'
+                    'sizeof(kamsta_graph_desc), offsetof(kamsta_graph_desc, out),'
+                    'sizeof(kamsta_batch_stats));}\n')
     exe = tmp_path / "sz"
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(prog), "-o", str(exe)],
                    check=True)
@@ -49,7 +51,8 @@ def test_struct_layouts_match_header(kamsta, tmp_path):
                                           check=True).stdout.split()]
     assert got == [C.sizeof(_native.Cfg), C.sizeof(_native.Stats), _native.WEDGE.itemsize,
                    _native.WEDGE64.itemsize, _native.Stats.trace_m.offset,
-                   _native.Cfg.seed.offset]
+                   _native.Cfg.seed.offset, C.sizeof(_native.GraphDesc),
+                   _native.GraphDesc.out.offset, C.sizeof(_native.BatchStats)]
 
 
 def test_cfg_default_mirrors_reference_algorithm_config(kamsta):

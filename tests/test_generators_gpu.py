@@ -1,0 +1,56 @@
+"""Device graph generators against the oracle's CPU generators, and MSF
+parity on their graphs.
+
+The device generators must be bit-identical to the oracle's (same seeded
+definition), so that GPU and CPU runs of a workload see the same input.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _dev_rgg(kamsta, ctx, n, radius, seed, wmax=254):
+    import torch
+    md = ctx.gen_rgg2d_dev(n, radius, seed, wmax)  # count only
+    d = torch.empty((max(md, 1), 3), dtype=torch.int32, device="cuda")
+    got = ctx.gen_rgg2d_dev(n, radius, seed, wmax, d.data_ptr(), md)
+    assert got == md
+    torch.cuda.synchronize()
+    return d[:md].cpu().numpy().view(np.uint32).reshape(-1).view(kamsta.WEDGE)
+
+
+@pytest.mark.parametrize("n,deg,seed", [(1, 4.0, 1), (2, 4.0, 1), (100, 4.0, 2), (1000, 16.0, 3),
+                                        (1 << 16, 16.0, 4), (1 << 18, 8.0, 5),
+                                        (1 << 20, 16.0, 6)])
+def test_rgg2d_matches_oracle(kamsta, oracle, n, deg, seed):
+    ctx = kamsta.Context(0)
+    r = oracle.rgg_radius(n, deg)
+    assert np.array_equal(_dev_rgg(kamsta, ctx, n, r, seed), oracle.gen_rgg2d(n, r, seed))
+
+
+@pytest.mark.parametrize("radius", [0.0, 1.0, 0.3])
+def test_rgg2d_extreme_radii(kamsta, oracle, radius):
+    ctx = kamsta.Context(0)
+    assert np.array_equal(_dev_rgg(kamsta, ctx, 300, radius, 9), oracle.gen_rgg2d(300, radius, 9))
+
+
+def test_rgg2d_capacity_error(kamsta):
+    import torch
+    ctx = kamsta.Context(0)
+    n = 5000
+    r = 0.02
+    md = ctx.gen_rgg2d_dev(n, r, 1, 254)
+    assert md > 10
+    d = torch.empty((md, 3), dtype=torch.int32, device="cuda")
+    with pytest.raises(kamsta.KamstaError):
+        ctx.gen_rgg2d_dev(n, r, 1, 254, d.data_ptr(), md - 1)
+
+
+@pytest.mark.parametrize("algo", ["boruvka_plain", "boruvka_local", "filter_boruvka"])
+@pytest.mark.parametrize("n,deg", [(1 << 12, 4.0), (1 << 16, 16.0), (1 << 18, 6.0)])
+def test_mst_on_rgg2d(kamsta, oracle, algo, n, deg):
+    from tests.test_parity_gpu import _check, _configs
+    fn, cfg = _configs(kamsta)[algo]
+    e = oracle.gen_rgg2d(n, oracle.rgg_radius(n, deg), 40 + n % 7)
+    _check(oracle, fn(e, cfg, n=n), e, n)

@@ -93,3 +93,55 @@ def test_gnm_properties(oracle, n, m, wmax):
 def test_gnm_rejects_too_many_edges(oracle):
     with pytest.raises(ValueError):
         oracle.gen_gnm(4, 7, 1)
+
+
+def _mix64(z):
+    M = (1 << 64) - 1
+    z = (z + 0x9E3779B97F4A7C15) & M
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & M
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & M
+    return z ^ (z >> 31)
+
+
+def _py_rgg2d(n, radius, seed, wmax=254):
+    """All-pairs restatement of the RGG-2D definition (small n only)."""
+    base = _mix64(seed ^ 0x5247473244)
+    wseed = _mix64(seed ^ 0x6A09E667F3BCC909)
+    R = 0 if radius <= 0 else (1 << 31) if radius >= 1 else int(radius * 2147483648.0)
+    cap = max(1, min(int(n ** 0.5 + 1e-9), 65536))
+    while cap * cap > n:
+        cap -= 1
+    cap = max(cap, 1)
+    G = cap if R == 0 else max(1, min((1 << 31) // R, cap))
+    pts = []
+    for i in range(n):
+        x, y = _mix64((base + 2 * i) % (1 << 64)) >> 33, _mix64((base + 2 * i + 1) % (1 << 64)) >> 33
+        cell = ((y * G) >> 31) * G + ((x * G) >> 31)
+        pts.append((cell, i, x, y))
+    pts.sort()
+    out = []
+    for j, (_, _, xj, yj) in enumerate(pts):
+        for k, (_, _, xk, yk) in enumerate(pts):
+            if k != j and (xj - xk) ** 2 + (yj - yk) ** 2 <= R * R:
+                canon = (min(j, k) << 32) | max(j, k)
+                w = 1 + ((_mix64(wseed ^ canon) * wmax) >> 64)
+                out.append((j, k, w))
+    return out
+
+
+@pytest.mark.parametrize("n,radius,seed", [(1, 0.5, 1), (40, 0.2, 2), (200, 0.1, 3),
+                                           (150, 1.0, 4), (90, 0.0, 5)])
+def test_rgg2d_matches_definition(oracle, n, radius, seed):
+    e = oracle.gen_rgg2d(n, radius, seed)
+    got = [(int(a), int(b), int(w)) for a, b, w in zip(e["src"], e["dst"], e["w"])]
+    assert got == _py_rgg2d(n, radius, seed)
+
+
+def test_rgg2d_properties(oracle):
+    n = 1 << 15
+    e = oracle.gen_rgg2d(n, oracle.rgg_radius(n, 16), 7)
+    s, d = e["src"].astype(np.uint64), e["dst"].astype(np.uint64)
+    k = (s << np.uint64(32)) | d
+    assert np.all(k[1:] > k[:-1])  # (src,dst) sorted, no duplicates
+    assert np.array_equal(np.sort((d << np.uint64(32)) | s), k)  # both directions
+    assert 14.0 < len(e) / n < 16.5  # border effects lower the mean degree slightly
