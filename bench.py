@@ -52,6 +52,16 @@ def parse_args():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-variants", action="store_true")
+    p.add_argument("--no-batch", action="store_true", help="skip the batched-solve workload")
+    p.add_argument("--no-serving", action="store_true", help="skip the serving workload")
+    p.add_argument("--batch-graphs", type=int, default=4096)
+    p.add_argument("--batch-budget-gb", type=float, default=64.0)
+    p.add_argument("--batch-steps", type=int, default=3)
+    p.add_argument("--serve-requests", type=int, default=20000)
+    p.add_argument("--serve-rate", type=float, default=0.0,
+                   help="Poisson arrival rate (requests/s); 0 = half the batched graphs/s")
+    p.add_argument("--serve-plain-requests", type=int, default=2000,
+                   help="requests replayed through sequential plain solves")
     return p.parse_args()
 
 
@@ -185,6 +195,155 @@ def run_reference(args, rep):
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def run_batch(args, K, ctx, sh, seed):
+    """4096 graphs (n log-uniform in [2^8, 2^20], degree U[4, 32], GNM/RGG
+    alternating) solved by kamsta_mst_batch_dev, against per-graph sequential
+    launches of the plain solver (kamsta_mst_boruvka_dev) on the same inputs."""
+    import torch
+    from kamsta_gb300 import workloads as W
+    specs = W.mixed_specs(args.batch_graphs, seed)
+    t0 = time.perf_counter()
+    edges, outs, counts = W.materialize(ctx, specs, stream=sh)
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    descs = W.descs_for(K, specs, edges, outs, counts)
+    cfg = K.AlgorithmConfig(local_preprocessing=K.LocalPreprocessing(args.local_preprocessing))
+    budget = int(args.batch_budget_gb * (1 << 30))
+    entries = sum(counts)
+    ctx.batch_dev(descs, cfg, budget, stream=sh)  # warm-up
+    torch.cuda.synchronize()
+    times, st = [], {}
+    for _ in range(args.batch_steps):
+        t0 = time.perf_counter()
+        ctx.batch_dev(descs, cfg, budget, stream=sh, stats=st)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    tb = statistics.median(times)
+    weights = [descs[i].total_weight for i in range(len(specs))]
+    counts_out = [descs[i].out_count for i in range(len(specs))]
+    assert all(descs[i].status == 0 for i in range(len(specs)))
+    # sequential plain launches, one graph after the other
+    tmp = {}
+    for i in range(min(8, len(specs))):  # warm the per-call path
+        ctx.boruvka_dev(edges[i].data_ptr(), counts[i], specs[i].n, outs[i].data_ptr(), cfg,
+                        stream=sh)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    seq_launches = 0
+    exact = True
+    seq_ms = []
+    for i, s_ in enumerate(specs):
+        ta = time.perf_counter()
+        k = ctx.boruvka_dev(edges[i].data_ptr(), counts[i], s_.n, outs[i].data_ptr(), cfg,
+                            stream=sh, stats=tmp)
+        seq_ms.append((time.perf_counter() - ta) * 1e3)
+        seq_launches += tmp["gpu_launches"]
+        exact &= (k == counts_out[i] and tmp["total_weight"] == weights[i])
+    torch.cuda.synchronize()
+    ts = time.perf_counter() - t0
+    line = {
+        "workload": (f"{len(specs)} graphs, n log-uniform in [2^8, 2^20], degree U[4,32], "
+                     "GNM/RGG-2D alternating, weights U[1,254], seeded per graph"),
+        "metric": "batched graphs/s", "value": len(specs) / tb, "unit": "graphs/s",
+        "ms_per_batch": tb * 1e3, "steps": args.batch_steps, "warmup": 1,
+        "directed_entries": entries, "edges_per_s": entries / tb,
+        "waves": st.get("waves"), "budget_gb": args.batch_budget_gb,
+        "gpu_launches": st.get("gpu_launches"), "union_solve_ms": st.get("solve_ms"),
+        "sequential_plain": {"value": len(specs) / ts, "unit": "graphs/s", "ms": ts * 1e3,
+                             "gpu_launches": seq_launches,
+                             "api": "kamsta_mst_boruvka_dev per graph"},
+        "speedup_vs_sequential": ts / tb,
+        "exact_vs_sequential": bool(exact),
+        "generation_s": gen_s,
+        "inputs": "device-resident (generated once before timing)",
+    }
+    return {"line": line, "specs": specs, "edges": edges, "outs": outs, "counts": counts,
+            "weights": weights, "graphs_per_s": len(specs) / tb, "seq_ms": seq_ms}
+
+
+def run_serving(args, K, ctx, sh, b):
+    """Poisson arrivals of requests drawn from the batch graph mix, served by
+    kamsta_server (continuous batching under the memory budget), against the
+    same arrivals replayed through sequential plain solves."""
+    import numpy as np
+    import torch
+    from kamsta_gb300 import workloads as W
+    specs, edges, counts, weights = b["specs"], b["edges"], b["counts"], b["weights"]
+    rng = np.random.default_rng(args.seed + 17)
+    R = args.serve_requests
+    gidx = rng.integers(0, len(specs), size=R)
+    rate = args.serve_rate or 0.5 * b["graphs_per_s"]
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=R))
+    # one output region per request (requests of the same graph may overlap)
+    ns = np.array([max(specs[g].n, 1) for g in gidx], dtype=np.int64)
+    offs = np.concatenate([[0], np.cumsum(ns)])
+    out = torch.empty((int(offs[-1]), 3), dtype=torch.int32, device="cuda")
+    base = out.data_ptr()
+    cfg = K.AlgorithmConfig(local_preprocessing=K.LocalPreprocessing(args.local_preprocessing))
+    srv = K.Server(torch.cuda.current_device(), budget_bytes=int(args.batch_budget_gb * (1 << 30)),
+                   workers=2, config=cfg)
+    done = {}
+    stop = threading.Event()
+
+    def collector():
+        while len(done) < R and not stop.is_set():
+            for c in srv.poll(timeout_us=20000):
+                done[c["tag"]] = c
+
+    th = threading.Thread(target=collector, daemon=True)
+    th.start()
+    t_start = time.perf_counter()
+    sub_t = np.empty(R)
+    for i in range(R):
+        target = t_start + arrivals[i]
+        while True:
+            now = time.perf_counter()
+            if now >= target:
+                break
+            if target - now > 2e-3:
+                time.sleep(target - now - 1e-3)
+        g = int(gidx[i])
+        sub_t[i] = time.perf_counter()
+        srv.submit(edges[g].data_ptr(), counts[g], specs[g].n, base + 12 * int(offs[i]), tag=i)
+    th.join(timeout=600)
+    stop.set()
+    t_end = time.perf_counter()
+    sst = srv.stats()
+    srv.close()
+    assert len(done) == R, f"serving: {len(done)} of {R} requests finished"
+    lat = [(done[i]["finish_us"] - done[i]["submit_us"]) / 1e3 for i in range(R)]
+    exact = all(done[i]["status"] == 0 and done[i]["total_weight"] == weights[int(gidx[i])]
+                for i in range(R))
+    span = max(done[i]["finish_us"] for i in range(R)) / 1e6 - min(
+        done[i]["submit_us"] for i in range(R)) / 1e6
+    res = {"workload": f"{R} requests, Poisson arrivals, graphs drawn from the batch mix",
+           "rate_per_s": rate, "requests": R, "throughput": R / span, "unit": "graphs/s",
+           **W.percentiles(lat), "mean_ms": float(np.mean(lat)),
+           "mean_batch": float(np.mean([done[i]["batch_size"] for i in range(R)])),
+           "waves": sst["waves"], "workers": 2, "budget_gb": args.batch_budget_gb,
+           "exact_vs_batch": bool(exact)}
+    # sequential plain solves under the same arrivals (FIFO, one at a time)
+    P = min(args.serve_plain_requests, R)
+    lat_p = []
+    t_free = 0.0
+    d_o = torch.empty((max(s.n for s in specs), 3), dtype=torch.int32, device="cuda")
+    t0 = time.perf_counter()
+    for i in range(P):
+        arr = t0 + arrivals[i]
+        now = time.perf_counter()
+        if now < arr:
+            time.sleep(arr - now)
+        g = int(gidx[i])
+        ctx.boruvka_dev(edges[g].data_ptr(), counts[g], specs[g].n, d_o.data_ptr(), cfg,
+                        stream=sh)
+        t_free = time.perf_counter()
+        lat_p.append((t_free - arr) * 1e3)
+    res["plain_sequential"] = {"requests": P, "throughput": P / (t_free - t0),
+                               **W.percentiles(lat_p), "mean_ms": float(np.mean(lat_p)),
+                               "api": "kamsta_mst_boruvka_dev per request, FIFO"}
+    return res
 
 
 def main():
@@ -359,6 +518,16 @@ def main():
             "sample": f"GNM n=2^{args.sample_log_n} m=2^{args.sample_log_m} seed={args.seed}, "
                       f"median of {len(times)} runs ({per:.3f} s each)",
             "gpu_same_sample_ms": sts["device_ms"]}
+    # ---- many-graph workloads: batched solve and the serving loop
+    if not (args.no_batch and args.no_serving):
+        del d_edges, d_out
+        torch.cuda.empty_cache()
+        ctx.trim()
+        bres = run_batch(args, K, ctx, sh, seed)
+        if not args.no_batch:
+            line["batch"] = bres["line"]
+        if not args.no_serving:
+            line["serving"] = run_serving(args, K, ctx, sh, bres)
     if rep.rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()

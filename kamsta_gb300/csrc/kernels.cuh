@@ -472,6 +472,65 @@ __global__ void __launch_bounds__(kBlock, 3)
 }
 
 // ---------------------------------------------------------------------------
+// Parallel-edge removal (EdgeProcessor::remove_duplicates_impl,
+// duplicate_detection.hpp:25-64: sort by (src, dst, w), keep the lightest).
+// Keys over the physical slots of a segmented list:
+//   ((min label << bb | max label) << wbits) | w,  value = slot position;
+// empty slots get ~0 and sort last.  After a stable LSD radix sort over the
+// key bits, the head of every (min, max) run is its lightest edge, ties
+// broken by the lower position, i.e. the survivor under the (w, min, max)
+// order.  Every other slot of the run is marked dead in place by turning it
+// into a self loop (b = a), which the next relabel pass drops.  A vertex's
+// minimum edge is always a run head, so fused minima and the hook are
+// unaffected.
+__global__ void k_list_wmax(SegIn in, uint32_t* out) {
+  const uint64_t phys = static_cast<uint64_t>(in.nseg) * in.cap;
+  uint32_t mx = 0;
+  for (uint64_t q = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; q < phys;
+       q += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    const uint32_t seg = static_cast<uint32_t>(q / in.cap);
+    if (q - static_cast<uint64_t>(seg) * in.cap < in.count[seg]) mx = max(mx, in.base[q].w);
+  }
+  mx = __reduce_max_sync(kFull, mx);
+  if ((threadIdx.x & 31) == 0 && mx) atomicMax(out, mx);
+}
+
+__global__ void k_dedupe_keys(SegIn in, uint32_t bb, uint32_t wbits, uint64_t* __restrict__ keys,
+                              uint32_t* __restrict__ vals) {
+  const uint64_t phys = static_cast<uint64_t>(in.nseg) * in.cap;
+  for (uint64_t q = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; q < phys;
+       q += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    const uint32_t seg = static_cast<uint32_t>(q / in.cap);
+    uint64_t key = ~0ull;
+    if (q - static_cast<uint64_t>(seg) * in.cap < in.count[seg]) {
+      const Rec r = in.base[q];
+      const uint64_t lo = min(r.a, r.b), hi = max(r.a, r.b);
+      key = (((lo << bb) | hi) << wbits) | r.w;
+    }
+    keys[q] = key;
+    vals[q] = static_cast<uint32_t>(q);
+  }
+}
+
+__global__ void k_dedupe_mark(const uint64_t* __restrict__ keys, const uint32_t* __restrict__ vals,
+                              uint64_t phys, uint32_t wbits, Rec* base,
+                              unsigned long long* dead) {
+  uint32_t d = 0;
+  for (uint64_t j = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; j < phys;
+       j += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    const uint64_t k = keys[j];
+    if (j == 0 || k == ~0ull) continue;
+    if ((k >> wbits) == (keys[j - 1] >> wbits)) {
+      Rec* r = base + vals[j];
+      r->b = r->a;
+      ++d;
+    }
+  }
+  d = __reduce_add_sync(kFull, d);
+  if ((threadIdx.x & 31) == 0 && d) atomicAdd(dead, static_cast<unsigned long long>(d));
+}
+
+// ---------------------------------------------------------------------------
 // Hook (determine_mst_edges, mst_utils_cut_edges.hpp:102-166, without cut
 // edges): every live vertex hooks onto the other endpoint of its minimum
 // edge; of a mutual pair the lower label stays root.  Vertices without an

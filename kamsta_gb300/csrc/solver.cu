@@ -24,6 +24,7 @@
 
 #include "kernels.cuh"
 #include "solver.cuh"
+#include "sort_gen.cuh"
 
 namespace kamsta {
 
@@ -142,6 +143,9 @@ class Solve {
   // Boruvka rounds on list L (dense labels in [0, nreps_)); minA_ holds the
   // round-0 minima.  Frees L if `own` is set.
   kamsta_status rounds(SegList* L, bool own);
+  // Parallel-edge removal on L (labels < nr): marks every edge but the
+  // lightest of each endpoint pair dead (a self loop) for the next pass.
+  kamsta_status dedupe(SegList* L, uint32_t nr);
   // Relabel `L` (or the directed input when L == nullptr, weights in
   // [wmin, wmax], a share `frac` of the entries) into the current dense
   // labels, fuse the round-0 minimum and contract the result.
@@ -206,7 +210,7 @@ class Solve {
   bool aligned16_ = false;
   bool debug_ = false;
   bool tolerate_overflow_ = false;
-  uint32_t launches_ = 0, rounds_ = 0, levels_ = 0;
+  uint32_t launches_ = 0, rounds_ = 0, levels_ = 0, dedupe_passes_ = 0;
   uint64_t alg_bytes_ = 0;
   double phase_ms_[KAMSTA_PHASES] = {};
   uint64_t phase_bytes_[KAMSTA_PHASES] = {};
@@ -484,6 +488,59 @@ kamsta_status Solve::pass(int phase, const SegList* src, const uint32_t* map, ui
 // ---------------------------------------------------------------------------
 // Boruvka rounds (boruvka3).  One host read per round: the new edge, vertex
 // and forest-edge counts.
+kamsta_status Solve::dedupe(SegList* L, uint32_t nr) {
+  if (L->total < 2 || nr < 2) return KAMSTA_OK;
+  const uint64_t phys = uint64_t(L->nseg) * L->cap;
+  if (phys >= (1ull << 32) - 8192) return KAMSTA_OK;  // positions ride in 32 bits
+  uint32_t bb = 1;
+  while (bb < 32 && (1ull << bb) < nr) ++bb;
+  const int t0 = tick();
+  uint32_t* d_wmax = reinterpret_cast<uint32_t*>(&ctx_->d_counters[kCMisc].cnt[2]);
+  CU_TRY(cudaMemsetAsync(ctx_->d_counters + kCMisc, 0, sizeof(DevCounters), st_));
+  k_list_wmax<<<grid_for(phys), kBlock, 0, st_>>>(L->in(), d_wmax);
+  KS_TRY(fetch_counters());
+  const uint32_t wmax = static_cast<uint32_t>(ctx_->h_counters[kCMisc].cnt[2]);
+  const uint32_t wbits = wmax ? 32u - static_cast<uint32_t>(__builtin_clz(wmax)) : 1u;
+  if (2 * bb + wbits > 64) return KAMSTA_OK;  // key does not fit: keep the duplicates
+  const int bits = static_cast<int>(2 * bb + wbits);
+  const RadixScratch rs = radix_scratch_bytes(phys);
+  const size_t kb = round_up(phys * sizeof(uint64_t), 256), vb = round_up(phys * sizeof(uint32_t), 256);
+  const size_t cb = round_up(rs.counts * sizeof(uint32_t), 256);
+  const size_t sb = round_up(rs.status * sizeof(uint64_t), 256);
+  void* mem = nullptr;
+  CU_TRY(cudaMallocFromPoolAsync(&mem, 2 * kb + 2 * vb + cb + sb, ctx_->pool, st_));
+  char* m = static_cast<char*>(mem);
+  uint64_t* keys = reinterpret_cast<uint64_t*>(m);
+  uint64_t* keys2 = reinterpret_cast<uint64_t*>(m + kb);
+  uint32_t* vals = reinterpret_cast<uint32_t*>(m + 2 * kb);
+  uint32_t* vals2 = reinterpret_cast<uint32_t*>(m + 2 * kb + vb);
+  uint32_t* counts = reinterpret_cast<uint32_t*>(m + 2 * kb + 2 * vb);
+  uint64_t* status = reinterpret_cast<uint64_t*>(m + 2 * kb + 2 * vb + cb);
+  k_dedupe_keys<<<grid_for(phys), kBlock, 0, st_>>>(L->in(), bb, wbits, keys, vals);
+  int alt = 0;
+  cudaError_t e = radix_sort_pairs_u32(st_, keys, keys2, vals, vals2, phys, bits, counts, status,
+                                       &ctx_->d_counters[kCMisc].ticket, ctx_->d_err, &alt, sms_);
+  if (e != cudaSuccess) {
+    cudaFreeAsync(mem, st_);
+    return cuda_status(e, "radix sort (dedupe)");
+  }
+  if (alt) {
+    std::swap(keys, keys2);
+    std::swap(vals, vals2);
+  }
+  k_dedupe_mark<<<grid_for(phys), kBlock, 0, st_>>>(keys, vals, phys, wbits, L->base,
+                                                   &ctx_->d_counters[kCMisc].cnt[3]);
+  CU_TRY(cudaFreeAsync(mem, st_));
+  tock(KAMSTA_PHASE_DEDUPE, t0);
+  const uint32_t passes = static_cast<uint32_t>((bits + 7) / 8);
+  // wmax read; keys: record read + key/value write; per digit pass: upsweep
+  // read, downsweep read + write of keys and values; mark: keys + values
+  account(KAMSTA_PHASE_DEDUPE,
+          phys * (16 + 16 + 12 + uint64_t(passes) * (8 + 24) + 12), 3 + 3 * passes);
+  dedupe_passes_++;
+  return KAMSTA_OK;
+}
+
 kamsta_status Solve::rounds(SegList* L, bool own) {
   levels_++;
   const uint32_t n0 = nreps_;
@@ -505,6 +562,10 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
     }
     trace(cur->total, nr);
     const uint64_t m = cur->total;
+    if (!(cfg_.flags & KAMSTA_FLAG_DEDUPE_NEVER) &&
+        ((cfg_.flags & KAMSTA_FLAG_DEDUPE_ALWAYS) ||
+         (cfg_.dedupe_ratio && m > uint64_t(cfg_.dedupe_ratio) * nr)))
+      KS_TRY(dedupe(cur, nr));
     CU_TRY(cudaMemsetAsync(ctx_->d_counters + kCVertex, 0, sizeof(DevCounters), st_));
     const int gv = grid_for(nr);
     const int tv = tick();
@@ -883,6 +944,7 @@ kamsta_status Solve::run(Algo algo, kamsta_wedge* d_out, SolveOut* out) {
     stats_->total_weight = out->weight;
     stats_->rounds = rounds_;
     stats_->levels = levels_;
+    stats_->dedupe_passes = dedupe_passes_;
     stats_->gpu_launches = launches_;
     stats_->device_ms = ms;
     stats_->alg_bytes = alg_bytes_;

@@ -25,10 +25,14 @@ def _configs(K):
         "boruvka_local": (K.boruvka, K.AlgorithmConfig(local_preprocessing=LP.MODIFIED_BORUVKA)),
         "filter_boruvka": (K.filter_boruvka, K.AlgorithmConfig()),
         "filter_boruvka_t1": (K.filter_boruvka, K.AlgorithmConfig(filter_threshold=1)),
+        "boruvka_dedupe": (K.boruvka, K.AlgorithmConfig(local_preprocessing=LP.NO_PREPROCESSING,
+                                                        dedupe="always")),
+        "filter_dedupe": (K.filter_boruvka, K.AlgorithmConfig(dedupe="always")),
     }
 
 
-ALGOS = ["boruvka_plain", "boruvka_local", "filter_boruvka", "filter_boruvka_t1"]
+ALGOS = ["boruvka_plain", "boruvka_local", "filter_boruvka", "filter_boruvka_t1",
+         "boruvka_dedupe", "filter_dedupe"]
 
 
 def _triples(mst):
@@ -191,3 +195,20 @@ def test_exactness_n22_m26(kamsta, oracle, algo):
     n, m = 1 << 22, 1 << 26
     e = oracle.gen_gnm(n, m, 2026)
     _check(oracle, fn(e, cfg, n=n), e, n)
+
+
+@pytest.mark.parametrize("mode,ratio", [("always", 0), ("auto", 2), ("auto", 8)])
+def test_dedupe_runs_and_keeps_the_forest(kamsta, oracle, mode, ratio):
+    """Parallel-edge removal (radix sort + keep the lightest) leaves the
+    forest unchanged and actually runs on a graph whose contraction creates
+    many parallel edges."""
+    n, m = 1 << 14, 1 << 19
+    e = oracle.gen_gnm(n, m, 31, 254)
+    st = {}
+    cfg = kamsta.AlgorithmConfig(dedupe=mode, dedupe_ratio=ratio)
+    got = kamsta.boruvka(e, cfg, n=n, stats=st)
+    _check(oracle, got, e, n)
+    assert st["dedupe_passes"] > 0
+    st0 = {}
+    kamsta.boruvka(e, kamsta.AlgorithmConfig(dedupe="never", dedupe_ratio=ratio), n=n, stats=st0)
+    assert st0["dedupe_passes"] == 0
