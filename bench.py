@@ -54,6 +54,9 @@ def parse_args():
     p.add_argument("--no-variants", action="store_true")
     p.add_argument("--no-batch", action="store_true", help="skip the batched-solve workload")
     p.add_argument("--no-serving", action="store_true", help="skip the serving workload")
+    p.add_argument("--no-geometric", action="store_true",
+                   help="skip filter-Boruvka on RGG-2D / RHG (n=2^24, degree 16)")
+    p.add_argument("--geo-log-n", type=int, default=24)
     p.add_argument("--batch-graphs", type=int, default=4096)
     p.add_argument("--batch-budget-gb", type=float, default=64.0)
     p.add_argument("--batch-steps", type=int, default=3)
@@ -195,6 +198,55 @@ def run_reference(args, rep):
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def run_geometric(args, K, ctx, sh, seed):
+    """filter-Boruvka on the geometric / skewed families: RGG-2D and RHG
+    (gamma 3), n=2^geo_log_n, average degree 16, generated on the device."""
+    import math
+    import torch
+    n = 1 << args.geo_log_n
+    res = {}
+    for fam in ("rgg2d", "rhg"):
+        t0 = time.perf_counter()
+        if fam == "rgg2d":
+            r = math.sqrt(16.0 / (math.pi * n))
+            md = ctx.gen_rgg2d_dev(n, r, seed, 254, stream=sh)
+            d = torch.empty((md, 3), dtype=torch.int32, device="cuda")
+            ctx.gen_rgg2d_dev(n, r, seed, 254, d.data_ptr(), md, stream=sh)
+        else:
+            md = ctx.gen_rhg_dev(n, 3.0, 16.0, seed, 254, stream=sh)
+            d = torch.empty((md, 3), dtype=torch.int32, device="cuda")
+            ctx.gen_rhg_dev(n, 3.0, 16.0, seed, 254, d.data_ptr(), md, stream=sh)
+        torch.cuda.synchronize()
+        gen_s = time.perf_counter() - t0
+        out = torch.empty((n, 3), dtype=torch.int32, device="cuda")
+        cfg = K.AlgorithmConfig()
+        ctx.filter_boruvka_dev(d.data_ptr(), md, n, out.data_ptr(), cfg, stream=sh)
+        torch.cuda.synchronize()
+        ms, ws, ks = [], set(), set()
+        for _ in range(max(3, args.steps)):
+            st = {}
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(torch.cuda.current_stream())
+            k = ctx.filter_boruvka_dev(d.data_ptr(), md, n, out.data_ptr(), cfg, stream=sh,
+                                       stats=st)
+            e1.record(torch.cuda.current_stream())
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            ws.add(st["total_weight"])
+            ks.add(k)
+        med = statistics.median(ms)
+        res[fam] = {"workload": f"{fam} n=2^{args.geo_log_n}, average degree 16"
+                                + (", gamma 3" if fam == "rhg" else "") + ", weights U[1,254]",
+                    "algorithm": "filter_boruvka (filter_hybridBoruvka), default config",
+                    "directed_entries": md, "value": md / (med / 1e3), "unit": UNIT,
+                    "ms_per_step": med, "forest_edges": ks.pop(), "forest_weight": ws.pop(),
+                    "deterministic": len(ws) == 0 and len(ks) == 0,
+                    "generation_s": gen_s}
+        del d, out
+        torch.cuda.empty_cache()
+    return res
 
 
 def run_batch(args, K, ctx, sh, seed):
@@ -518,11 +570,15 @@ def main():
             "sample": f"GNM n=2^{args.sample_log_n} m=2^{args.sample_log_m} seed={args.seed}, "
                       f"median of {len(times)} runs ({per:.3f} s each)",
             "gpu_same_sample_ms": sts["device_ms"]}
-    # ---- many-graph workloads: batched solve and the serving loop
-    if not (args.no_batch and args.no_serving):
+    # ---- geometric / skewed families and the many-graph workloads
+    if not (args.no_batch and args.no_serving and args.no_geometric):
         del d_edges, d_out
         torch.cuda.empty_cache()
         ctx.trim()
+    if not args.no_geometric:
+        line["geometric"] = run_geometric(args, K, ctx, sh, seed)
+        ctx.trim()
+    if not (args.no_batch and args.no_serving):
         bres = run_batch(args, K, ctx, sh, seed)
         if not args.no_batch:
             line["batch"] = bres["line"]

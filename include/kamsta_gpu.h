@@ -246,6 +246,24 @@ kamsta_status kamsta_mst_batch(kamsta_ctx* ctx, kamsta_graph_desc* graphs, uint3
                                const kamsta_cfg* cfg, uint64_t budget_bytes,
                                kamsta_batch_stats* stats);
 
+/* Batch tuning of a context: the CTA size of the persistent small-graph
+ * kernel (256, 512 or 1024 threads) and the largest n it takes (4096 ..
+ * 32768; larger graphs go to the union solve).  kamsta_batch_autotune times
+ * every candidate on the given sample of graphs (device buffers; their
+ * outputs are written as by kamsta_mst_batch_dev), keeps the fastest in the
+ * context and reports the timings.  No counterpart in the reference. */
+typedef struct kamsta_tuning {
+  uint32_t small_threads;  /* chosen CTA size                                */
+  uint32_t small_max_n;    /* chosen cutoff                                  */
+  double threads_ms[3];    /* sample's small graphs at 256 / 512 / 1024      */
+  double cutoff_ms[4];     /* whole sample at cutoff 4096 / 8192 / 16384 / 32768 */
+} kamsta_tuning;
+kamsta_status kamsta_batch_autotune(kamsta_ctx* ctx, kamsta_graph_desc* graphs,
+                                    uint32_t count, const kamsta_cfg* cfg,
+                                    kamsta_tuning* out, kamsta_stream stream);
+/* Sets (e.g. from a cached autotune result) or clears (zeros) the tuning. */
+kamsta_status kamsta_ctx_set_tuning(kamsta_ctx* ctx, const kamsta_tuning* tuning);
+
 /* ---- serving loop -------------------------------------------------------
  * No counterpart in the reference.  A continuous-batching request loop:
  * clients submit jobs whose edge arrays already sit in device memory (their
@@ -302,6 +320,66 @@ kamsta_status kamsta_server_stats(kamsta_server* server, uint64_t* queued,
 /* Finishes every queued job, then stops the workers and frees the server. */
 kamsta_status kamsta_server_destroy(kamsta_server* server);
 
+/* ---- compressed input (Compression::SEVEN_BIT_DIFF_ENCODING) ------------
+ * The reference's difference-encoded edge container
+ * (datastructures/compression/difference_encoded_graph.hpp:14-261, varints
+ * of variable_length_encoding.hpp:6-167): per edge varint(src - prev_src),
+ * varint(dst), varint(w), 7 bits per byte, little endian, 0x80 = more bytes
+ * follow.  The list is cut into chunks of chunk_edges (1..4096) edges, each
+ * with its raw first edge and the byte offset of its encoded rest, so the
+ * device decodes one chunk per CTA.  Input must be (src, dst) sorted. */
+typedef struct kamsta_cgraph {
+  uint64_t m_directed;            /* directed entries                          */
+  uint32_t n;                     /* vertex count                              */
+  uint32_t chunk_edges;           /* edges per chunk (the last may be shorter) */
+  uint64_t num_chunks;            /* ceil(m_directed / chunk_edges)            */
+  uint64_t data_bytes;            /* encoded bytes                             */
+  const uint64_t* chunk_offset;   /* [num_chunks + 1] byte offsets into data   */
+  const kamsta_wedge* chunk_first;/* [num_chunks] first edge of each chunk     */
+  const uint8_t* data;            /* encoded edges 1.. of every chunk          */
+} kamsta_cgraph;
+
+/* Host encoder (all host cores).  With data == NULL only *data_bytes (and
+ * chunk_offset, if given) is computed. */
+kamsta_status kamsta_encode_7bit(const kamsta_wedge* edges, uint64_t m_directed,
+                                 uint32_t chunk_edges, uint64_t* chunk_offset,
+                                 kamsta_wedge* chunk_first, uint8_t* data,
+                                 uint64_t data_capacity, uint64_t* data_bytes);
+/* Device decoder: g holds device pointers; d_out receives m_directed entries. */
+kamsta_status kamsta_decode_7bit_dev(kamsta_ctx* ctx, const kamsta_cgraph* g,
+                                     kamsta_wedge* d_out, kamsta_stream stream);
+/* Solve from a compressed graph held in device memory (decoded into
+ * context scratch, then kamsta_mst_boruvka_dev). */
+kamsta_status kamsta_mst_boruvka_7bit_dev(kamsta_ctx* ctx, const kamsta_cgraph* g,
+                                          const kamsta_cfg* cfg, kamsta_wedge* d_out,
+                                          uint64_t* out_count, kamsta_stats* stats,
+                                          kamsta_stream stream);
+/* Same from host memory: only the compressed bytes cross to the device. */
+kamsta_status kamsta_mst_boruvka_7bit(const kamsta_cgraph* g, const kamsta_cfg* cfg,
+                                      kamsta_wedge* out, uint64_t* out_count,
+                                      kamsta_stats* stats);
+
+/* ---- reading the reference's binary edge files -------------------------
+ * Real-world inputs of the reference (evaluation/README.md:21-22, read by
+ * graphs::read_weighted_binaries(files, 4, 1),
+ * benchmarks/mst_benchmarks.hpp:185-190): possibly unsorted edge lists of
+ * 9-byte records (4-byte source, 4-byte destination, 1-byte weight, little
+ * endian), over one or more files.  The files are streamed to the device
+ * (reading and host-to-device copies overlap) and turned into the input
+ * contract: sorted by (src, dst), self loops dropped, of duplicate (src,
+ * dst) entries only the lightest kept; KAMSTA_LOAD_SYMMETRIZE adds the
+ * reverse of every record first, so both directions are present.  n_out =
+ * largest id + 1 (ids < 2^28).  kamsta_wedge9_capacity gives an upper bound
+ * of the entries written (records, doubled when symmetrising). */
+#define KAMSTA_LOAD_SYMMETRIZE 0x1u
+kamsta_status kamsta_wedge9_capacity(const char* const* paths, uint32_t num_paths,
+                                     uint32_t flags, uint64_t* capacity);
+kamsta_status kamsta_load_wedge9_dev(kamsta_ctx* ctx, const char* const* paths,
+                                     uint32_t num_paths, uint32_t flags,
+                                     kamsta_wedge* d_out, uint64_t capacity,
+                                     uint64_t* m_directed_out, uint32_t* n_out,
+                                     kamsta_stream stream);
+
 /* ---- device graph generators (seeded; identical to the oracle's CPU
  * generators).  d_out must hold 2*m entries; *m_directed_out receives the
  * number written.  Stand-ins for KaGen's get_gnm / get_rgg2D / get_rhg
@@ -320,6 +398,16 @@ kamsta_status kamsta_gen_rgg2d_dev(kamsta_ctx* ctx, uint32_t n, double radius,
                                    uint64_t seed, uint32_t max_weight,
                                    kamsta_wedge* d_out, uint64_t capacity,
                                    uint64_t* m_directed_out, kamsta_stream stream);
+/* Threshold random hyperbolic graph: power-law exponent gamma > 2 (the
+ * reference's --gamma), target average degree avg_degree; hubs of very high
+ * degree.  Counting / capacity convention as kamsta_gen_rgg2d_dev.  The
+ * per-point coordinates are computed on the host with the C library's
+ * acosh/exp/sinh; the pair test runs on the device.  Stand-in for get_rhg
+ * (benchmarks/mst_benchmarks.hpp:143-158). */
+kamsta_status kamsta_gen_rhg_dev(kamsta_ctx* ctx, uint32_t n, double gamma,
+                                 double avg_degree, uint64_t seed, uint32_t max_weight,
+                                 kamsta_wedge* d_out, uint64_t capacity,
+                                 uint64_t* m_directed_out, kamsta_stream stream);
 
 #ifdef __cplusplus
 } /* extern "C" */

@@ -28,7 +28,8 @@ from ._native import (FLAG_DEDUPE_ALWAYS, FLAG_DEDUPE_NEVER, FLAG_FILTER, FLAG_S
 
 __all__ = ["LocalPreprocessing", "Compression", "AlgorithmConfig", "boruvka", "filter_boruvka",
            "boruvka_wedge64", "Context", "WEDGE", "WEDGE64", "KamstaError", "Stats",
-           "as_wedges", "mst_weight", "version", "batch", "GraphDesc", "BatchStats", "Server"]
+           "as_wedges", "mst_weight", "version", "batch", "GraphDesc", "BatchStats", "Server", "Compressed",
+           "boruvka_7bit"]
 
 
 class LocalPreprocessing(enum.IntEnum):
@@ -149,6 +150,55 @@ def boruvka_wedge64(input_edges: np.ndarray, config: AlgorithmConfig | None = No
     check(lib().kamsta_mst_boruvka_wedge64(e.ctypes.data_as(C.c_void_p), len(e), int(n),
                                            C.byref(cfg), out.ctypes.data_as(C.c_void_p),
                                            C.byref(cnt), C.byref(st)))
+    if stats is not None:
+        stats.update(st.as_dict())
+    return out[: cnt.value].copy()
+
+
+class Compressed:
+    """A 7-bit varint difference-encoded edge list (kamsta_cgraph) in host
+    memory: per chunk a raw first edge and a byte offset, then varint(src -
+    prev_src), varint(dst), varint(w) per edge (the reference's
+    SEVEN_BIT_DIFF_ENCODING container)."""
+
+    def __init__(self, edges, n: int, chunk_edges: int = 2048):
+        e = as_wedges(edges)
+        self.m, self.n, self.chunk_edges = len(e), int(n), int(chunk_edges)
+        self.num_chunks = (self.m + self.chunk_edges - 1) // self.chunk_edges
+        self.offset = np.zeros(self.num_chunks + 1, np.uint64)
+        self.first = np.empty(max(self.num_chunks, 1), WEDGE)
+        nb = C.c_uint64(0)
+        L = lib()
+        ep = e.ctypes.data if len(e) else None
+        check(L.kamsta_encode_7bit(ep, self.m, self.chunk_edges, self.offset.ctypes.data, None,
+                                   None, 0, C.byref(nb)))
+        self.data = np.empty(max(nb.value, 1), np.uint8)
+        check(L.kamsta_encode_7bit(ep, self.m, self.chunk_edges, self.offset.ctypes.data,
+                                   self.first.ctypes.data, self.data.ctypes.data, nb.value,
+                                   C.byref(nb)))
+        self.data_bytes = int(nb.value)
+
+    def c_struct(self, offset_ptr=None, first_ptr=None, data_ptr=None) -> _native.CGraph:
+        return _native.CGraph(self.m, self.n, self.chunk_edges, self.num_chunks,
+                              self.data_bytes,
+                              offset_ptr if offset_ptr is not None else self.offset.ctypes.data,
+                              first_ptr if first_ptr is not None else self.first.ctypes.data,
+                              data_ptr if data_ptr is not None else self.data.ctypes.data)
+
+    def total_bytes(self) -> int:
+        return self.data_bytes + 8 * (self.num_chunks + 1) + 12 * self.num_chunks
+
+
+def boruvka_7bit(cg: "Compressed", config: AlgorithmConfig | None = None,
+                 stats: dict | None = None) -> np.ndarray:
+    """kamsta_mst_boruvka_7bit: solve from compressed host memory."""
+    g = cg.c_struct()
+    cfg = (config or AlgorithmConfig()).to_c()
+    out = np.empty(max(cg.n, 1), WEDGE)
+    cnt = C.c_uint64(0)
+    st = Stats()
+    check(lib().kamsta_mst_boruvka_7bit(C.byref(g), C.byref(cfg), out.ctypes.data_as(C.c_void_p),
+                                        C.byref(cnt), C.byref(st)))
     if stats is not None:
         stats.update(st.as_dict())
     return out[: cnt.value].copy()
@@ -323,3 +373,72 @@ class Context:
                                          int(max_weight), C.c_void_p(d_out or 0), int(capacity),
                                          C.byref(cnt), C.c_void_p(stream or 0)))
         return int(cnt.value)
+
+    def gen_rhg_dev(self, n: int, gamma: float, avg_degree: float, seed: int, max_weight: int,
+                    d_out: int = 0, capacity: int = 0, stream=0) -> int:
+        """Device threshold random hyperbolic graph.  With d_out == 0 it only
+        counts; returns the number of directed entries."""
+        cnt = C.c_uint64(0)
+        check(lib().kamsta_gen_rhg_dev(self._h, int(n), float(gamma), float(avg_degree),
+                                       int(seed), int(max_weight), C.c_void_p(d_out or 0),
+                                       int(capacity), C.byref(cnt), C.c_void_p(stream or 0)))
+        return int(cnt.value)
+
+    def load_wedge9_dev(self, paths, symmetrize: bool = True, stream=0):
+        """Stream the reference's 9-byte binary edge files to the device.
+        Returns (edges tensor (m, 3) int32 on cuda, m_directed, n)."""
+        import torch
+        if isinstance(paths, (str, bytes)):
+            paths = [paths]
+        arr = (C.c_char_p * len(paths))(*[p.encode() if isinstance(p, str) else p
+                                          for p in paths])
+        flags = _native.LOAD_SYMMETRIZE if symmetrize else 0
+        cap = C.c_uint64(0)
+        check(lib().kamsta_wedge9_capacity(arr, len(paths), flags, C.byref(cap)))
+        out = torch.empty((max(cap.value, 1), 3), dtype=torch.int32, device="cuda")
+        m, n = C.c_uint64(0), C.c_uint32(0)
+        check(lib().kamsta_load_wedge9_dev(self._h, arr, len(paths), flags,
+                                           C.c_void_p(out.data_ptr()), cap.value, C.byref(m),
+                                           C.byref(n), C.c_void_p(stream or 0)))
+        return out[: m.value], int(m.value), int(n.value)
+
+    def _cgraph_dev(self, cg: "Compressed"):
+        import torch
+        off = torch.from_numpy(cg.offset.view(np.int64)).cuda()
+        first = torch.from_numpy(cg.first.view(np.uint32).view(np.int32).copy()).cuda()
+        data = torch.from_numpy(cg.data.view(np.int8).copy()).cuda()
+        torch.cuda.synchronize()
+        return (off, first, data), cg.c_struct(off.data_ptr(), first.data_ptr(), data.data_ptr())
+
+    def decode_7bit_dev(self, cg: "Compressed", d_out: int, stream=0):
+        """Decode a compressed graph (copied to the device first) into d_out."""
+        keep, g = self._cgraph_dev(cg)
+        check(lib().kamsta_decode_7bit_dev(self._h, C.byref(g), C.c_void_p(d_out),
+                                           C.c_void_p(stream or 0)))
+        return keep
+
+    def boruvka_7bit_dev(self, g, d_out: int, config=None, stream=0,
+                         stats: dict | None = None) -> int:
+        """kamsta_mst_boruvka_7bit_dev; g is a CGraph of device pointers."""
+        cfg = (config or AlgorithmConfig()).to_c()
+        cnt = C.c_uint64(0)
+        st = Stats()
+        check(lib().kamsta_mst_boruvka_7bit_dev(self._h, C.byref(g), C.byref(cfg),
+                                                C.c_void_p(d_out), C.byref(cnt), C.byref(st),
+                                                C.c_void_p(stream or 0)))
+        if stats is not None:
+            stats.update(st.as_dict())
+        return int(cnt.value)
+
+    def batch_autotune(self, descs, config=None, stream=0) -> dict:
+        """kamsta_batch_autotune on a sample of graphs (GraphDesc array)."""
+        cfg = (config or AlgorithmConfig()).to_c()
+        t = _native.Tuning()
+        check(lib().kamsta_batch_autotune(self._h, descs, len(descs), C.byref(cfg), C.byref(t),
+                                          C.c_void_p(stream or 0)))
+        return t.as_dict()
+
+    def set_tuning(self, small_threads: int = 0, small_max_n: int = 0):
+        t = _native.Tuning()
+        t.small_threads, t.small_max_n = int(small_threads), int(small_max_n)
+        check(lib().kamsta_ctx_set_tuning(self._h, C.byref(t)))

@@ -24,6 +24,7 @@ FLAG_DEDUPE_NEVER = 0x4
 FLAG_DEDUPE_ALWAYS = 0x8
 FLAG_TRACE = 0x10
 FLAG_FILTER = 0x20
+LOAD_SYMMETRIZE = 0x1
 TRACE_MAX = 128
 PHASES = ["plan", "first_pass", "round_edges", "round_verts", "class_pass", "finalize", "emit",
           "dedupe"]
@@ -99,6 +100,22 @@ class Completion(C.Structure):
                 ("start_us", C.c_double), ("finish_us", C.c_double)]
 
 
+class CGraph(C.Structure):
+    _fields_ = [("m_directed", C.c_uint64), ("n", C.c_uint32), ("chunk_edges", C.c_uint32),
+                ("num_chunks", C.c_uint64), ("data_bytes", C.c_uint64),
+                ("chunk_offset", C.c_void_p), ("chunk_first", C.c_void_p), ("data", C.c_void_p)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("small_threads", C.c_uint32), ("small_max_n", C.c_uint32),
+                ("threads_ms", C.c_double * 3), ("cutoff_ms", C.c_double * 4)]
+
+    def as_dict(self) -> dict:
+        return {"small_threads": self.small_threads, "small_max_n": self.small_max_n,
+                "threads_ms": dict(zip((256, 512, 1024), list(self.threads_ms))),
+                "cutoff_ms": dict(zip((4096, 8192, 16384, 32768), list(self.cutoff_ms)))}
+
+
 _lib = None
 
 # Every symbol declared in include/kamsta_gpu.h, with its ctypes signature.
@@ -128,11 +145,25 @@ SIGNATURES = {
     "kamsta_server_stats": (I32, [P, C.POINTER(U64), C.POINTER(U64), C.POINTER(U64),
                                   C.POINTER(U64)]),
     "kamsta_server_destroy": (I32, [P]),
+    "kamsta_encode_7bit": (I32, [P, U64, U32, P, P, P, U64, C.POINTER(U64)]),
+    "kamsta_decode_7bit_dev": (I32, [P, C.POINTER(CGraph), P, P]),
+    "kamsta_mst_boruvka_7bit_dev": (I32, [P, C.POINTER(CGraph), C.POINTER(Cfg), P,
+                                          C.POINTER(U64), C.POINTER(Stats), P]),
+    "kamsta_mst_boruvka_7bit": (I32, [C.POINTER(CGraph), C.POINTER(Cfg), P, C.POINTER(U64),
+                                      C.POINTER(Stats)]),
+    "kamsta_wedge9_capacity": (I32, [C.POINTER(C.c_char_p), U32, U32, C.POINTER(U64)]),
+    "kamsta_load_wedge9_dev": (I32, [P, C.POINTER(C.c_char_p), U32, U32, P, U64,
+                                     C.POINTER(U64), C.POINTER(U32), P]),
     "kamsta_gen_gnm_dev": (I32, [P, U32, U64, U64, U32, P, C.POINTER(U64), P]),
     "kamsta_gen_rgg2d_dev": (I32, [P, U32, C.c_double, U64, U32, P, U64, C.POINTER(U64), P]),
+    "kamsta_gen_rhg_dev": (I32, [P, U32, C.c_double, C.c_double, U64, U32, P, U64,
+                                 C.POINTER(U64), P]),
     "kamsta_mst_boruvka_noalloc": (I32, [P, U64, U32, P, C.POINTER(U64), C.POINTER(U64), P]),
     "kamsta_mst_batch_dev": (I32, [P, C.POINTER(GraphDesc), U32, C.POINTER(Cfg), U64,
                                    C.POINTER(BatchStats), P]),
+    "kamsta_batch_autotune": (I32, [P, C.POINTER(GraphDesc), U32, C.POINTER(Cfg),
+                                    C.POINTER(Tuning), P]),
+    "kamsta_ctx_set_tuning": (I32, [P, C.POINTER(Tuning)]),
     "kamsta_mst_batch": (I32, [P, C.POINTER(GraphDesc), U32, C.POINTER(Cfg), U64,
                                C.POINTER(BatchStats)]),
 }

@@ -39,8 +39,11 @@ def headers() -> list[str]:
 
 def _compile(src: str, verbose: bool, ptxas_v: bool) -> str:
     obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+    # host code without fused multiply-add: the RHG generator's per-point
+    # values must round exactly like the oracle's (built the same way)
     cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-           "-Xcompiler", "-O3", "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include"),
+           "-Xcompiler", "-O3", "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr",
+           "-I", os.path.join(ROOT, "include"),
            "-c", src, "-o", obj]
     if ptxas_v:
         cmd.insert(1, "-Xptxas=-v")

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "batch.cuh"
+#include "codec.cuh"
 #include "solver.cuh"
 
 namespace kamsta {
@@ -16,8 +17,12 @@ namespace {
 kamsta_status check_cfg(const kamsta_cfg* cfg) {
   if (!cfg) return KAMSTA_OK;
   if (cfg->compression != KAMSTA_NO_COMPRESSION) {
-    set_error("compression: only NO_COMPRESSION is implemented");
-    return KAMSTA_E_UNSUPPORTED;
+    set_error(cfg->compression == KAMSTA_SEVEN_BIT_DIFF_ENCODING
+                  ? "compression: SEVEN_BIT_DIFF_ENCODING input goes through "
+                    "kamsta_mst_boruvka_7bit / kamsta_mst_boruvka_7bit_dev"
+                  : "compression: unknown value");
+    return cfg->compression == KAMSTA_SEVEN_BIT_DIFF_ENCODING ? KAMSTA_E_UNSUPPORTED
+                                                               : KAMSTA_E_INPUT;
   }
   if (cfg->local_preprocessing < KAMSTA_NO_PREPROCESSING ||
       cfg->local_preprocessing > KAMSTA_REDUCE_EDGES_THEN_BORUVKA) {
@@ -128,6 +133,49 @@ kamsta_status solve_dev(Algo algo, kamsta_ctx* ctx, const kamsta_wedge* d_edges,
   return s;
 }
 
+// Decode a compressed graph (device pointers) into pool scratch and solve it.
+kamsta_status solve_7bit_locked(kamsta_ctx* ctx, const kamsta_cgraph& g, kamsta_cfg c,
+                                kamsta_wedge* d_out, uint64_t* out_count, kamsta_stats* stats,
+                                cudaStream_t st) {
+  *out_count = 0;
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  if (g.m_directed == 0 || g.n == 0) return KAMSTA_OK;
+  void* buf = nullptr;
+  cudaError_t e = cudaMallocFromPoolAsync(&buf, g.m_directed * sizeof(kamsta_wedge), ctx->pool, st);
+  if (e != cudaSuccess) return cuda_status(e, "decode buffer");
+  struct Free {
+    void* p;
+    cudaStream_t s;
+    ~Free() { cudaFreeAsync(p, s); }
+  } fr{buf, st};
+  e = cudaMemsetAsync(ctx->d_err, 0, sizeof(uint32_t), st);
+  if (e != cudaSuccess) return cuda_status(e, "cudaMemsetAsync");
+  kamsta_status s = decode_7bit(g, static_cast<kamsta_wedge*>(buf), ctx->d_err, st);
+  if (s != KAMSTA_OK) return s;
+  e = cudaMemcpyAsync(ctx->h_err, ctx->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_status(e, "decode");
+  if (*ctx->h_err) {
+    set_error("decode_7bit: malformed chunk (value count or length)");
+    return KAMSTA_E_INPUT;
+  }
+  c.compression = KAMSTA_NO_COMPRESSION;
+  SolveOut so;
+  s = solve_device(ctx, Algo::kBoruvka, static_cast<kamsta_wedge*>(buf), g.m_directed, g.n, c,
+                   d_out, &so, stats, st);
+  *out_count = so.count;
+  return s;
+}
+
+kamsta_status check_cgraph(const kamsta_cgraph* g) {
+  if (!g || (g->m_directed && (!g->chunk_offset || !g->chunk_first ||
+                               (g->data_bytes && !g->data)))) {
+    set_error("null pointer argument");
+    return KAMSTA_E_INPUT;
+  }
+  return KAMSTA_OK;
+}
+
 kamsta_status batch_call(kamsta_ctx* ctx, kamsta_graph_desc* graphs, uint32_t count,
                          const kamsta_cfg* cfg, uint64_t budget, kamsta_batch_stats* stats,
                          bool host_buffers, kamsta_stream stream) {
@@ -189,6 +237,9 @@ kamsta_status kamsta_ctx_create(int device, kamsta_ctx** out) {
   c->device = device;
   kamsta_status s = KAMSTA_OK;
   if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming)) != cudaSuccess ||
       (e = cudaMalloc(&c->d_counters, sizeof(DevCounters) * kCSlots)) != cudaSuccess ||
       (e = cudaMalloc(&c->d_err, sizeof(uint32_t))) != cudaSuccess ||
       (e = cudaMalloc(&c->d_samples, sizeof(uint32_t) * kSampleCap)) != cudaSuccess ||
@@ -229,6 +280,7 @@ kamsta_status kamsta_ctx_destroy(kamsta_ctx* ctx) {
   cudaGetDevice(&prev);
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->aux) cudaStreamSynchronize(ctx->aux);
   ctx->fixed.release();
   if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
   if (ctx->d_counters) cudaFree(ctx->d_counters);
@@ -241,6 +293,9 @@ kamsta_status kamsta_ctx_destroy(kamsta_ctx* ctx) {
   for (int i = 0; i < kTimerEvents; ++i)
     if (ctx->tev[i]) cudaEventDestroy(ctx->tev[i]);
   ctx->io.release();
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+  if (ctx->aux) cudaStreamDestroy(ctx->aux);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   cudaSetDevice(prev);
   delete ctx;
@@ -322,6 +377,119 @@ kamsta_status kamsta_mst_filter_boruvka_dev(kamsta_ctx* ctx, const kamsta_wedge*
                    stream);
 }
 
+kamsta_status kamsta_encode_7bit(const kamsta_wedge* edges, uint64_t m_directed,
+                                 uint32_t chunk_edges, uint64_t* chunk_offset,
+                                 kamsta_wedge* chunk_first, uint8_t* data,
+                                 uint64_t data_capacity, uint64_t* data_bytes) {
+  if (!data_bytes || (m_directed && !edges)) {
+    set_error("null pointer argument");
+    return KAMSTA_E_INPUT;
+  }
+  return encode_7bit(edges, m_directed, chunk_edges, chunk_offset, chunk_first, data,
+                     data_capacity, data_bytes);
+}
+
+kamsta_status kamsta_decode_7bit_dev(kamsta_ctx* ctx, const kamsta_cgraph* g,
+                                     kamsta_wedge* d_out, kamsta_stream stream) {
+  kamsta_status s = check_cgraph(g);
+  if (s != KAMSTA_OK) return s;
+  if (!ctx || (g->m_directed && !d_out)) {
+    set_error("null pointer argument");
+    return KAMSTA_E_INPUT;
+  }
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  cudaError_t e = cudaMemsetAsync(ctx->d_err, 0, sizeof(uint32_t), st);
+  if (e != cudaSuccess) return cuda_status(e, "cudaMemsetAsync");
+  s = decode_7bit(*g, d_out, ctx->d_err, st);
+  if (s != KAMSTA_OK) return s;
+  e = cudaMemcpyAsync(ctx->h_err, ctx->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_status(e, "decode");
+  if (*ctx->h_err) {
+    set_error("decode_7bit: malformed chunk (value count or length)");
+    return KAMSTA_E_INPUT;
+  }
+  return KAMSTA_OK;
+}
+
+kamsta_status kamsta_mst_boruvka_7bit_dev(kamsta_ctx* ctx, const kamsta_cgraph* g,
+                                          const kamsta_cfg* cfg, kamsta_wedge* d_out,
+                                          uint64_t* out_count, kamsta_stats* stats,
+                                          kamsta_stream stream) {
+  kamsta_status s = check_cgraph(g);
+  if (s != KAMSTA_OK) return s;
+  if (!ctx || !out_count || (g->n > 1 && !d_out)) {
+    set_error("null pointer argument");
+    return KAMSTA_E_INPUT;
+  }
+  kamsta_cfg c = cfg_or_default(cfg);
+  c.compression = KAMSTA_NO_COMPRESSION;
+  s = check_cfg(&c);
+  if (s != KAMSTA_OK) return s;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  return solve_7bit_locked(ctx, *g, c, d_out, out_count, stats, st);
+}
+
+kamsta_status kamsta_mst_boruvka_7bit(const kamsta_cgraph* g, const kamsta_cfg* cfg,
+                                      kamsta_wedge* out, uint64_t* out_count,
+                                      kamsta_stats* stats) {
+  kamsta_status s = check_cgraph(g);
+  if (s != KAMSTA_OK) return s;
+  if (!out_count || (g->n > 1 && !out)) {
+    set_error("null pointer argument");
+    return KAMSTA_E_INPUT;
+  }
+  kamsta_cfg c = cfg_or_default(cfg);
+  c.compression = KAMSTA_NO_COMPRESSION;
+  s = check_cfg(&c);
+  if (s != KAMSTA_OK) return s;
+  kamsta_ctx* ctx = nullptr;
+  s = g_default.get(&ctx);
+  if (s != KAMSTA_OK) return s;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  *out_count = 0;
+  if (g->m_directed == 0 || g->n == 0) {
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    return KAMSTA_OK;
+  }
+  // compressed bytes, chunk table and the forest in the context's io arena
+  const size_t ob = (sizeof(uint64_t) * (g->num_chunks + 1) + 255) & ~size_t(255);
+  const size_t fb = (sizeof(kamsta_wedge) * g->num_chunks + 255) & ~size_t(255);
+  const size_t db = (g->data_bytes + 255) & ~size_t(255);
+  const size_t outb = std::max<uint64_t>(g->n, 1) * sizeof(kamsta_wedge);
+  cudaError_t e = ctx->io.reserve(ob + fb + db + outb + 1024);
+  if (e != cudaSuccess) return cuda_status(e, "device buffers for compressed input");
+  kamsta_cgraph dg = *g;
+  uint64_t* doff = ctx->io.take<uint64_t>(g->num_chunks + 1);
+  kamsta_wedge* dfirst = ctx->io.take<kamsta_wedge>(g->num_chunks);
+  uint8_t* ddata = ctx->io.take<uint8_t>(std::max<uint64_t>(g->data_bytes, 1));
+  kamsta_wedge* dout = ctx->io.take<kamsta_wedge>(std::max<uint64_t>(g->n, 1));
+  cudaStream_t st = ctx->stream;
+  e = cudaMemcpyAsync(doff, g->chunk_offset, sizeof(uint64_t) * (g->num_chunks + 1),
+                      cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dfirst, g->chunk_first, sizeof(kamsta_wedge) * g->num_chunks,
+                        cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && g->data_bytes)
+    e = cudaMemcpyAsync(ddata, g->data, g->data_bytes, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_status(e, "cudaMemcpyAsync(H2D)");
+  dg.chunk_offset = doff;
+  dg.chunk_first = dfirst;
+  dg.data = ddata;
+  uint64_t cnt = 0;
+  s = solve_7bit_locked(ctx, dg, c, dout, &cnt, stats, st);
+  if (s != KAMSTA_OK) return s;
+  if (cnt) {
+    e = cudaMemcpyAsync(out, dout, cnt * sizeof(kamsta_wedge), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_status(e, "cudaMemcpyAsync(D2H)");
+  }
+  *out_count = cnt;
+  return KAMSTA_OK;
+}
+
 kamsta_status kamsta_mst_batch_dev(kamsta_ctx* ctx, kamsta_graph_desc* graphs, uint32_t count,
                                    const kamsta_cfg* cfg, uint64_t budget_bytes,
                                    kamsta_batch_stats* stats, kamsta_stream stream) {
@@ -330,6 +498,38 @@ kamsta_status kamsta_mst_batch_dev(kamsta_ctx* ctx, kamsta_graph_desc* graphs, u
     return KAMSTA_E_INPUT;
   }
   return batch_call(ctx, graphs, count, cfg, budget_bytes, stats, false, stream);
+}
+
+kamsta_status kamsta_batch_autotune(kamsta_ctx* ctx, kamsta_graph_desc* graphs, uint32_t count,
+                                    const kamsta_cfg* cfg, kamsta_tuning* out,
+                                    kamsta_stream stream) {
+  if (!ctx || !out || (count && !graphs)) {
+    set_error("null pointer argument");
+    return KAMSTA_E_INPUT;
+  }
+  kamsta_status s = check_cfg(cfg);
+  if (s != KAMSTA_OK) return s;
+  kamsta_cfg c = cfg_or_default(cfg);
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  const Algo algo = (c.flags & KAMSTA_FLAG_FILTER) ? Algo::kFilterBoruvka : Algo::kBoruvka;
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  return batch_autotune(ctx, algo, graphs, count, c, st, out);
+}
+
+kamsta_status kamsta_ctx_set_tuning(kamsta_ctx* ctx, const kamsta_tuning* t) {
+  if (!ctx) {
+    set_error("null context");
+    return KAMSTA_E_INPUT;
+  }
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  if (t && t->small_threads && t->small_threads != 256 && t->small_threads != 512 &&
+      t->small_threads != 1024) {
+    set_error("tuning: small_threads must be 256, 512 or 1024");
+    return KAMSTA_E_INPUT;
+  }
+  ctx->tune_small_threads = t ? t->small_threads : 0;
+  ctx->tune_small_max_n = t ? t->small_max_n : 0;
+  return KAMSTA_OK;
 }
 
 kamsta_status kamsta_mst_batch(kamsta_ctx* ctx, kamsta_graph_desc* graphs, uint32_t count,

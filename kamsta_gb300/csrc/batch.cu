@@ -11,13 +11,14 @@
 //                    voff to src/dst (u32 words, coalesced); an id >= n_g is
 //                    replaced by an id the solver skips and flags graph g
 //   k_batch_order    (KAMSTA_FLAG_VALIDATE) per-graph (src,dst) order check
-//   solve_device     the single-graph solver over the union
-//   k_batch_keys     forest edges -> 64-bit (min, max) keys + weights
-//   radix sort       by (min, max): groups the forest by graph (voff is
-//                    monotone) and orders each graph's edges by (src, dst)
-//   k_batch_bounds   first forest entry of every graph (binary search)
-//   k_batch_scatter  un-shift and write to each graph's output; per-graph
-//                    weight sums
+//   solve_device     the single-graph solver over the union; the forest comes
+//                    back as one bit per union entry (its src<dst copy)
+//   k_batch_popc + scan  rank of every set bit
+//   k_batch_bounds   first rank of every graph
+//   k_batch_scatter  each forest edge, un-shifted, to its graph's output at
+//                    its rank: input order, i.e. sorted by (src, dst); per-
+//                    graph weight sums
+// Small graphs skip the union (k_small_batch, one CTA per graph).
 // The reference has no batch API: its benchmark solves one graph per MPI
 // job (benchmarks/mst.cpp:215-228); the result of each graph here equals a
 // kamsta_mst_boruvka call on that graph alone, sorted by (src, dst).
@@ -28,6 +29,7 @@
 
 #include "sort_gen.cuh"
 #include "solver.cuh"
+#include "small_solve.cuh"
 #include "batch.cuh"
 
 namespace kamsta {
@@ -116,73 +118,81 @@ __global__ void __launch_bounds__(kBatchBlock)
   }
 }
 
-__global__ void k_batch_keys(const kamsta_wedge* __restrict__ f, uint64_t K, uint32_t b,
-                             uint64_t* __restrict__ keys, uint32_t* __restrict__ w) {
-  for (uint64_t j = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; j < K;
-       j += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
-    const kamsta_wedge e = f[j];
-    const uint32_t lo = min(e.src, e.dst), hi = max(e.src, e.dst);
-    keys[j] = (static_cast<uint64_t>(lo) << b) | hi;
-    w[j] = e.w;
-  }
+__global__ void k_batch_popc(const uint32_t* __restrict__ bits, uint64_t W,
+                             uint32_t* __restrict__ pc) {
+  for (uint64_t q = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; q < W;
+       q += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+    pc[q] = __popc(bits[q]);
 }
 
-// begin[g] = first sorted key whose min id is >= voff[g]
-__global__ void k_batch_bounds(WaveTable t, const uint64_t* __restrict__ keys, uint64_t K,
-                               uint32_t b) {
+// begin[g] = forest edges of the graphs before g: set bits before eoff[g]
+__global__ void k_batch_bounds(WaveTable t, const uint32_t* __restrict__ bits,
+                               const uint32_t* __restrict__ pre) {
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g > t.G) return;
-  const uint64_t x = t.voff[g] << b;
-  uint64_t lo = 0, hi = K;
-  while (lo < hi) {
-    const uint64_t mid = (lo + hi) >> 1;
-    if (keys[mid] < x) lo = mid + 1; else hi = mid;
-  }
-  t.begin[g] = lo;
+  const uint64_t e = t.eoff[g];
+  const uint32_t low = static_cast<uint32_t>(e & 31);
+  t.begin[g] = pre[e >> 5] + (low ? __popc(bits[e >> 5] & ((1u << low) - 1)) : 0u);
 }
 
+// One thread per bitmap word: each set bit is a forest edge (the union entry
+// at that position); it goes, un-shifted, to its graph's output at its rank
+// minus the graph's first rank, so every graph's forest is in input order,
+// i.e. sorted by (src, dst).  Weights are summed per graph (one atomic per
+// warp when the warp's edges share a graph).
 __global__ void __launch_bounds__(kBatchBlock)
-    k_batch_scatter(WaveTable t, const uint64_t* __restrict__ keys,
-                    const uint32_t* __restrict__ w, uint64_t K, uint32_t b) {
-  const uint64_t mask = (1ull << b) - 1;
+    k_batch_scatter(WaveTable t, const uint32_t* __restrict__ uni,
+                    const uint32_t* __restrict__ bits, const uint32_t* __restrict__ pre,
+                    uint64_t W) {
   const uint32_t lane = threadIdx.x & 31;
-  for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x);
-       base < K; base += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
-    const uint64_t j = base + threadIdx.x;
-    const bool live = j < K;
-    uint32_t g = 0;
-    uint64_t wt = 0;
-    if (live) {
-      const uint64_t key = keys[j];
-      const uint64_t lo = key >> b, hi = key & mask;
-      g = upper_graph(t.voff, t.G, lo);
-      const uint64_t v = t.voff[g];
-      uint32_t* o = t.out[g] + 3 * (j - t.begin[g]);
-      o[0] = static_cast<uint32_t>(lo - v);
-      o[1] = static_cast<uint32_t>(hi - v);
-      o[2] = w[j];
-      wt = w[j];
+  for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x); base < W;
+       base += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    const uint64_t q = base + threadIdx.x;
+    uint32_t f = q < W ? bits[q] : 0u;
+    uint32_t g0 = 0xffffffffu;
+    uint64_t w0 = 0;
+    if (f) {
+      uint32_t rank = pre[q];
+      uint64_t pos = q * 32 + (__ffs(f) - 1);
+      uint32_t g = upper_graph(t.eoff, t.G, pos);
+      g0 = g;
+      while (f) {
+        const uint32_t b = __ffs(f) - 1;
+        f &= f - 1;
+        pos = q * 32 + b;
+        while (pos >= t.eoff[g + 1]) ++g;
+        const uint32_t* e = uni + 3 * pos;
+        const uint32_t v = static_cast<uint32_t>(t.voff[g]);
+        const uint32_t wt = e[2];
+        uint32_t* o = t.out[g] + 3 * (rank - t.begin[g]);
+        o[0] = e[0] - v;
+        o[1] = e[1] - v;
+        o[2] = wt;
+        ++rank;
+        if (g == g0) {
+          w0 += wt;
+        } else {
+          atomicAdd(reinterpret_cast<unsigned long long*>(&t.weight[g]),
+                    static_cast<unsigned long long>(wt));
+        }
+      }
     }
-    // one atomic per warp when the warp's live entries share a graph
-    const uint32_t live_mask = __ballot_sync(kFull, live);
-    const uint32_t leader = __ffs(live_mask) - 1;
-    const uint32_t g0 = __shfl_sync(kFull, g, leader);
-    if (__all_sync(kFull, !live || g == g0)) {
-      const uint64_t s = warp_sum(wt);
-      if (lane == leader) atomicAdd(reinterpret_cast<unsigned long long*>(&t.weight[g0]),
-                                    static_cast<unsigned long long>(s));
-    } else if (live) {
-      atomicAdd(reinterpret_cast<unsigned long long*>(&t.weight[g]),
-                static_cast<unsigned long long>(wt));
+    // the first graph's sum: one atomic per warp when the warp agrees
+    const uint32_t have = __ballot_sync(kFull, g0 != 0xffffffffu);
+    if (!have) continue;
+    const uint32_t leader = __ffs(have) - 1;
+    const uint32_t gl = __shfl_sync(kFull, g0, leader);
+    if (__all_sync(kFull, g0 == 0xffffffffu || g0 == gl)) {
+      const uint64_t sum = warp_sum(w0);
+      if (lane == leader) atomicAdd(reinterpret_cast<unsigned long long*>(&t.weight[gl]),
+                                    static_cast<unsigned long long>(sum));
+    } else if (g0 != 0xffffffffu) {
+      atomicAdd(reinterpret_cast<unsigned long long*>(&t.weight[g0]),
+                static_cast<unsigned long long>(w0));
     }
   }
 }
 
-inline uint32_t bits_for(uint64_t x) {  // bits to hold values < x (x >= 1)
-  uint32_t b = 1;
-  while (b < 64 && (1ull << b) < x) ++b;
-  return b;
-}
 
 inline size_t up256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -242,9 +252,135 @@ std::vector<std::pair<uint32_t, uint32_t>> plan_waves(const kamsta_graph_desc* g
   return waves;
 }
 
-kamsta_status solve_wave(kamsta_ctx* ctx, Algo algo, kamsta_graph_desc* g, uint32_t G,
-                         const kamsta_cfg& cfg, bool host_buffers, cudaStream_t st,
-                         BatchWaveStats* ws) {
+namespace {
+
+// ---------------------------------------------------------------------------
+// Small graphs (n <= 32768, m_directed <= 262144): one persistent launch.
+// Each CTA takes the next graph from a work queue (largest first) and solves
+// it entirely on its own (small_solve.cuh) in its own scratch slot; the
+// forest comes out sorted by (src, dst), like the union path's.
+
+// CTA sizes the persistent kernel is built for; the context's tuning picks
+// one (kamsta_batch_autotune), 512 by default.
+constexpr int kSmallThreadsDefault = 512;
+
+struct SmallTable {
+  const uint32_t* const* edges;
+  uint32_t* const* out;
+  const uint32_t* md;
+  const uint32_t* n;
+  const uint32_t* order;  // graph indices, largest first
+  small::Result* res;
+  uint32_t G;
+  uint32_t check_order;
+};
+
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS)
+    k_small_batch(SmallTable t, unsigned char* __restrict__ scratch, uint32_t* queue) {
+  __shared__ uint32_t s_q;
+  unsigned char* mine = scratch + static_cast<size_t>(blockIdx.x) * small::kScratchBytes;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_q = atomicAdd(queue, 1u);
+    __syncthreads();
+    const uint32_t q = s_q;
+    if (q >= t.G) return;
+    const uint32_t g = t.order[q];
+    small::solve<THREADS, small::Out::kSorted>(t.edges[g], t.md[g], t.n[g], mine, t.out[g],
+                                                      &t.res[g], true, t.check_order != 0);
+  }
+}
+
+uint32_t small_max_n(const kamsta_ctx* ctx) {
+  return ctx->tune_small_max_n ? std::min<uint32_t>(ctx->tune_small_max_n, small::kMaxN)
+                               : small::kMaxN;
+}
+
+bool is_small(const kamsta_ctx* ctx, const kamsta_graph_desc& g) {
+  return g.n <= small_max_n(ctx) && g.m_directed <= small::kMaxMd;
+}
+
+template <int THREADS>
+cudaError_t launch_small_kernel(const SmallTable& t, unsigned char* scratch, uint32_t* queue,
+                                uint32_t grid, cudaStream_t st) {
+  k_small_batch<THREADS><<<grid, THREADS, 0, st>>>(t, scratch, queue);
+  return cudaGetLastError();
+}
+
+int small_per_sm(int threads) {
+  int per_sm = 1;
+  if (threads == 256)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_small_batch<256>, 256, 0);
+  else if (threads == 1024)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_small_batch<1024>, 1024, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_small_batch<512>, 512, 0);
+  return std::max(per_sm, 1);
+}
+
+// Launches the small graphs on `st` and returns; `res` (host) is valid after
+// the stream synchronises.  Device buffers stay alive in `keep`.
+kamsta_status launch_small(kamsta_ctx* ctx, kamsta_graph_desc* g, const std::vector<uint32_t>& idx,
+                           const kamsta_cfg& cfg, cudaStream_t st, PoolBuf* tab, PoolBuf* scr,
+                           small::Result** d_res, uint32_t* launches) {
+  const uint32_t S = static_cast<uint32_t>(idx.size());
+  std::vector<uint32_t> order(S);
+  for (uint32_t i = 0; i < S; ++i) order[i] = i;
+  std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+    return g[idx[a]].m_directed + g[idx[a]].n > g[idx[b]].m_directed + g[idx[b]].n;
+  });
+  const size_t o_edges = 0;
+  const size_t o_out = o_edges + up256(sizeof(void*) * S);
+  const size_t o_md = o_out + up256(sizeof(void*) * S);
+  const size_t o_n = o_md + up256(sizeof(uint32_t) * S);
+  const size_t o_order = o_n + up256(sizeof(uint32_t) * S);
+  const size_t o_res = o_order + up256(sizeof(uint32_t) * S);
+  const size_t o_queue = o_res + up256(sizeof(small::Result) * S);
+  const size_t bytes = o_queue + 256;
+  std::vector<unsigned char> h(bytes, 0);
+  for (uint32_t i = 0; i < S; ++i) {
+    const kamsta_graph_desc& d = g[idx[i]];
+    reinterpret_cast<const void**>(h.data() + o_edges)[i] = d.edges;
+    reinterpret_cast<void**>(h.data() + o_out)[i] = d.out;
+    reinterpret_cast<uint32_t*>(h.data() + o_md)[i] = static_cast<uint32_t>(d.m_directed);
+    reinterpret_cast<uint32_t*>(h.data() + o_n)[i] = d.n;
+  }
+  std::memcpy(h.data() + o_order, order.data(), sizeof(uint32_t) * S);
+  B_TRY(tab->alloc(ctx, bytes, st));
+  unsigned char* d = static_cast<unsigned char*>(tab->p);
+  B_TRY(cudaMemcpyAsync(d, h.data(), bytes, cudaMemcpyHostToDevice, st));
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int threads = ctx->tune_small_threads ? static_cast<int>(ctx->tune_small_threads)
+                                              : kSmallThreadsDefault;
+  const uint32_t grid = std::max<uint32_t>(
+      1, std::min<uint32_t>(S, static_cast<uint32_t>(small_per_sm(threads) * sms)));
+  B_TRY(scr->alloc(ctx, static_cast<size_t>(grid) * small::kScratchBytes, st));
+  SmallTable t;
+  t.edges = reinterpret_cast<const uint32_t* const*>(d + o_edges);
+  t.out = reinterpret_cast<uint32_t* const*>(d + o_out);
+  t.md = reinterpret_cast<const uint32_t*>(d + o_md);
+  t.n = reinterpret_cast<const uint32_t*>(d + o_n);
+  t.order = reinterpret_cast<const uint32_t*>(d + o_order);
+  t.res = reinterpret_cast<small::Result*>(d + o_res);
+  t.G = S;
+  t.check_order = (cfg.flags & KAMSTA_FLAG_VALIDATE) ? 1u : 0u;
+  unsigned char* scratch = static_cast<unsigned char*>(scr->p);
+  uint32_t* queue = reinterpret_cast<uint32_t*>(d + o_queue);
+  if (threads == 256) B_TRY(launch_small_kernel<256>(t, scratch, queue, grid, st));
+  else if (threads == 1024) B_TRY(launch_small_kernel<1024>(t, scratch, queue, grid, st));
+  else B_TRY(launch_small_kernel<512>(t, scratch, queue, grid, st));
+  *d_res = t.res;
+  ++*launches;
+  return KAMSTA_OK;
+}
+
+// The union path for the graphs g[0..G).
+kamsta_status solve_union(kamsta_ctx* ctx, Algo algo, kamsta_graph_desc* g, uint32_t G,
+                          const kamsta_cfg& cfg, bool host_buffers, cudaStream_t st,
+                          BatchWaveStats* ws) {
   // ---- host side of the wave table
   std::vector<uint64_t> eoff(G + 1, 0), voff(G + 1, 0);
   for (uint32_t i = 0; i < G; ++i) {
@@ -269,7 +405,7 @@ kamsta_status solve_wave(kamsta_ctx* ctx, Algo algo, kamsta_graph_desc* g, uint3
   const size_t o_err = o_weight + up256(sizeof(uint64_t) * G);
   const size_t tbytes = o_err + up256(sizeof(uint32_t) * G);
   std::vector<unsigned char> h(tbytes, 0);
-  PoolBuf tbuf, ubuf, fbuf, obuf;
+  PoolBuf tbuf, ubuf, obuf;
   B_TRY(tbuf.alloc(ctx, tbytes, st));
   B_TRY(ubuf.alloc(ctx, std::max<uint64_t>(M, 1) * sizeof(kamsta_wedge), st));
   kamsta_wedge* uni = static_cast<kamsta_wedge*>(ubuf.p);
@@ -337,53 +473,41 @@ kamsta_status solve_wave(kamsta_ctx* ctx, Algo algo, kamsta_graph_desc* g, uint3
   // ---- one solve over the union (validation already done per graph)
   kamsta_cfg ucfg = cfg;
   ucfg.flags &= ~(KAMSTA_FLAG_VALIDATE | KAMSTA_FLAG_SORT_OUTPUT);
-  B_TRY(fbuf.alloc(ctx, std::max<uint64_t>(N, 1) * sizeof(kamsta_wedge), st));
-  kamsta_wedge* forest = static_cast<kamsta_wedge*>(fbuf.p);
+  // the forest comes back as one bit per union entry (its src<dst copy)
+  const uint64_t W = (M + 31) / 32;
+  PoolBuf bb, pcb, preb, stb;
+  B_TRY(bb.alloc(ctx, sizeof(uint32_t) * (W + 1), st));
+  uint32_t* bits = static_cast<uint32_t*>(bb.p);
+  B_TRY(cudaMemsetAsync(bits, 0, sizeof(uint32_t) * (W + 1), st));
   SolveOut so;
   kamsta_stats sst;
-  B_KTRY(solve_device(ctx, algo, uni, M, static_cast<uint32_t>(N), ucfg, forest, &so, &sst, st));
+  B_KTRY(solve_device(ctx, algo, uni, M, static_cast<uint32_t>(N), ucfg, nullptr, &so, &sst, st,
+                      bits));
   launches += sst.gpu_launches;
   ws->solve_ms = sst.device_ms;
-  ubuf.reset();  // the union input is no longer needed
-  // ---- split the forest per graph
-  const uint64_t K = so.count;
-  const uint32_t b = bits_for(std::max<uint64_t>(N, 2));
-  PoolBuf kb, vb, cb, sb;
-  uint64_t *keys = nullptr, *keys2 = nullptr;
-  uint32_t *w = nullptr, *w2 = nullptr;
-  if (K) {
-    const RadixScratch rs = radix_scratch_bytes(K);
-    const size_t kbytes = up256(sizeof(uint64_t) * K);
-    const size_t vbytes = up256(sizeof(uint32_t) * K);
-    B_TRY(kb.alloc(ctx, 2 * kbytes, st));
-    B_TRY(vb.alloc(ctx, 2 * vbytes, st));
-    B_TRY(cb.alloc(ctx, sizeof(uint32_t) * rs.counts + 256, st));
-    B_TRY(sb.alloc(ctx, sizeof(uint64_t) * rs.status + 256, st));
-    keys = static_cast<uint64_t*>(kb.p);
-    keys2 = reinterpret_cast<uint64_t*>(static_cast<char*>(kb.p) + kbytes);
-    w = static_cast<uint32_t*>(vb.p);
-    w2 = reinterpret_cast<uint32_t*>(static_cast<char*>(vb.p) + vbytes);
+  // ---- split: ranks of the set bits (word popcounts + exclusive scan), the
+  // first rank of every graph, then every forest edge to its graph's output
+  B_TRY(pcb.alloc(ctx, sizeof(uint32_t) * (W + 1), st));
+  B_TRY(preb.alloc(ctx, sizeof(uint32_t) * (W + 1), st));
+  B_TRY(stb.alloc(ctx, sizeof(uint64_t) * ((W + 1) / 2048 + 2), st));
+  uint32_t* pc = static_cast<uint32_t*>(pcb.p);
+  uint32_t* pre = static_cast<uint32_t*>(preb.p);
+  {
     const uint32_t blocks = static_cast<uint32_t>(
-        std::min<uint64_t>((K + kBatchBlock - 1) / kBatchBlock, sms * 8ull));
-    k_batch_keys<<<blocks, kBatchBlock, 0, st>>>(forest, K, b, keys, w);
-    ++launches;
-    int alt = 0;
-    uint32_t* ticket = &ctx->d_counters[kCMisc].ticket;
-    B_TRY(radix_sort_pairs_u32(st, keys, keys2, w, w2, K, 2 * b, static_cast<uint32_t*>(cb.p),
-                               static_cast<uint64_t*>(sb.p), ticket, ctx->d_err, &alt, sms));
-    launches += 3 * ((2 * b + 7) / 8);
-    if (alt) {
-      std::swap(keys, keys2);
-      std::swap(w, w2);
-    }
+        std::min<uint64_t>((W + 1 + kBatchBlock - 1) / kBatchBlock, sms * 8ull));
+    k_batch_popc<<<blocks, kBatchBlock, 0, st>>>(bits, W + 1, pc);
+    B_TRY(exclusive_scan_u32(st, pc, pre, W + 1, static_cast<uint64_t*>(stb.p),
+                             &ctx->d_counters[kCMisc].ticket, ctx->d_err, sms));
+    launches += 2;
   }
   B_TRY(cudaMemsetAsync(d + o_weight, 0, sizeof(uint64_t) * G, st));
-  k_batch_bounds<<<(G + 1 + kBatchBlock - 1) / kBatchBlock, kBatchBlock, 0, st>>>(t, keys, K, b);
+  k_batch_bounds<<<(G + 1 + kBatchBlock - 1) / kBatchBlock, kBatchBlock, 0, st>>>(t, bits, pre);
   ++launches;
-  if (K) {
+  if (so.count) {
     const uint32_t blocks = static_cast<uint32_t>(
-        std::min<uint64_t>((K + kBatchBlock - 1) / kBatchBlock, sms * 8ull));
-    k_batch_scatter<<<blocks, kBatchBlock, 0, st>>>(t, keys, w, K, b);
+        std::min<uint64_t>((W + kBatchBlock - 1) / kBatchBlock, sms * 16ull));
+    k_batch_scatter<<<blocks, kBatchBlock, 0, st>>>(t, reinterpret_cast<const uint32_t*>(uni),
+                                                    bits, pre, W);
     ++launches;
   }
   B_TRY(cudaGetLastError());
@@ -395,7 +519,7 @@ kamsta_status solve_wave(kamsta_ctx* ctx, Algo algo, kamsta_graph_desc* g, uint3
   B_TRY(cudaStreamSynchronize(st));
   derr = *ctx->h_err;
   if (derr) {
-    set_error("batch: device wait cap reached in the forest sort");
+    set_error("batch: device wait cap reached in the forest split");
     return KAMSTA_E_NOCONVERGE;
   }
   const uint64_t* hb = reinterpret_cast<const uint64_t*>(back.data());
@@ -418,6 +542,118 @@ kamsta_status solve_wave(kamsta_ctx* ctx, Algo algo, kamsta_graph_desc* g, uint3
   }
   if (host_buffers) B_TRY(cudaStreamSynchronize(st));
   ws->launches = launches;
+  return KAMSTA_OK;
+}
+
+}  // namespace
+
+bool is_small_graph(const kamsta_ctx* ctx, const kamsta_graph_desc& g) { return is_small(ctx, g); }
+
+kamsta_status solve_wave(kamsta_ctx* ctx, Algo algo, kamsta_graph_desc* g, uint32_t G,
+                         const kamsta_cfg& cfg, bool host_buffers, cudaStream_t st,
+                         BatchWaveStats* ws) {
+  std::vector<uint32_t> sm, lg;
+  for (uint32_t i = 0; i < G; ++i)
+    ((!host_buffers && is_small(ctx, g[i])) ? sm : lg).push_back(i);
+  if (sm.empty()) return solve_union(ctx, algo, g, G, cfg, host_buffers, st, ws);
+  // small graphs on the auxiliary stream, overlapping the union solve (the
+  // forest is the same for boruvka and filter_boruvka)
+  B_TRY(cudaEventRecord(ctx->ev_fork, st));
+  B_TRY(cudaStreamWaitEvent(ctx->aux, ctx->ev_fork, 0));
+  PoolBuf tab, scr;
+  small::Result* d_res = nullptr;
+  uint32_t launches = 0;
+  B_KTRY(launch_small(ctx, g, sm, cfg, ctx->aux, &tab, &scr, &d_res, &launches));
+  std::vector<small::Result> h_res(sm.size());
+  B_TRY(cudaMemcpyAsync(h_res.data(), d_res, sizeof(small::Result) * sm.size(),
+                        cudaMemcpyDeviceToHost, ctx->aux));
+  BatchWaveStats us;
+  kamsta_status s = KAMSTA_OK;
+  if (!lg.empty()) {
+    std::vector<kamsta_graph_desc> sub(lg.size());
+    for (size_t k = 0; k < lg.size(); ++k) sub[k] = g[lg[k]];
+    s = solve_union(ctx, algo, sub.data(), static_cast<uint32_t>(lg.size()), cfg, host_buffers,
+                    st, &us);
+    for (size_t k = 0; k < lg.size(); ++k) g[lg[k]] = sub[k];
+  }
+  B_TRY(cudaEventRecord(ctx->ev_join, ctx->aux));
+  B_TRY(cudaStreamWaitEvent(st, ctx->ev_join, 0));
+  B_TRY(cudaStreamSynchronize(ctx->aux));
+  if (s != KAMSTA_OK) return s;
+  uint64_t entries = 0, verts = 0;
+  for (size_t k = 0; k < sm.size(); ++k) {
+    kamsta_graph_desc& d = g[sm[k]];
+    const small::Result& r = h_res[k];
+    entries += d.m_directed;
+    verts += d.n;
+    if (r.err) {
+      d.status = (r.err & ~(kErrRange | kErrOrder)) ? KAMSTA_E_NOCONVERGE : KAMSTA_E_INPUT;
+      d.out_count = 0;
+      d.total_weight = 0;
+    } else {
+      d.status = KAMSTA_OK;
+      d.out_count = r.count;
+      d.total_weight = r.weight;
+    }
+  }
+  ws->entries = us.entries + entries;
+  ws->vertices = us.vertices + verts;
+  ws->launches = us.launches + launches;
+  ws->solve_ms = us.solve_ms;
+  return KAMSTA_OK;
+}
+
+// Autotuner of the batch path: times the persistent small-graph kernel at
+// each CTA size on the sample's small graphs, then the small/union cutoff on
+// the whole sample, and keeps the fastest in the context.
+kamsta_status batch_autotune(kamsta_ctx* ctx, Algo algo, kamsta_graph_desc* g, uint32_t count,
+                             const kamsta_cfg& cfg, cudaStream_t st, kamsta_tuning* out) {
+  static const uint32_t kThreads[3] = {256, 512, 1024};
+  static const uint32_t kCut[4] = {4096, 8192, 16384, 32768};
+  std::memset(out, 0, sizeof(*out));
+  auto timed = [&](kamsta_graph_desc* gg, uint32_t cnt, double* ms) -> kamsta_status {
+    double best = 1e300;
+    for (int rep = 0; rep < 3; ++rep) {  // the first run warms the pool
+      const auto t0 = std::chrono::steady_clock::now();
+      kamsta_status s = solve_batch(ctx, algo, gg, cnt, cfg, 0, false, nullptr, st);
+      if (s != KAMSTA_OK) return s;
+      const double t = std::chrono::duration<double, std::milli>(
+                           std::chrono::steady_clock::now() - t0).count();
+      if (rep > 0) best = std::min(best, t);
+    }
+    *ms = best;
+    return KAMSTA_OK;
+  };
+  std::vector<kamsta_graph_desc> smalls;
+  for (uint32_t i = 0; i < count; ++i)
+    if (g[i].n <= small::kMaxN && g[i].m_directed <= small::kMaxMd) smalls.push_back(g[i]);
+  ctx->tune_small_max_n = small::kMaxN;
+  uint32_t best_t = kSmallThreadsDefault;
+  double best_ms = 1e300;
+  if (!smalls.empty()) {
+    for (int i = 0; i < 3; ++i) {
+      ctx->tune_small_threads = kThreads[i];
+      B_KTRY(timed(smalls.data(), static_cast<uint32_t>(smalls.size()), &out->threads_ms[i]));
+      if (out->threads_ms[i] < best_ms) {
+        best_ms = out->threads_ms[i];
+        best_t = kThreads[i];
+      }
+    }
+  }
+  ctx->tune_small_threads = best_t;
+  uint32_t best_c = small::kMaxN;
+  best_ms = 1e300;
+  for (int i = 0; i < 4; ++i) {
+    ctx->tune_small_max_n = kCut[i];
+    B_KTRY(timed(g, count, &out->cutoff_ms[i]));
+    if (out->cutoff_ms[i] < best_ms) {
+      best_ms = out->cutoff_ms[i];
+      best_c = kCut[i];
+    }
+  }
+  ctx->tune_small_max_n = best_c;
+  out->small_threads = best_t;
+  out->small_max_n = best_c;
   return KAMSTA_OK;
 }
 

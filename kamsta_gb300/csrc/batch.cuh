@@ -20,6 +20,10 @@ struct BatchWaveStats {
   double solve_ms = 0;
 };
 
+// Graphs the persistent single-CTA path takes (n <= 32768, m_directed <=
+// 262144).
+bool is_small_graph(const kamsta_ctx* ctx, const kamsta_graph_desc& g);
+
 // Device bytes a graph adds to a wave at its peak (input copy, edge lists,
 // forest sort, vertex arrays); used for wave planning and serving admission.
 uint64_t batch_graph_bytes(uint64_t m_directed, uint32_t n);
@@ -29,9 +33,12 @@ uint64_t batch_graph_bytes(uint64_t m_directed, uint32_t n);
 std::vector<std::pair<uint32_t, uint32_t>> plan_waves(const kamsta_graph_desc* g, uint32_t count,
                                                       uint64_t budget);
 
-// One wave: the disjoint union of g[0..G) solved as one graph, the forest
-// split back per graph (sorted by (src, dst)).  host_buffers: edges/out are
-// host pointers.
+// One wave.  Small graphs (n <= 32768, m_directed <= 262144; device
+// buffers only) go to one persistent launch on the context's auxiliary
+// stream, one CTA per graph from a work queue; the others are solved as
+// their disjoint union on `st`, the forest split back per graph.  Either
+// way each forest is sorted by (src, dst).  host_buffers: edges/out are host
+// pointers.
 kamsta_status solve_wave(kamsta_ctx* ctx, Algo algo, kamsta_graph_desc* g, uint32_t G,
                          const kamsta_cfg& cfg, bool host_buffers, cudaStream_t st,
                          BatchWaveStats* ws);
@@ -39,5 +46,8 @@ kamsta_status solve_wave(kamsta_ctx* ctx, Algo algo, kamsta_graph_desc* g, uint3
 kamsta_status solve_batch(kamsta_ctx* ctx, Algo algo, kamsta_graph_desc* g, uint32_t count,
                           const kamsta_cfg& cfg, uint64_t budget, bool host_buffers,
                           kamsta_batch_stats* st, cudaStream_t stream);
+
+kamsta_status batch_autotune(kamsta_ctx* ctx, Algo algo, kamsta_graph_desc* g, uint32_t count,
+                             const kamsta_cfg& cfg, cudaStream_t st, kamsta_tuning* out);
 
 }  // namespace kamsta

@@ -1,0 +1,238 @@
+// codec.cu -- 7-bit varint difference encoding of the directed input
+// (Compression::SEVEN_BIT_DIFF_ENCODING, algorithm_configurations.hpp:18-25).
+//
+// Per edge the reference stores varint(src - prev_src), varint(dst),
+// varint(w) (DifferenceEncodedGraph::encode_edges,
+// difference_encoded_graph.hpp:175-205) with its 7-bit little-endian
+// varint, continuation bit 0x80 (encode_value / decode_value,
+// variable_length_encoding.hpp:6-167); the edge list is cut into chunks, each
+// starting with a raw first edge and a byte offset.  The byte stream of a
+// chunk here is exactly that; chunks are small (<= 4096 edges) so that the
+// device decodes one chunk per CTA:
+//   1. the chunk's bytes go to shared memory;
+//   2. a block scan over "last byte of a value" flags gives every byte its
+//      value index; the thread holding a value's last byte assembles it;
+//   3. a block scan over the src deltas restores src; edges are written out.
+// The host encoder runs on all host cores.  A decoded input feeds the normal
+// solver, so a compressed graph costs about half the bytes to keep resident
+// or to copy to the device.
+#include <algorithm>
+#include <atomic>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+#include "codec.cuh"
+#include "common.cuh"
+#include "solver.cuh"
+
+namespace kamsta {
+
+namespace {
+
+constexpr uint32_t kMaxChunkEdges = 4096;
+constexpr int kDecBlock = 256;
+
+inline uint32_t varint_len(uint64_t v) {
+  uint32_t n = 1;
+  while (v >= 128) {
+    v >>= 7;
+    ++n;
+  }
+  return n;
+}
+
+inline uint8_t* varint_put(uint64_t v, uint8_t* o) {
+  while (v >= 128) {
+    *o++ = static_cast<uint8_t>((v & 0x7f) | 0x80);
+    v >>= 7;
+  }
+  *o++ = static_cast<uint8_t>(v);
+  return o;
+}
+
+// Block-wide exclusive scan of one u32 per thread; returns the total.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* excl, uint32_t* s_warp) {
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(kFull, incl, o);
+    if (lane >= static_cast<uint32_t>(o)) incl += y;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t wv = lane < kDecBlock / 32 ? s_warp[lane] : 0u;
+    uint32_t wi = wv;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, wi, o);
+      if (lane >= static_cast<uint32_t>(o)) wi += y;
+    }
+    if (lane < kDecBlock / 32) s_warp[lane] = wi - wv;
+    if (lane == kDecBlock / 32 - 1) s_warp[kDecBlock / 32] = wi;
+  }
+  __syncthreads();
+  *excl = s_warp[warp] + incl - v;
+  const uint32_t total = s_warp[kDecBlock / 32];
+  __syncthreads();
+  return total;
+}
+
+__global__ void __launch_bounds__(kDecBlock)
+    k_decode_7bit(const uint64_t* __restrict__ chunk_off, const kamsta_wedge* __restrict__ first,
+                  const uint8_t* __restrict__ data, uint64_t m, uint32_t C, uint64_t nchunks,
+                  uint32_t* __restrict__ out, uint32_t* err) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint32_t* vals = reinterpret_cast<uint32_t*>(smem);          // 3 * C values
+  uint8_t* bytes = smem + sizeof(uint32_t) * 3 * C;             // <= 15 * C bytes
+  __shared__ uint32_t s_warp[kDecBlock / 32 + 1];
+  for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const uint64_t e0 = c * C;
+    const uint32_t ce = static_cast<uint32_t>(m - e0 < C ? m - e0 : C);  // edges in chunk
+    const uint64_t b0 = chunk_off[c];
+    const uint32_t nb = static_cast<uint32_t>(chunk_off[c + 1] - b0);
+    const uint32_t nv = 3 * (ce - 1);
+    if (nb > 15u * C) {  // cannot come from sorted 32-bit input
+      if (threadIdx.x == 0) atomicOr(err, kErrRange);
+      continue;
+    }
+    for (uint32_t i = threadIdx.x; i < nb; i += kDecBlock) bytes[i] = data[b0 + i];
+    __syncthreads();
+    // value index of every byte: terminators (no continuation bit) before it
+    const uint32_t per = (nb + kDecBlock - 1) / kDecBlock;
+    const uint32_t lo = threadIdx.x * per, hi = min(nb, lo + per);
+    uint32_t cnt = 0;
+    for (uint32_t i = lo; i < hi; ++i) cnt += (bytes[i] & 0x80) ? 0u : 1u;
+    uint32_t vbase = 0;
+    const uint32_t total = block_excl_scan(cnt, &vbase, s_warp);
+    if (total != nv) {
+      if (threadIdx.x == 0) atomicOr(err, kErrRange);
+      continue;
+    }
+    uint32_t v = vbase;
+    for (uint32_t i = lo; i < hi; ++i) {
+      if (bytes[i] & 0x80) continue;
+      uint32_t s = i;  // first byte of the value
+      while (s > 0 && (bytes[s - 1] & 0x80) && i - s < 9) --s;
+      uint64_t x = 0;
+      for (uint32_t k = s; k <= i; ++k) x |= static_cast<uint64_t>(bytes[k] & 0x7f) << (7 * (k - s));
+      vals[v++] = static_cast<uint32_t>(x);  // ids and weights are 32-bit: arithmetic mod 2^32
+    }
+    __syncthreads();
+    // src = first src + running sum of the deltas; thread t owns edges
+    // [1 + t*pe, 1 + (t+1)*pe)
+    const uint32_t pe = (ce - 1 + kDecBlock - 1) / kDecBlock;
+    const uint32_t a = 1 + threadIdx.x * pe, z = min(ce, a + pe);
+    uint32_t dsum = 0;
+    for (uint32_t e = a; e < z; ++e) dsum += vals[3 * (e - 1)];
+    uint32_t dpre = 0;
+    block_excl_scan(dsum, &dpre, s_warp);
+    const kamsta_wedge f = first[c];
+    uint32_t src = f.src + dpre;
+    if (threadIdx.x == 0) {
+      out[3 * e0] = f.src;
+      out[3 * e0 + 1] = f.dst;
+      out[3 * e0 + 2] = f.w;
+    }
+    for (uint32_t e = a; e < z; ++e) {
+      src += vals[3 * (e - 1)];
+      const uint64_t o = 3 * (e0 + e);
+      out[o] = src;
+      out[o + 1] = vals[3 * (e - 1) + 1];
+      out[o + 2] = vals[3 * (e - 1) + 2];
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+kamsta_status encode_7bit(const kamsta_wedge* e, uint64_t m, uint32_t C, uint64_t* off,
+                          kamsta_wedge* first, uint8_t* data, uint64_t cap, uint64_t* bytes) {
+  *bytes = 0;
+  if (C == 0 || C > kMaxChunkEdges) {
+    set_error("encode_7bit: chunk_edges must be in [1, 4096]");
+    return KAMSTA_E_INPUT;
+  }
+  const uint64_t nch = (m + C - 1) / C;
+  std::vector<uint64_t> len(nch, 0);
+  const unsigned hw = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+  auto par = [&](auto&& fn) {
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < hw; ++t)
+      th.emplace_back([&, t] {
+        for (uint64_t c = nch * t / hw; c < nch * (t + 1) / hw; ++c) fn(c);
+      });
+    for (auto& x : th) x.join();
+  };
+  std::atomic<bool> bad{false};
+  par([&](uint64_t c) {
+    uint64_t l = 0;
+    const uint64_t a = c * C, z = std::min<uint64_t>(m, a + C);
+    for (uint64_t i = a + 1; i < z; ++i) {
+      if (e[i].src < e[i - 1].src) bad = true;  // deltas must be non-negative
+      l += varint_len(static_cast<uint64_t>(e[i].src) - e[i - 1].src) + varint_len(e[i].dst) +
+           varint_len(e[i].w);
+    }
+    len[c] = l;
+  });
+  if (bad) {
+    set_error("encode_7bit: input must be sorted by src");
+    return KAMSTA_E_INPUT;
+  }
+  uint64_t total = 0;
+  for (uint64_t c = 0; c < nch; ++c) {
+    if (off) off[c] = total;
+    total += len[c];
+  }
+  if (off) off[nch] = total;
+  *bytes = total;
+  if (!data) return KAMSTA_OK;
+  if (!off || !first) {
+    set_error("encode_7bit: chunk_offset and chunk_first are required");
+    return KAMSTA_E_INPUT;
+  }
+  if (total > cap) {
+    set_error("encode_7bit: data capacity too small (required bytes in data_bytes)");
+    return KAMSTA_E_INPUT;
+  }
+  par([&](uint64_t c) {
+    const uint64_t a = c * C, z = std::min<uint64_t>(m, a + C);
+    first[c] = e[a];
+    uint8_t* o = data + off[c];
+    for (uint64_t i = a + 1; i < z; ++i) {
+      o = varint_put(static_cast<uint64_t>(e[i].src) - e[i - 1].src, o);
+      o = varint_put(e[i].dst, o);
+      o = varint_put(e[i].w, o);
+    }
+  });
+  return KAMSTA_OK;
+}
+
+kamsta_status decode_7bit(const kamsta_cgraph& g, kamsta_wedge* d_out, uint32_t* d_err,
+                          cudaStream_t st) {
+  if (g.m_directed == 0) return KAMSTA_OK;
+  if (g.chunk_edges == 0 || g.chunk_edges > kMaxChunkEdges ||
+      g.num_chunks != (g.m_directed + g.chunk_edges - 1) / g.chunk_edges) {
+    set_error("decode_7bit: inconsistent chunk layout");
+    return KAMSTA_E_INPUT;
+  }
+  const size_t smem = 27ull * g.chunk_edges + 64;
+  cudaError_t e = cudaFuncSetAttribute(k_decode_7bit, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(smem));
+  if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(k_decode_7bit)");
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const uint64_t grid = std::min<uint64_t>(g.num_chunks, uint64_t(sms) * 8);
+  k_decode_7bit<<<static_cast<uint32_t>(grid), kDecBlock, smem, st>>>(
+      g.chunk_offset, g.chunk_first, g.data, g.m_directed, g.chunk_edges, g.num_chunks,
+      reinterpret_cast<uint32_t*>(d_out), d_err);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_status(e, "k_decode_7bit");
+  return KAMSTA_OK;
+}
+
+}  // namespace kamsta

@@ -305,6 +305,12 @@ __global__ void __launch_bounds__(kBlock, 3)
       }
       cls[j] = weight_class<NOUT>(wt, p);
     }
+    {  // a tile that keeps nothing (typical of the filter passes) is done
+      bool any = false;
+#pragma unroll
+      for (int j = 0; j < kItemsDir; ++j) any |= cls[j] != 0xff;
+      if (!__syncthreads_or(any)) continue;
+    }
     seg_tile_finish<NOUT, kItemsDir>(cls, run, p, [&](uint32_t t) {
       Rec r;
       r.a = words[3 * t];
@@ -465,6 +471,12 @@ __global__ void __launch_bounds__(kBlock, 3)
       recs[t].a = la;
       recs[t].b = lb;
       cls[j] = weight_class<NOUT>(r.w, p);
+    }
+    {  // a tile that keeps nothing is done
+      bool any = false;
+#pragma unroll
+      for (int j = 0; j < kItemsRec; ++j) any |= cls[j] != 0xff;
+      if (!__syncthreads_or(any)) continue;
     }
     seg_tile_finish<NOUT, kItemsRec>(cls, run, p, [&](uint32_t t) { return recs[t]; });
   }
@@ -910,6 +922,22 @@ __global__ void k_emit(uint64_t k, const uint32_t* __restrict__ msf,
     out_words[3 * i + 1] = d;
     out_words[3 * i + 2] = w;
     local += w;
+  }
+  local = warp_sum(local);
+  if (lane_id() == 0 && local) atomicAdd(weight, static_cast<unsigned long long>(local));
+}
+
+// Forest as a bitmap over input positions (batch split): bit oid of every
+// forest edge is set, and the weights are summed.
+__global__ void k_mark_forest(uint64_t k, const uint32_t* __restrict__ msf,
+                              const uint32_t* __restrict__ in_words, uint32_t* __restrict__ bits,
+                              unsigned long long* weight) {
+  uint64_t local = 0;
+  for (uint64_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k;
+       i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    const uint32_t oid = msf[i];
+    atomicOr(&bits[oid >> 5], 1u << (oid & 31));
+    local += in_words[3ull * oid + 2];
   }
   local = warp_sum(local);
   if (lane_id() == 0 && local) atomicAdd(weight, static_cast<unsigned long long>(local));

@@ -13,6 +13,7 @@
 // The reference has no serving loop (its benchmark runs one graph per MPI
 // job, benchmarks/mst.cpp:215-228); per job the result equals the batch
 // entry point on that graph alone.
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -92,40 +93,65 @@ void kamsta_server::worker(int w) {
       ++waves;
     }
     if (!queue.empty()) cv_work.notify_one();  // more work for another worker
-    const double start = now_us();
-    descs.resize(batch.size());
-    for (size_t i = 0; i < batch.size(); ++i) {
-      descs[i] = kamsta_graph_desc{};
-      descs[i].edges = batch[i].req.d_edges;
-      descs[i].m_directed = batch[i].req.m_directed;
-      descs[i].n = batch[i].req.n;
-      descs[i].out = batch[i].req.d_out;
+    // small jobs first (one persistent launch, finished in well under a
+    // millisecond), then the rest as one union solve; each group completes
+    // as soon as it is done
+    std::stable_partition(batch.begin(), batch.end(), [ctx](const Job& j) {
+      kamsta_graph_desc d{};
+      d.m_directed = j.req.m_directed;
+      d.n = j.req.n;
+      return is_small_graph(ctx, d);
+    });
+    size_t first_large = 0;
+    while (first_large < batch.size()) {
+      kamsta_graph_desc d{};
+      d.m_directed = batch[first_large].req.m_directed;
+      d.n = batch[first_large].req.n;
+      if (!is_small_graph(ctx, d)) break;
+      ++first_large;
     }
-    BatchWaveStats ws;
-    kamsta_status s;
-    {
-      std::lock_guard<std::mutex> clk(ctx->mu);
-      s = solve_wave(ctx, algo, descs.data(), static_cast<uint32_t>(descs.size()), scfg, false,
-                     ctx->stream, &ws);
-    }
-    const double finish = now_us();
-    {
+    const size_t groups[3] = {0, first_large, batch.size()};
+    for (int grp = 0; grp < 2; ++grp) {
+      const size_t a = groups[grp], z = groups[grp + 1];
+      if (a == z) continue;
+      const double start = now_us();
+      descs.resize(z - a);
+      uint64_t gbytes = 0;
+      for (size_t i = a; i < z; ++i) {
+        kamsta_graph_desc& d = descs[i - a];
+        d = kamsta_graph_desc{};
+        d.edges = batch[i].req.d_edges;
+        d.m_directed = batch[i].req.m_directed;
+        d.n = batch[i].req.n;
+        d.out = batch[i].req.d_out;
+        gbytes += batch[i].bytes;
+      }
+      BatchWaveStats ws;
+      kamsta_status s;
+      {
+        std::lock_guard<std::mutex> clk(ctx->mu);
+        s = solve_wave(ctx, algo, descs.data(), static_cast<uint32_t>(descs.size()), scfg, false,
+                       ctx->stream, &ws);
+      }
+      const double finish = now_us();
       std::lock_guard<std::mutex> lk(mu);
-      for (size_t i = 0; i < batch.size(); ++i) {
+      for (size_t i = a; i < z; ++i) {
+        const kamsta_graph_desc& d = descs[i - a];
         kamsta_completion c{};
         c.ticket = batch[i].ticket;
         c.user_tag = batch[i].req.user_tag;
-        c.status = s != KAMSTA_OK ? s : descs[i].status;
-        c.out_count = s == KAMSTA_OK ? descs[i].out_count : 0;
-        c.total_weight = s == KAMSTA_OK ? descs[i].total_weight : 0;
+        c.status = s != KAMSTA_OK ? s : d.status;
+        c.out_count = s == KAMSTA_OK ? d.out_count : 0;
+        c.total_weight = s == KAMSTA_OK ? d.total_weight : 0;
         c.batch_size = static_cast<uint32_t>(batch.size());
         c.submit_us = batch[i].submit_us;
         c.start_us = start;
         c.finish_us = finish;
         done.push_back(c);
       }
-      bytes_in_use -= bytes;
-      in_flight -= batch.size();
+      bytes_in_use -= gbytes;
+      in_flight -= z - a;
+      cv_done.notify_all();
     }
     cv_done.notify_all();
     cv_work.notify_all();

@@ -114,6 +114,8 @@ class Solve {
   }
 
   kamsta_status run(Algo algo, kamsta_wedge* d_out, SolveOut* out);
+  // forest as a bitmap over input positions instead of edges (batch split)
+  uint32_t* forest_bits_ = nullptr;
 
  private:
   // ---- memory
@@ -925,7 +927,13 @@ kamsta_status Solve::run(Algo algo, kamsta_wedge* d_out, SolveOut* out) {
   KS_TRY(algo == Algo::kBoruvka ? run_boruvka() : run_filter_boruvka());
   // forest output
   CU_TRY(cudaMemsetAsync(ctx_->d_counters + kCMisc, 0, sizeof(DevCounters), st_));
-  if (msf_count_ > 0) {
+  if (msf_count_ > 0 && forest_bits_) {
+    const int tm = tick();
+    k_mark_forest<<<grid_for(msf_count_), kBlock, 0, st_>>>(msf_count_, msf_, in_, forest_bits_,
+                                                             &ctx_->d_counters[kCMisc].weight);
+    tock(KAMSTA_PHASE_EMIT, tm);
+    account(KAMSTA_PHASE_EMIT, msf_count_ * (4 + 4 + 8), 1);
+  } else if (msf_count_ > 0) {
     const int tm = tick();
     k_emit<<<grid_for(msf_count_), kBlock, 0, st_>>>(msf_count_, msf_, in_,
                                                       reinterpret_cast<uint32_t*>(d_out),
@@ -960,9 +968,10 @@ kamsta_status Solve::run(Algo algo, kamsta_wedge* d_out, SolveOut* out) {
 kamsta_status solve_device(kamsta_ctx* ctx, Algo algo, const kamsta_wedge* d_in,
                            uint64_t m_directed, uint32_t n, const kamsta_cfg& cfg,
                            kamsta_wedge* d_out, SolveOut* out, kamsta_stats* st,
-                           cudaStream_t stream) {
+                           cudaStream_t stream, uint32_t* d_forest_bits) {
   if (st) std::memset(st, 0, sizeof(*st));
   Solve s(ctx, stream ? stream : ctx->stream, d_in, m_directed, n, cfg, st);
+  s.forest_bits_ = d_forest_bits;
   return s.run(algo, d_out, out);
 }
 

@@ -51,6 +51,11 @@ constexpr int kTimerEvents = 64;
 struct kamsta_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t aux = nullptr;    // second stream: small graphs of a batch wave
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // batch tuning (kamsta_batch_autotune); 0 = built-in default
+  uint32_t tune_small_threads = 0;  // CTA size of the persistent small-graph kernel
+  uint32_t tune_small_max_n = 0;    // largest n taken by that kernel
   kamsta::Arena fixed;   // vertex arrays and look-back words
   cudaMemPool_t pool = nullptr;  // edge lists (stream-ordered, cached between calls)
   kamsta::DevCounters* d_counters = nullptr;  // kCSlots blocks
@@ -75,11 +80,13 @@ struct SolveOut {
 enum class Algo { kBoruvka, kFilterBoruvka };
 
 // Solves one graph whose directed, (src,dst)-sorted input lies in device
-// memory.  Writes the forest to d_out (device, capacity >= n-1).
+// memory.  Writes the forest to d_out (device, capacity >= n-1), or, when
+// d_forest_bits is given (zeroed, one bit per input entry), sets the bit of
+// the src<dst input copy of every forest edge instead.
 kamsta_status solve_device(kamsta_ctx* ctx, Algo algo, const kamsta_wedge* d_in,
                            uint64_t m_directed, uint32_t n, const kamsta_cfg& cfg,
                            kamsta_wedge* d_out, SolveOut* out, kamsta_stats* st,
-                           cudaStream_t stream);
+                           cudaStream_t stream, uint32_t* d_forest_bits = nullptr);
 
 void set_error(const std::string& msg);
 kamsta_status cuda_status(cudaError_t e, const char* what);

@@ -432,6 +432,25 @@ __global__ void k_sum_u32(const uint32_t* v, uint64_t n, unsigned long long* out
   if ((threadIdx.x & 31) == 0) atomicAdd(out, static_cast<unsigned long long>(s));
 }
 
+cudaError_t exclusive_scan_u32(cudaStream_t st, const uint32_t* in, uint32_t* out, uint64_t n,
+                               uint64_t* status, uint32_t* ticket, uint32_t* err, int sms) {
+  if (n == 0) return cudaSuccess;
+  const uint32_t nst = cdiv(n, kScanTile);
+  cudaError_t e = cudaMemsetAsync(status, 0, sizeof(uint64_t) * nst, st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(ticket, 0, sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  k_scan_u32<<<std::min<uint32_t>(nst, sms * 4), kRsBlock, 0, st>>>(in, out, n, status, ticket,
+                                                                     nst, err);
+  return cudaGetLastError();
+}
+
+cudaError_t sum_u32(cudaStream_t st, const uint32_t* v, uint64_t n, unsigned long long* out,
+                    int sms) {
+  k_sum_u32<<<sms * 8, 256, 0, st>>>(v, n, out);
+  return cudaGetLastError();
+}
+
 static uint64_t isqrt64(uint64_t n) {
   uint64_t s = static_cast<uint64_t>(std::sqrt(static_cast<double>(n)));
   while (s * s > n) --s;

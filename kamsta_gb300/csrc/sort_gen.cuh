@@ -29,8 +29,23 @@ cudaError_t radix_sort_pairs_u64(cudaStream_t st, uint64_t* keys, uint64_t* keys
                                  uint32_t* counts, uint64_t* status, uint32_t* ticket,
                                  uint32_t* err, int* result_alt, int sms);
 
+// Exclusive prefix sum of n u32 values (single pass, decoupled look-back);
+// `status` needs ceil(n / 2048) + 1 words.  Sum of n u32 values into *out
+// (added to its current value).
+cudaError_t exclusive_scan_u32(cudaStream_t st, const uint32_t* in, uint32_t* out, uint64_t n,
+                               uint64_t* status, uint32_t* ticket, uint32_t* err, int sms);
+cudaError_t sum_u32(cudaStream_t st, const uint32_t* v, uint64_t n, unsigned long long* out,
+                    int sms);
+
 kamsta_status gen_gnm(kamsta_ctx* ctx, uint32_t n, uint64_t m, uint64_t seed,
                       uint32_t max_weight, kamsta_wedge* d_out, uint64_t* m_out,
                       cudaStream_t st);
+
+kamsta_status gen_rgg2d(kamsta_ctx* ctx, uint32_t n, double radius, uint64_t seed,
+                        uint32_t max_weight, kamsta_wedge* d_out, uint64_t capacity,
+                        uint64_t* m_out, cudaStream_t st);
+kamsta_status gen_rhg(kamsta_ctx* ctx, uint32_t n, double gamma, double avg_degree, uint64_t seed,
+                      uint32_t max_weight, kamsta_wedge* d_out, uint64_t capacity,
+                      uint64_t* m_out, cudaStream_t st);
 
 }  // namespace kamsta

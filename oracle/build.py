@@ -20,7 +20,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
         t = os.path.getmtime(LIB)
         if all(os.path.getmtime(d) <= t for d in deps):
             return LIB
-    cmd = ["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared",
+    # -ffp-contract=off: the generators' floating-point definitions are
+    # evaluated without fused multiply-add, exactly like the device code
+    cmd = ["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared", "-ffp-contract=off",
            "-Wall", "-Wno-unused-function", "-o", LIB + ".tmp"] + SRC
     if verbose:
         print(" ".join(cmd), file=sys.stderr)

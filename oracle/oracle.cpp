@@ -570,3 +570,191 @@ extern "C" int oracle_gen_rgg2d(uint32_t n, double radius, uint64_t seed, uint32
   }
   return 0;
 }
+
+// ---------------------------------------------------------------------------
+// Seeded threshold random hyperbolic graph (stand-in for KaGen's get_rhg,
+// benchmarks/mst_benchmarks.hpp:143-158).  The definition, shared with the
+// device generator kamsta_gen_rhg_dev:
+//   alpha = (gamma - 1) / 2 (gamma > 2), xi = alpha / (alpha - 1/2),
+//   disk radius R = max(1, 2 ln(2 xi^2 n / (pi k))) (the asymptotic
+//   threshold-RHG degree formula, k = target average degree);
+//   base = mix64(seed ^ 0x524847); point i: u = (mix64(base + 2i) >> 11) 2^-53,
+//   v = (mix64(base + 2i + 1) >> 11) 2^-53,
+//   r = min(R, acosh(1 + u (cosh(alpha R) - 1)) / alpha), theta = 2 pi v;
+//   per point E = exp(r), Ei = exp(-r), S = sinh(r) (C library functions on
+//   the host), band = min(15, floor(16 r / R));
+//   ids = ranks of the points sorted by (band, bits(theta) >> 5, i);
+//   p ~ q (a = lower id, b = higher id) iff
+//     ((2 s) s) S_a S_b <= cosh R - 0.5 (E_a Ei_b + Ei_a E_b),
+//   s = hsin(d / 2), d = |theta_a - theta_b| folded to [0, pi], hsin the
+//   degree-21 Taylor polynomial of sin in the fixed Horner order below; all
+//   arithmetic in double, round to nearest, no fused multiply-add.
+// Candidates come from per-band angular windows that contain every pair the
+// test can accept (derived from sin^2(d/2) <= cosh R / (2 S_p sinh(b_lo))
+// with generous margins), so the edge set does not depend on the window.
+namespace gen {
+
+constexpr int kRhgBands = 16;
+constexpr double kTwoPi = 6.283185307179586;
+constexpr double kPi = 3.141592653589793;
+
+inline double rhg_hsin(double x) {
+  const double x2 = x * x;
+  double t = 1.0 - x2 / 420.0;
+  t = 1.0 - x2 / 342.0 * t;
+  t = 1.0 - x2 / 272.0 * t;
+  t = 1.0 - x2 / 210.0 * t;
+  t = 1.0 - x2 / 156.0 * t;
+  t = 1.0 - x2 / 110.0 * t;
+  t = 1.0 - x2 / 72.0 * t;
+  t = 1.0 - x2 / 42.0 * t;
+  t = 1.0 - x2 / 20.0 * t;
+  t = 1.0 - x2 / 6.0 * t;
+  return x * t;
+}
+
+struct RhgPoint {
+  double theta, E, Ei, S;
+  uint64_t key;  // band << 58 | bits(theta) >> 5
+};
+
+inline double rhg_radius(uint32_t n, double gamma, double k) {
+  const double alpha = (gamma - 1.0) / 2.0;
+  const double xi = alpha / (alpha - 0.5);
+  const double R = 2.0 * std::log(2.0 * xi * xi * n / (kPi * k));
+  return R > 1.0 ? R : 1.0;  // tiny graphs: at least a unit disk
+}
+
+inline RhgPoint rhg_point(uint64_t base, uint64_t i, double alpha, double R, double coshAR1) {
+  const double u = static_cast<double>(mix64(base + 2 * i) >> 11) * 0x1.0p-53;
+  const double v = static_cast<double>(mix64(base + 2 * i + 1) >> 11) * 0x1.0p-53;
+  double r = std::acosh(1.0 + u * coshAR1) / alpha;
+  if (r > R) r = R;
+  RhgPoint p;
+  p.theta = kTwoPi * v;
+  p.E = std::exp(r);
+  p.Ei = std::exp(-r);
+  p.S = std::sinh(r);
+  int band = static_cast<int>(std::floor(r * kRhgBands / R));
+  if (band > kRhgBands - 1) band = kRhgBands - 1;
+  if (band < 0) band = 0;
+  uint64_t tb;
+  std::memcpy(&tb, &p.theta, sizeof(tb));
+  p.key = (static_cast<uint64_t>(band) << 58) | (tb >> 5);
+  return p;
+}
+
+inline bool rhg_edge(const RhgPoint& a, const RhgPoint& b, double coshR) {
+  double d = a.theta > b.theta ? a.theta - b.theta : b.theta - a.theta;
+  if (d > kPi) d = kTwoPi - d;
+  const double s = rhg_hsin(d * 0.5);
+  const double lhs = 2.0 * s * s * a.S * b.S;
+  const double rhs = coshR - 0.5 * (a.E * b.Ei + a.Ei * b.E);
+  return lhs <= rhs;
+}
+
+}  // namespace gen
+
+extern "C" int oracle_gen_rhg(uint32_t n, double gamma, double avg_degree, uint64_t seed,
+                              uint32_t max_weight, kamsta_wedge* out, uint64_t capacity,
+                              uint64_t* m_directed_out) {
+  using namespace gen;
+  *m_directed_out = 0;
+  if (max_weight == 0 || !(gamma > 2.0) || !(avg_degree > 0)) return 1;
+  if (n == 0) return 0;
+  const double alpha = (gamma - 1.0) / 2.0;
+  const double R = rhg_radius(n, gamma, avg_degree);
+  if (!(R > 0)) return 1;
+  const double coshR = std::cosh(R), coshAR1 = std::cosh(alpha * R) - 1.0;
+  const uint64_t base = mix64(seed ^ 0x524847ull);
+  const uint64_t wseed = mix64(seed ^ 0x6a09e667f3bcc909ull);
+  std::vector<RhgPoint> pt(n);
+  std::vector<std::pair<uint64_t, uint32_t>> order(n);
+#pragma omp parallel for schedule(static)
+  for (uint64_t i = 0; i < n; ++i) {
+    pt[i] = rhg_point(base, i, alpha, R, coshAR1);
+    order[i] = {pt[i].key, static_cast<uint32_t>(i)};
+  }
+  std::sort(order.begin(), order.end());
+  std::vector<RhgPoint> P(n);
+  for (uint64_t j = 0; j < n; ++j) P[j] = pt[order[j].second];
+  std::vector<uint64_t> bstart(kRhgBands + 1, 0);
+  for (int b = 0; b <= kRhgBands; ++b) {
+    const uint64_t x = static_cast<uint64_t>(b) << 58;
+    bstart[b] = std::lower_bound(order.begin(), order.end(), std::make_pair(x, 0u)) - order.begin();
+  }
+  std::vector<double> sh_lo(kRhgBands);
+  for (int b = 0; b < kRhgBands; ++b) sh_lo[b] = std::sinh(R * b / kRhgBands);
+  auto tkey = [](double t) {
+    uint64_t tb;
+    std::memcpy(&tb, &t, sizeof(tb));
+    return tb >> 5;
+  };
+  // index range [lo, hi) of band b whose (truncated) angle lies in [t0, t1]
+  auto range = [&](int b, double t0, double t1, uint64_t* lo, uint64_t* hi) {
+    const uint64_t bk = static_cast<uint64_t>(b) << 58;
+    auto first = order.begin() + bstart[b], last = order.begin() + bstart[b + 1];
+    *lo = std::lower_bound(first, last, std::make_pair(bk | tkey(t0), 0u)) - order.begin();
+    *hi = std::upper_bound(first, last, std::make_pair(bk | tkey(t1), 0xffffffffu)) -
+          order.begin();
+  };
+  auto visit = [&](uint64_t j, auto&& emit) {
+    const RhgPoint& p = P[j];
+    for (int b = 0; b < kRhgBands; ++b) {
+      if (bstart[b] == bstart[b + 1]) continue;
+      bool full = sh_lo[b] <= 0.0 || p.S <= 0.0;
+      double D = 0;
+      if (!full) {
+        const double s = std::sqrt(coshR / (2.0 * p.S * sh_lo[b])) * (1.0 + 1e-6);
+        if (s >= 1.0) full = true;
+        else {
+          D = 2.0 * std::asin(s) + 1e-9;
+          if (D >= kPi) full = true;
+        }
+      }
+      uint64_t r0 = bstart[b], r1 = bstart[b], r2 = bstart[b], r3 = bstart[b];
+      if (full) {
+        r1 = bstart[b + 1];
+      } else {
+        const double lo = p.theta - D, hi = p.theta + D;
+        if (lo < 0) {
+          range(b, 0.0, hi, &r0, &r1);
+          range(b, lo + kTwoPi, kTwoPi, &r2, &r3);
+        } else if (hi >= kTwoPi) {
+          range(b, 0.0, hi - kTwoPi, &r0, &r1);
+          range(b, lo, kTwoPi, &r2, &r3);
+        } else {
+          range(b, lo, hi, &r0, &r1);
+        }
+      }
+      for (int part = 0; part < 2; ++part) {
+        const uint64_t a0 = part ? r2 : r0, a1 = part ? r3 : r1;
+        for (uint64_t k = a0; k < a1; ++k) {
+          if (k == j) continue;
+          const bool e = j < k ? rhg_edge(P[j], P[k], coshR) : rhg_edge(P[k], P[j], coshR);
+          if (e) emit(k);
+        }
+      }
+    }
+  };
+  std::vector<uint64_t> off(static_cast<uint64_t>(n) + 1, 0);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (uint64_t j = 0; j < n; ++j) {
+    uint64_t d = 0;
+    visit(j, [&](uint64_t) { ++d; });
+    off[j + 1] = d;
+  }
+  for (uint64_t j = 0; j < n; ++j) off[j + 1] += off[j];
+  *m_directed_out = off[n];
+  if (off[n] > capacity) return 2;
+#pragma omp parallel for schedule(dynamic, 256)
+  for (uint64_t j = 0; j < n; ++j) {
+    uint64_t o = off[j];
+    visit(j, [&](uint64_t k) {
+      const uint64_t canon = (std::min(j, k) << 32) | std::max(j, k);
+      const uint32_t w = 1 + static_cast<uint32_t>(hi64(mix64(wseed ^ canon), max_weight));
+      out[o++] = kamsta_wedge{static_cast<uint32_t>(j), static_cast<uint32_t>(k), w};
+    });
+  }
+  return 0;
+}

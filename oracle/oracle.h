@@ -20,6 +20,8 @@
  *                              device generator kamsta_gen_gnm_dev.
  *   oracle_gen_rgg2d        -- seeded 2-D random geometric graph; bit-identical
  *                              to kamsta_gen_rgg2d_dev.
+ *   oracle_gen_rhg          -- seeded threshold random hyperbolic graph;
+ *                              bit-identical to kamsta_gen_rhg_dev.
  *
  * Parity status: the reference ships no golden vectors (its only test,
  * tests/test_sets.sh, checks the MSF weight against this same Kruskal).
@@ -62,6 +64,14 @@ int oracle_gen_gnm(uint32_t n, uint64_t m, uint64_t seed, uint32_t max_weight,
  * 1 on bad arguments. */
 int oracle_gen_rgg2d(uint32_t n, double radius, uint64_t seed, uint32_t max_weight,
                      kamsta_wedge* out, uint64_t capacity, uint64_t* m_directed_out);
+
+/* Seeded threshold random hyperbolic graph (power-law exponent gamma > 2,
+ * target average degree); definition in oracle.cpp, bit-identical to the
+ * device generator kamsta_gen_rhg_dev on the same machine.  Same return
+ * convention as oracle_gen_rgg2d. */
+int oracle_gen_rhg(uint32_t n, double gamma, double avg_degree, uint64_t seed,
+                   uint32_t max_weight, kamsta_wedge* out, uint64_t capacity,
+                   uint64_t* m_directed_out);
 
 /* Number of OpenMP threads the oracle uses when threads == 0. */
 int oracle_max_threads(void);

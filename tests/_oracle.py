@@ -27,6 +27,8 @@ def lib():
                                             C.POINTER(U64), C.POINTER(U32)]
         L.oracle_gen_gnm.argtypes = [U32, U64, U64, U32, P, C.POINTER(U64)]
         L.oracle_gen_rgg2d.argtypes = [U32, C.c_double, U64, U32, P, U64, C.POINTER(U64)]
+        L.oracle_gen_rhg.argtypes = [U32, C.c_double, C.c_double, U64, U32, P, U64,
+                                     C.POINTER(U64)]
         L.oracle_max_threads.restype = C.c_int
         _lib = L
     return _lib
@@ -49,6 +51,19 @@ def gen_rgg2d(n: int, radius: float, seed: int, max_weight: int = 254) -> np.nda
     out = np.empty(max(cnt.value, 1), WEDGE)
     rc = lib().oracle_gen_rgg2d(n, radius, seed, max_weight, out.ctypes.data, cnt.value,
                                 C.byref(cnt))
+    assert rc == 0
+    return out[: cnt.value]
+
+
+def gen_rhg(n: int, gamma: float, avg_degree: float, seed: int,
+            max_weight: int = 254) -> np.ndarray:
+    cnt = C.c_uint64()
+    rc = lib().oracle_gen_rhg(n, gamma, avg_degree, seed, max_weight, None, 0, C.byref(cnt))
+    if rc not in (0, 2):
+        raise ValueError("oracle_gen_rhg: bad arguments")
+    out = np.empty(max(cnt.value, 1), WEDGE)
+    rc = lib().oracle_gen_rhg(n, gamma, avg_degree, seed, max_weight, out.ctypes.data,
+                              cnt.value, C.byref(cnt))
     assert rc == 0
     return out[: cnt.value]
 

@@ -54,3 +54,42 @@ def test_mst_on_rgg2d(kamsta, oracle, algo, n, deg):
     fn, cfg = _configs(kamsta)[algo]
     e = oracle.gen_rgg2d(n, oracle.rgg_radius(n, deg), 40 + n % 7)
     _check(oracle, fn(e, cfg, n=n), e, n)
+
+
+def _dev_rhg(kamsta, ctx, n, gamma, k, seed, wmax=254):
+    import torch
+    md = ctx.gen_rhg_dev(n, gamma, k, seed, wmax)
+    d = torch.empty((max(md, 1), 3), dtype=torch.int32, device="cuda")
+    assert ctx.gen_rhg_dev(n, gamma, k, seed, wmax, d.data_ptr(), md) == md
+    torch.cuda.synchronize()
+    return d[:md].cpu().numpy().view(np.uint32).reshape(-1).view(kamsta.WEDGE)
+
+
+@pytest.mark.parametrize("n,gamma,k,seed", [(1, 3.0, 16, 1), (2, 3.0, 4, 2), (300, 3.0, 16, 3),
+                                            (5000, 2.5, 10, 4), (1 << 16, 3.0, 16, 5),
+                                            (1 << 18, 3.0, 16, 6), (1 << 17, 4.0, 8, 7)])
+def test_rhg_matches_oracle(kamsta, oracle, n, gamma, k, seed):
+    ctx = kamsta.Context(0)
+    assert np.array_equal(_dev_rhg(kamsta, ctx, n, gamma, k, seed),
+                          oracle.gen_rhg(n, gamma, k, seed))
+
+
+@pytest.mark.parametrize("algo", ["boruvka_plain", "boruvka_local", "filter_boruvka",
+                                  "filter_dedupe"])
+@pytest.mark.parametrize("n,k", [(1 << 12, 8.0), (1 << 16, 16.0), (1 << 19, 16.0)])
+def test_mst_on_rhg(kamsta, oracle, algo, n, k):
+    from tests.test_parity_gpu import _check, _configs
+    fn, cfg = _configs(kamsta)[algo]
+    e = oracle.gen_rhg(n, 3.0, k, 50 + n % 11)
+    _check(oracle, fn(e, cfg, n=n), e, n)
+
+
+@pytest.mark.parametrize("family", ["rgg2d", "rhg"])
+def test_filter_boruvka_geometric_config_exactness(kamsta, oracle, family):
+    """The geometric / skewed configuration (filter-Boruvka on RGG-2D and RHG
+    with average degree 16) at n=2^21, checked against Kruskal."""
+    n = 1 << 21
+    e = (oracle.gen_rgg2d(n, oracle.rgg_radius(n, 16), 2024) if family == "rgg2d"
+         else oracle.gen_rhg(n, 3.0, 16, 2024))
+    from tests.test_parity_gpu import _check
+    _check(oracle, kamsta.filter_boruvka(e, kamsta.AlgorithmConfig(), n=n), e, n)

@@ -145,3 +145,69 @@ def test_rgg2d_properties(oracle):
     assert np.all(k[1:] > k[:-1])  # (src,dst) sorted, no duplicates
     assert np.array_equal(np.sort((d << np.uint64(32)) | s), k)  # both directions
     assert 14.0 < len(e) / n < 16.5  # border effects lower the mean degree slightly
+
+
+def _py_rhg(n, gamma, k, seed, wmax=254):
+    """All-pairs restatement of the RHG definition (small n only); Python's
+    math module uses the same C library functions as the generators' host
+    code, and Python floats round like the device code (no FMA)."""
+    import math
+    alpha = (gamma - 1) / 2
+    xi = alpha / (alpha - 0.5)
+    R = max(1.0, 2.0 * math.log(2.0 * xi * xi * n / (3.141592653589793 * k)))
+    coshR, coshAR1 = math.cosh(R), math.cosh(alpha * R) - 1.0
+    base = _mix64(seed ^ 0x524847)
+    wseed = _mix64(seed ^ 0x6A09E667F3BCC909)
+    pts = []
+    for i in range(n):
+        u = (_mix64((base + 2 * i) % (1 << 64)) >> 11) * 2.0 ** -53
+        v = (_mix64((base + 2 * i + 1) % (1 << 64)) >> 11) * 2.0 ** -53
+        r = min(R, math.acosh(1.0 + u * coshAR1) / alpha)
+        theta = 6.283185307179586 * v
+        band = max(0, min(15, math.floor(r * 16 / R)))
+        tb = np.array([theta]).view(np.uint64)[0]
+        pts.append(((band << 58) | (int(tb) >> 5), i, theta, math.exp(r), math.exp(-r),
+                    math.sinh(r)))
+    pts.sort(key=lambda p: (p[0], p[1]))
+
+    def hsin(x):
+        x2 = x * x
+        t = 1.0 - x2 / 420.0
+        for c in (342.0, 272.0, 210.0, 156.0, 110.0, 72.0, 42.0, 20.0, 6.0):
+            t = 1.0 - x2 / c * t
+        return x * t
+
+    out = []
+    for j in range(n):
+        for q in range(n):
+            if q == j:
+                continue
+            a, b = (pts[j], pts[q]) if j < q else (pts[q], pts[j])
+            d = abs(a[2] - b[2])
+            if d > 3.141592653589793:
+                d = 6.283185307179586 - d
+            s = hsin(d * 0.5)
+            if 2.0 * s * s * a[5] * b[5] <= coshR - 0.5 * (a[3] * b[4] + a[4] * b[3]):
+                canon = (min(j, q) << 32) | max(j, q)
+                out.append((j, q, 1 + ((_mix64(wseed ^ canon) * wmax) >> 64)))
+    return out
+
+
+@pytest.mark.parametrize("n,gamma,k,seed", [(1, 3.0, 8, 1), (60, 3.0, 8, 2), (300, 3.0, 16, 3),
+                                            (250, 2.6, 10, 4), (200, 4.0, 6, 5)])
+def test_rhg_matches_definition(oracle, n, gamma, k, seed):
+    e = oracle.gen_rhg(n, gamma, k, seed)
+    got = [(int(a), int(b), int(w)) for a, b, w in zip(e["src"], e["dst"], e["w"])]
+    assert got == _py_rhg(n, gamma, k, seed)
+
+
+def test_rhg_properties(oracle):
+    n = 1 << 15
+    e = oracle.gen_rhg(n, 3.0, 16, 7)
+    s, d = e["src"].astype(np.uint64), e["dst"].astype(np.uint64)
+    k = (s << np.uint64(32)) | d
+    assert np.all(k[1:] > k[:-1])
+    assert np.array_equal(np.sort((d << np.uint64(32)) | s), k)
+    deg = np.bincount(e["src"], minlength=n)
+    assert 8 < len(e) / n < 32        # near the target average degree
+    assert deg.max() > 20 * len(e) / n  # power law: hubs
