@@ -121,7 +121,7 @@ typedef struct kamsta_stats {
   double device_ms;        /* device time of the solve (CUDA events)       */
   uint64_t alg_bytes;      /* algorithmic HBM bytes of the solve            */
   uint32_t trace_len;      /* entries in trace_m / trace_n                  */
-  uint32_t pad_;
+  uint32_t row_scans;      /* heavy-class contractions done by row scans    */
   uint64_t trace_m[KAMSTA_TRACE_MAX]; /* live undirected edges per round   */
   uint64_t trace_n[KAMSTA_TRACE_MAX]; /* live vertices per round           */
   double phase_ms[KAMSTA_PHASES];     /* device time per phase             */
@@ -281,6 +281,8 @@ typedef struct kamsta_server_cfg {
   uint32_t workers;          /* worker threads / streams (1..8, default 2)   */
   kamsta_cfg solver;         /* solver options for every job (FILTER flag    */
                              /* selects filter_boruvka)                      */
+  uint32_t small_threads;    /* batch tuning of the workers' contexts        */
+  uint32_t small_max_n;      /* (kamsta_tuning; 0 = built-in default)        */
 } kamsta_server_cfg;
 
 typedef struct kamsta_request {

@@ -239,7 +239,8 @@ class Server:
     """
 
     def __init__(self, device: int = 0, budget_bytes: int = 0, max_batch: int = 0,
-                 workers: int = 2, config: AlgorithmConfig | None = None):
+                 workers: int = 2, config: AlgorithmConfig | None = None,
+                 tuning: dict | None = None):
         c = _native.ServerCfg()
         check(lib().kamsta_server_cfg_default(C.byref(c)))
         if budget_bytes:
@@ -248,6 +249,9 @@ class Server:
             c.max_batch = int(max_batch)
         c.workers = int(workers)
         c.solver = (config or AlgorithmConfig()).to_c()
+        if tuning:
+            c.small_threads = int(tuning.get("small_threads", 0))
+            c.small_max_n = int(tuning.get("small_max_n", 0))
         h = C.c_void_p()
         check(lib().kamsta_server_create(int(device), C.byref(c), C.byref(h)))
         self._h = h

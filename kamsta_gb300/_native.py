@@ -52,13 +52,13 @@ class Stats(C.Structure):
                 ("rounds", C.c_uint32), ("levels", C.c_uint32),
                 ("dedupe_passes", C.c_uint32), ("gpu_launches", C.c_uint32),
                 ("device_ms", C.c_double), ("alg_bytes", C.c_uint64),
-                ("trace_len", C.c_uint32), ("pad_", C.c_uint32),
+                ("trace_len", C.c_uint32), ("row_scans", C.c_uint32),
                 ("trace_m", C.c_uint64 * TRACE_MAX), ("trace_n", C.c_uint64 * TRACE_MAX),
                 ("phase_ms", C.c_double * len(PHASES)), ("phase_bytes", C.c_uint64 * len(PHASES)),
                 ("phase_launches", C.c_uint32 * len(PHASES))]
 
     def as_dict(self) -> dict:
-        skip = ("trace_m", "trace_n", "pad_", "phase_ms", "phase_bytes", "phase_launches")
+        skip = ("trace_m", "trace_n", "phase_ms", "phase_bytes", "phase_launches")
         d = {k: getattr(self, k) for k, _ in self._fields_ if k not in skip}
         d["trace"] = [(int(self.trace_m[i]), int(self.trace_n[i])) for i in range(self.trace_len)]
         d["phases"] = {name: {"ms": float(self.phase_ms[i]), "bytes": int(self.phase_bytes[i]),
@@ -85,7 +85,8 @@ class BatchStats(C.Structure):
 
 class ServerCfg(C.Structure):
     _fields_ = [("budget_bytes", C.c_uint64), ("max_batch", C.c_uint32),
-                ("workers", C.c_uint32), ("solver", Cfg)]
+                ("workers", C.c_uint32), ("solver", Cfg), ("small_threads", C.c_uint32),
+                ("small_max_n", C.c_uint32)]
 
 
 class Request(C.Structure):

@@ -305,12 +305,6 @@ __global__ void __launch_bounds__(kBlock, 3)
       }
       cls[j] = weight_class<NOUT>(wt, p);
     }
-    {  // a tile that keeps nothing (typical of the filter passes) is done
-      bool any = false;
-#pragma unroll
-      for (int j = 0; j < kItemsDir; ++j) any |= cls[j] != 0xff;
-      if (!__syncthreads_or(any)) continue;
-    }
     seg_tile_finish<NOUT, kItemsDir>(cls, run, p, [&](uint32_t t) {
       Rec r;
       r.a = words[3 * t];
@@ -471,12 +465,6 @@ __global__ void __launch_bounds__(kBlock, 3)
       recs[t].a = la;
       recs[t].b = lb;
       cls[j] = weight_class<NOUT>(r.w, p);
-    }
-    {  // a tile that keeps nothing is done
-      bool any = false;
-#pragma unroll
-      for (int j = 0; j < kItemsRec; ++j) any |= cls[j] != 0xff;
-      if (!__syncthreads_or(any)) continue;
     }
     seg_tile_finish<NOUT, kItemsRec>(cls, run, p, [&](uint32_t t) { return recs[t]; });
   }
@@ -872,6 +860,132 @@ __global__ void k_big_bitmap(uint32_t n, const uint32_t* __restrict__ D, uint32_
     const uint32_t x = wi * 32 + lane_id();
     const uint32_t b = __ballot_sync(kFull, x < n && D[x] == g);
     if (lane_id() == 0) bits[wi] = b;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Heavy-class contraction by row scans.  When the largest component holds
+// all but a few vertices, an edge of the directed input survives the
+// relabel pass (endpoint labels differ) only if one endpoint lies outside
+// that component.  Those edges are found by scanning the input rows of the
+// outside vertices -- the input is (src, dst)-sorted, so a row is two binary
+// searches away -- instead of streaming the whole input.  Each surviving
+// edge is reported with the position of its src<dst copy (oid), exactly the
+// record the streaming pass would have kept; sorting by oid restores the
+// streaming pass's order.
+
+// Vertices outside the largest component (bit 0 in `big`), any order.
+__global__ void k_outside_big(uint32_t n, const uint32_t* __restrict__ big, uint32_t* __restrict__ out,
+                             uint32_t cap, unsigned long long* count) {
+  const uint32_t words = (n + 31) / 32;
+  for (uint32_t wi = blockIdx.x * blockDim.x + threadIdx.x; wi < words;
+       wi += gridDim.x * blockDim.x) {
+    uint32_t f = ~big[wi];
+    const uint32_t base = wi * 32;
+    if (base + 32 > n) f &= (n - base >= 32) ? ~0u : ((1u << (n - base)) - 1);
+    if (!f) continue;
+    const uint64_t o = atomicAdd(count, static_cast<unsigned long long>(__popc(f)));
+    uint64_t k = o;
+    while (f) {
+      const uint32_t b = __ffs(f) - 1;
+      f &= f - 1;
+      if (k < cap) out[k] = base + b;
+      ++k;
+    }
+  }
+}
+
+// first directed entry with src >= v (entries [0, md) sorted by src)
+__device__ __forceinline__ uint64_t row_begin(const uint32_t* __restrict__ in, uint64_t md,
+                                              uint32_t v) {
+  uint64_t lo = 0, hi = md;
+  while (lo < hi) {
+    const uint64_t mid = (lo + hi) >> 1;
+    if (in[3 * mid] < v) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+// One warp per outside vertex v: every entry (v, d, w) of its row with w in
+// [wmin, wmax] whose relabelled endpoints differ; d outside too and d < v:
+// reported from d's row; d inside and d < v: the oid is found in d's row.
+// WRITE = false counts, WRITE = true writes records at atomic slots.
+template <bool WRITE>
+__global__ void k_row_scan(const uint32_t* __restrict__ in, uint64_t md, uint32_t n,
+                           const uint32_t* __restrict__ S, uint32_t ns,
+                           const uint32_t* __restrict__ D, const uint32_t* __restrict__ big,
+                           uint32_t big_label, uint32_t wmin, uint32_t wmax, Rec* __restrict__ out,
+                           uint64_t cap, unsigned long long* count, uint32_t* err) {
+  const uint32_t lane = lane_id();
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < ns; k += warps) {
+    const uint32_t v = S[k];
+    const uint64_t lo = row_begin(in, md, v), hi = row_begin(in, md, v + 1);
+    const uint32_t la = D[v];
+    for (uint64_t i0 = lo; i0 < hi; i0 += 32) {
+      const uint64_t i = i0 + lane;
+      bool keep = false;
+      Rec r;
+      if (i < hi) {
+        const uint32_t d = in[3 * i + 1], w = in[3 * i + 2];
+        if (d < n && d != v && w >= wmin && w <= wmax) {
+          const bool d_big = (__ldg(big + (d >> 5)) >> (d & 31)) & 1u;
+          const uint32_t lb = d_big ? big_label : D[d];
+          if (la != lb) {
+            if (v < d) {
+              keep = true;
+              r = Rec{la, lb, w, static_cast<uint32_t>(i)};
+            } else if (d_big) {
+              // the src<dst copy (d, v) sits in d's row, sorted by dst
+              uint64_t a = row_begin(in, md, d), b = row_begin(in, md, d + 1);
+              while (a < b) {
+                const uint64_t mid = (a + b) >> 1;
+                if (in[3 * mid + 1] < v) a = mid + 1; else b = mid;
+              }
+              if (a < md && in[3 * a] == d && in[3 * a + 1] == v) {
+                keep = true;
+                r = Rec{lb, la, w, static_cast<uint32_t>(a)};
+              }
+            }
+          }
+        }
+      }
+      const uint32_t bal = __ballot_sync(kFull, keep);
+      if (!bal) continue;
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(count, static_cast<unsigned long long>(__popc(bal)));
+      base = __shfl_sync(kFull, base, 0);
+      if (WRITE && keep) {
+        const uint64_t slot = base + __popc(bal & lanemask_lt());
+        if (slot < cap) out[slot] = r;
+        else atomicOr(err, kErrOverflow);
+      }
+    }
+  }
+}
+
+__global__ void k_set_u32(uint32_t* p, uint32_t v) { *p = v; }
+
+// oid keys of the collected records (for the sort back into input order)
+__global__ void k_rec_oid_keys(const Rec* __restrict__ r, uint64_t k, uint64_t* __restrict__ keys,
+                               uint32_t* __restrict__ idx) {
+  for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < k;
+       i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    keys[i] = r[i].oid;
+    idx[i] = static_cast<uint32_t>(i);
+  }
+}
+
+// out[p] = in[idx[p]] and the round-0 minimum with position p
+__global__ void k_rec_place_min(const Rec* __restrict__ in, const uint32_t* __restrict__ idx,
+                                uint64_t k, Rec* __restrict__ out, uint64_t* minval) {
+  for (uint64_t p = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; p < k;
+       p += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    const Rec r = in[idx[p]];
+    out[p] = r;
+    const uint64_t v = (static_cast<uint64_t>(r.w) << 32) | p;
+    red_min(&minval[r.a], v);
+    red_min(&minval[r.b], v);
   }
 }
 

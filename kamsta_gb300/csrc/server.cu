@@ -214,6 +214,15 @@ kamsta_status kamsta_server_create(int device, const kamsta_server_cfg* cfg,
     // to the device at the wave's synchronisation points
     uint64_t keep = c.budget_bytes / c.workers;
     cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    kamsta_tuning tune{};
+    tune.small_threads = c.small_threads;
+    tune.small_max_n = c.small_max_n;
+    if (kamsta_ctx_set_tuning(ctx, &tune) != KAMSTA_OK) {
+      for (auto* p : s->ctxs) kamsta_ctx_destroy(p);
+      kamsta_ctx_destroy(ctx);
+      delete s;
+      return KAMSTA_E_INPUT;
+    }
     s->ctxs.push_back(ctx);
   }
   for (uint32_t w = 0; w < c.workers; ++w)

@@ -152,6 +152,9 @@ class Solve {
   // [wmin, wmax], a share `frac` of the entries) into the current dense
   // labels, fuse the round-0 minimum and contract the result.
   kamsta_status contract(const SegList* L, uint32_t wmin, uint32_t wmax, double frac);
+  // contract()'s pass over the directed input done by row scans of the
+  // vertices outside the largest component (done = false: too many of them)
+  kamsta_status contract_rows(uint32_t wmin, uint32_t wmax, SegList* E, bool* done);
   // Largest current component (mode of sampled labels); when it holds at
   // least half the vertices, its membership bitmap is built into big_ and
   // the next D-relabelling pass skips gathers for edges inside it.
@@ -212,7 +215,8 @@ class Solve {
   bool aligned16_ = false;
   bool debug_ = false;
   bool tolerate_overflow_ = false;
-  uint32_t launches_ = 0, rounds_ = 0, levels_ = 0, dedupe_passes_ = 0;
+  uint32_t launches_ = 0, rounds_ = 0, levels_ = 0, dedupe_passes_ = 0, row_scans_ = 0;
+  bool final_contraction_ = false;  // rounds() of the last contraction (boruvka)
   uint64_t alg_bytes_ = 0;
   double phase_ms_[KAMSTA_PHASES] = {};
   uint64_t phase_bytes_[KAMSTA_PHASES] = {};
@@ -642,6 +646,7 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
   if (cur_owned) free_list(cur);
   rounds_ += r;
   if (r == 0) return KAMSTA_OK;  // nothing contracted; labels unchanged
+  if (final_contraction_) return KAMSTA_OK;  // no later pass needs the labels
   ca.rounds = r;
   ca.P = P_;
   ca.err = ctx_->d_err;
@@ -771,10 +776,91 @@ kamsta_status Solve::pick_big(uint32_t* label, bool* use) {
   return KAMSTA_OK;
 }
 
+kamsta_status Solve::contract_rows(uint32_t wmin, uint32_t wmax, SegList* E, bool* done) {
+  *done = false;
+  // the vertices outside the largest component
+  const uint32_t cap_s = std::max<uint32_t>(1u << 16, n_ / 32);
+  void* smem = nullptr;
+  CU_TRY(cudaMallocFromPoolAsync(&smem, sizeof(uint32_t) * cap_s, ctx_->pool, st_));
+  struct Free {
+    void* p;
+    cudaStream_t s;
+    ~Free() {
+      if (p) cudaFreeAsync(p, s);
+    }
+  } fs{smem, st_};
+  uint32_t* S = static_cast<uint32_t*>(smem);
+  const int t0 = tick();
+  CU_TRY(cudaMemsetAsync(ctx_->d_counters + kCMisc, 0, sizeof(DevCounters), st_));
+  unsigned long long* cnt = &ctx_->d_counters[kCMisc].cnt[0];
+  k_outside_big<<<grid_for((n_ + 31) / 32), kBlock, 0, st_>>>(n_, big_, S, cap_s, cnt);
+  KS_TRY(fetch_counters());
+  const uint64_t ns = ctx_->h_counters[kCMisc].cnt[0];
+  if (ns > cap_s) return KAMSTA_OK;  // too many: stream the input instead
+  const int grid = grid_for(std::max<uint64_t>(ns * 32, 1));
+  // count, then write the surviving edges
+  k_row_scan<false><<<grid, kBlock, 0, st_>>>(in_, md_, n_, S, static_cast<uint32_t>(ns), D_,
+                                              big_, big_label_, wmin, wmax, nullptr, 0,
+                                              &ctx_->d_counters[kCMisc].cnt[1], ctx_->d_err);
+  KS_TRY(fetch_counters());
+  const uint64_t k = ctx_->h_counters[kCMisc].cnt[1];
+  KS_TRY(alloc_list(E, 1, std::max<uint64_t>(k, 1)));
+  if (k > 0) {
+    void* tmem = nullptr;
+    const RadixScratch rs = radix_scratch_bytes(k);
+    const size_t rb = round_up(k * sizeof(Rec), 256), kb = round_up(k * 8, 256),
+                 ib = round_up(k * 4, 256), cb = round_up(rs.counts * 4, 256),
+                 sb = round_up(rs.status * 8, 256);
+    CU_TRY(cudaMallocFromPoolAsync(&tmem, rb + 2 * kb + 2 * ib + cb + sb, ctx_->pool, st_));
+    Free ft{tmem, st_};
+    char* m = static_cast<char*>(tmem);
+    Rec* tmp = reinterpret_cast<Rec*>(m);
+    uint64_t* keys = reinterpret_cast<uint64_t*>(m + rb);
+    uint64_t* keys2 = reinterpret_cast<uint64_t*>(m + rb + kb);
+    uint32_t* idx = reinterpret_cast<uint32_t*>(m + rb + 2 * kb);
+    uint32_t* idx2 = reinterpret_cast<uint32_t*>(m + rb + 2 * kb + ib);
+    uint32_t* counts = reinterpret_cast<uint32_t*>(m + rb + 2 * kb + 2 * ib);
+    uint64_t* status = reinterpret_cast<uint64_t*>(m + rb + 2 * kb + 2 * ib + cb);
+    k_row_scan<true><<<grid, kBlock, 0, st_>>>(in_, md_, n_, S, static_cast<uint32_t>(ns), D_,
+                                               big_, big_label_, wmin, wmax, tmp, k,
+                                               &ctx_->d_counters[kCMisc].cnt[2], ctx_->d_err);
+    k_rec_oid_keys<<<grid_for(k), kBlock, 0, st_>>>(tmp, k, keys, idx);
+    int alt = 0;
+    uint32_t bits = 1;
+    while (bits < 64 && (1ull << bits) < md_) ++bits;
+    cudaError_t e = radix_sort_pairs_u32(st_, keys, keys2, idx, idx2, k, static_cast<int>(bits),
+                                         counts, status, &ctx_->d_counters[kCMisc].ticket,
+                                         ctx_->d_err, &alt, sms_);
+    if (e != cudaSuccess) return cuda_status(e, "radix sort (row scan)");
+    if (alt) std::swap(idx, idx2);
+    k_rec_place_min<<<grid_for(k), kBlock, 0, st_>>>(tmp, idx, k, E->base, minA_);
+    k_set_u32<<<1, 1, 0, st_>>>(E->d_count, static_cast<uint32_t>(k));
+    KS_TRY(fetch_counters());  // also: the scratch above is released after use
+  }
+  E->h_count.assign(1, static_cast<uint32_t>(k));
+  E->total = k;
+  tock(KAMSTA_PHASE_CLASS_PASS, t0);
+  // outside set, rows (entries of the scanned rows twice), kept records,
+  // sort and placement
+  account(KAMSTA_PHASE_CLASS_PASS, uint64_t(n_) / 8 + ns * 4 + k * (16 + 12 + 16 + 16 + 16), 6);
+  ++row_scans_;
+  *done = true;
+  return KAMSTA_OK;
+}
+
 kamsta_status Solve::contract(const SegList* L, uint32_t wmin, uint32_t wmax, double frac) {
   if ((L && L->total == 0) || nreps_ <= 1) return KAMSTA_OK;
   fill_inf(minA_, nreps_);
   KS_TRY(pick_big(&big_label_, &use_big_));
+  if (!L && use_big_) {  // heaviest class of the directed input: row scans
+    SegList* E = new_list();
+    bool done = false;
+    KS_TRY(contract_rows(wmin, wmax, E, &done));
+    if (done) {
+      use_big_ = false;
+      return rounds(E, true);
+    }
+  }
   SegList* E = new_list();
   SegList* outs[1] = {E};
   const double f[1] = {frac};
@@ -814,16 +900,23 @@ kamsta_status Solve::run_boruvka() {
       break;
   }
   for (int c = 0; c < nmat; ++c) KS_TRY(debug_list("after first pass", *C[c], n_));
+  // the last contraction skips the final label update (nothing reads it)
+  const int steps = nmat + std::max(0, K - nmat + 1);
+  int step = 0;
+  final_contraction_ = ++step == steps;
   KS_TRY(rounds(C[0], true));
   for (int c = 1; c < nmat; ++c) {
+    final_contraction_ = ++step == steps;
     KS_TRY(contract(C[c], 0, 0xffffffffu, 1.0));
     free_list(C[c]);
   }
   for (int c = nmat; c <= K; ++c) {
     const uint32_t lo = b[c - 1] + 1;
     const uint32_t hi = c < K ? b[c] : 0xffffffffu;
+    final_contraction_ = ++step == steps;
     KS_TRY(contract(nullptr, lo, hi, sample_share(samples_host_, lo, hi)));
   }
+  final_contraction_ = false;
   return KAMSTA_OK;
 }
 
@@ -953,6 +1046,7 @@ kamsta_status Solve::run(Algo algo, kamsta_wedge* d_out, SolveOut* out) {
     stats_->rounds = rounds_;
     stats_->levels = levels_;
     stats_->dedupe_passes = dedupe_passes_;
+    stats_->row_scans = row_scans_;
     stats_->gpu_launches = launches_;
     stats_->device_ms = ms;
     stats_->alg_bytes = alg_bytes_;

@@ -39,11 +39,12 @@ def test_struct_layouts_match_header(kamsta, tmp_path):
     from kamsta_gb300 import _native
     prog = tmp_path / "sz.c"
     prog.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "kamsta_gpu.h"\n'
-                    'int main(){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(kamsta_cfg),'
+                    'int main(){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(kamsta_cfg),'
                     'sizeof(kamsta_stats), sizeof(kamsta_wedge), sizeof(kamsta_wedge64),'
                     'offsetof(kamsta_stats, trace_m), offsetof(kamsta_cfg, seed),'
                     'sizeof(kamsta_graph_desc), offsetof(kamsta_graph_desc, out),'
-                    'sizeof(kamsta_batch_stats));}\n')
+                    'sizeof(kamsta_batch_stats), sizeof(kamsta_server_cfg), sizeof(kamsta_request),'
+                    'sizeof(kamsta_completion), sizeof(kamsta_cgraph), sizeof(kamsta_tuning));}\n')
     exe = tmp_path / "sz"
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(prog), "-o", str(exe)],
                    check=True)
@@ -52,7 +53,10 @@ def test_struct_layouts_match_header(kamsta, tmp_path):
     assert got == [C.sizeof(_native.Cfg), C.sizeof(_native.Stats), _native.WEDGE.itemsize,
                    _native.WEDGE64.itemsize, _native.Stats.trace_m.offset,
                    _native.Cfg.seed.offset, C.sizeof(_native.GraphDesc),
-                   _native.GraphDesc.out.offset, C.sizeof(_native.BatchStats)]
+                   _native.GraphDesc.out.offset, C.sizeof(_native.BatchStats),
+                   C.sizeof(_native.ServerCfg), C.sizeof(_native.Request),
+                   C.sizeof(_native.Completion), C.sizeof(_native.CGraph),
+                   C.sizeof(_native.Tuning)]
 
 
 def test_cfg_default_mirrors_reference_algorithm_config(kamsta):

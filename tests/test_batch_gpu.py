@@ -129,3 +129,41 @@ def test_batch_dev_equals_alone(kamsta):
             assert descs[i].total_weight == int(a[:, 2].astype(np.uint64).sum())
         if budget:
             assert st["waves"] > 1
+
+
+def test_autotune_keeps_results(kamsta):
+    """kamsta_batch_autotune picks valid settings, and every setting gives the
+    same forests (the tuning changes schedules, never results)."""
+    import torch
+    ctx = kamsta.Context(0)
+    rng = np.random.default_rng(3)
+    specs = [(int(2 ** rng.uniform(8, 17)), float(rng.uniform(4, 24))) for _ in range(40)]
+    bufs, outs, descs = [], [], (kamsta.GraphDesc * len(specs))()
+    for i, (n, deg) in enumerate(specs):
+        m = min(n * (n - 1) // 2, int(n * deg / 2))
+        d = torch.empty((2 * m, 3), dtype=torch.int32, device="cuda")
+        md = ctx.gen_gnm_dev(n, m, 900 + i, 254, d.data_ptr())
+        o = torch.zeros((max(n, 1), 3), dtype=torch.int32, device="cuda")
+        bufs.append(d)
+        outs.append(o)
+        descs[i].edges, descs[i].m_directed, descs[i].n, descs[i].out = d.data_ptr(), md, n, \
+            o.data_ptr()
+    torch.cuda.synchronize()
+    ref = None
+    for threads, cut in [(256, 4096), (512, 32768), (1024, 16384)]:
+        ctx.set_tuning(threads, cut)
+        ctx.batch_dev(descs)
+        torch.cuda.synchronize()
+        got = [outs[i][:descs[i].out_count].cpu().numpy().copy() for i in range(len(specs))]
+        if ref is None:
+            ref = got
+        else:
+            assert all(np.array_equal(a, b) for a, b in zip(ref, got))
+    t = ctx.batch_autotune(descs)
+    assert t["small_threads"] in (256, 512, 1024)
+    assert t["small_max_n"] in (4096, 8192, 16384, 32768)
+    assert all(v > 0 for v in t["cutoff_ms"].values())
+    ctx.batch_dev(descs)
+    torch.cuda.synchronize()
+    assert all(np.array_equal(ref[i], outs[i][:descs[i].out_count].cpu().numpy())
+               for i in range(len(specs)))

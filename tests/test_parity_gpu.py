@@ -212,3 +212,15 @@ def test_dedupe_runs_and_keeps_the_forest(kamsta, oracle, mode, ratio):
     st0 = {}
     kamsta.boruvka(e, kamsta.AlgorithmConfig(dedupe="never", dedupe_ratio=ratio), n=n, stats=st0)
     assert st0["dedupe_passes"] == 0
+
+
+def test_row_scan_contraction_is_used_and_exact(kamsta, oracle):
+    """The heaviest class of a dense G(n,m) is contracted by scanning only the
+    rows of the few vertices outside the giant component; the forest stays
+    the oracle's."""
+    n, m = 1 << 20, 1 << 24
+    e = oracle.gen_gnm(n, m, 77)
+    st = {}
+    got = kamsta.boruvka(e, kamsta.AlgorithmConfig(local_preprocessing=1), n=n, stats=st)
+    _check(oracle, got, e, n)
+    assert st["row_scans"] >= 1
