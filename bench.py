@@ -436,7 +436,20 @@ def main():
     assert got == md
     torch.cuda.synchronize()
 
-    cfg = K.AlgorithmConfig(local_preprocessing=K.LocalPreprocessing(args.local_preprocessing))
+    # autotune the first-pass tile (entries per thread) on this workload:
+    # one untimed solve per candidate, the fastest is used for every step
+    tiles = {}
+    for items, seg in ((8, 8), (12, 8), (16, 8), (8, 4), (12, 4)):
+        c = K.AlgorithmConfig(local_preprocessing=K.LocalPreprocessing(args.local_preprocessing),
+                              items_per_thread=items, seg_items_per_thread=seg)
+        ctx.boruvka_dev(d_edges.data_ptr(), md, n, d_out.data_ptr(), c, stream=sh)
+        st = {}
+        ctx.boruvka_dev(d_edges.data_ptr(), md, n, d_out.data_ptr(), c, stream=sh, stats=st)
+        tiles[f"{items}x{seg}"] = st["device_ms"]
+    best = min(tiles, key=tiles.get)
+    best_items, best_seg = (int(x) for x in best.split("x"))
+    cfg = K.AlgorithmConfig(local_preprocessing=K.LocalPreprocessing(args.local_preprocessing),
+                            items_per_thread=best_items, seg_items_per_thread=best_seg)
     results = []
 
     def step(stats=None):
@@ -507,6 +520,9 @@ def main():
                    "algorithm": "boruvka (hybridBoruvka), local_preprocessing="
                                 f"{args.local_preprocessing} (reference benchmark default 1)",
                    "l2": "input (24 GiB) >> L2 (129 MB); no flush needed",
+                   "first_pass_items_per_thread": best_items,
+                   "list_pass_records_per_thread": best_seg,
+                   "tile_autotune_ms": tiles,
                    "parallelism": f"replicas x{args.gpus}"},
         "forest_edges": forest, "forest_weight": per_step[-1]["total_weight"],
         "gpu_launches": launches, "roofline": roofline, "clocks": clk,

@@ -56,6 +56,8 @@ class AlgorithmConfig:
     trace: bool = False
     seed: int | None = None
     filter: bool = False        # batch / serving: filter_boruvka instead of boruvka
+    items_per_thread: int = 0   # first-pass tile: 8, 12 or 16 entries per thread (0 = 8)
+    seg_items_per_thread: int = 0  # list-pass tile: 4 or 8 records per thread (0 = 4)
 
     def to_c(self) -> _native.Cfg:
         c = _native.default_cfg()
@@ -77,6 +79,8 @@ class AlgorithmConfig:
             flags |= FLAG_DEDUPE_ALWAYS
         c.flags = flags
         c.dedupe_ratio = int(self.dedupe_ratio)
+        c.items_per_thread = int(self.items_per_thread)
+        c.seg_items_per_thread = int(self.seg_items_per_thread)
         if self.seed is not None:
             c.seed = int(self.seed)
         return c

@@ -44,7 +44,7 @@ class Cfg(C.Structure):
     _fields_ = [("local_preprocessing", C.c_int32), ("compression", C.c_int32),
                 ("filter_threshold", C.c_uint64), ("flags", C.c_uint32),
                 ("dedupe_ratio", C.c_uint32), ("seed", C.c_uint64),
-                ("block_threads", C.c_uint32), ("items_per_thread", C.c_uint32)]
+                ("seg_items_per_thread", C.c_uint32), ("items_per_thread", C.c_uint32)]
 
 
 class Stats(C.Structure):

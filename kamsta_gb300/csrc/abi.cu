@@ -24,6 +24,16 @@ kamsta_status check_cfg(const kamsta_cfg* cfg) {
     return cfg->compression == KAMSTA_SEVEN_BIT_DIFF_ENCODING ? KAMSTA_E_UNSUPPORTED
                                                                : KAMSTA_E_INPUT;
   }
+  if (cfg->items_per_thread != 0 && cfg->items_per_thread != 8 && cfg->items_per_thread != 12 &&
+      cfg->items_per_thread != 16) {
+    set_error("items_per_thread: 0, 8, 12 or 16");
+    return KAMSTA_E_INPUT;
+  }
+  if (cfg->seg_items_per_thread != 0 && cfg->seg_items_per_thread != 4 &&
+      cfg->seg_items_per_thread != 8) {
+    set_error("seg_items_per_thread: 0, 4 or 8");
+    return KAMSTA_E_INPUT;
+  }
   if (cfg->local_preprocessing < KAMSTA_NO_PREPROCESSING ||
       cfg->local_preprocessing > KAMSTA_REDUCE_EDGES_THEN_BORUVKA) {
     set_error("local_preprocessing: unknown value");
@@ -64,6 +74,25 @@ struct DefaultCtx {
 };
 thread_local DefaultCtx g_default;
 
+// Host-to-device copy of a large input as pieces alternating between the
+// context's two streams (two copy engines in flight); the main stream waits
+// for both before the solve.
+cudaError_t copy_in(kamsta_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  constexpr size_t kPiece = 256ull << 20;
+  if (bytes <= 2 * kPiece)
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  cudaError_t e = cudaEventRecord(ctx->ev_fork, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->aux, ctx->ev_fork, 0);
+  for (size_t off = 0, k = 0; e == cudaSuccess && off < bytes; off += kPiece, ++k) {
+    const size_t len = std::min(kPiece, bytes - off);
+    e = cudaMemcpyAsync(static_cast<char*>(dst) + off, static_cast<const char*>(src) + off, len,
+                        cudaMemcpyHostToDevice, (k & 1) ? ctx->aux : ctx->stream);
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_join, ctx->aux);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0);
+  return e;
+}
+
 kamsta_status solve_host(Algo algo, const kamsta_wedge* edges, uint64_t m, uint32_t n,
                          const kamsta_cfg* cfg, kamsta_wedge* out, uint64_t* out_count,
                          kamsta_stats* stats) {
@@ -88,7 +117,7 @@ kamsta_status solve_host(Algo algo, const kamsta_wedge* edges, uint64_t m, uint3
   if (e != cudaSuccess) return cuda_status(e, "device buffers for host input");
   kamsta_wedge* din = ctx->io.take<kamsta_wedge>(m);
   kamsta_wedge* dout = ctx->io.take<kamsta_wedge>(std::max<uint64_t>(n, 1));
-  e = cudaMemcpyAsync(din, edges, m * sizeof(kamsta_wedge), cudaMemcpyHostToDevice, ctx->stream);
+  e = copy_in(ctx, din, edges, m * sizeof(kamsta_wedge));
   if (e != cudaSuccess) return cuda_status(e, "cudaMemcpyAsync(H2D)");
   SolveOut so;
   s = solve_device(ctx, algo, din, m, n, c, dout, &so, stats, ctx->stream);

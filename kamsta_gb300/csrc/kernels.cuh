@@ -17,8 +17,8 @@
 namespace kamsta {
 
 constexpr int kBlock = 256;
-constexpr int kItemsDir = 12;   // directed 12-byte records per thread
-constexpr int kItemsRec = 8;    // 16-byte records per thread
+constexpr int kItemsDir = 8;    // directed 12-byte records per thread (default tile)
+constexpr int kItemsRec = 4;    // 16-byte records per thread (default tile)
 constexpr int kItemsVtx = 8;    // vertices per thread in the vertex scans
 constexpr int kMaxOut = 3;      // weight classes materialised by one pass
 
@@ -76,20 +76,38 @@ struct PassArgs {
   uint32_t aligned16; // directed source base is 16-byte aligned
 };
 
-// Relabel both endpoints; false when they land in the same component.
-__device__ __forceinline__ bool relabel(const PassArgs& p, uint32_t s, uint32_t d, uint32_t& la,
-                                        uint32_t& lb) {
-  if (p.big) {
-    const bool bs = (__ldg(p.big + (s >> 5)) >> (s & 31)) & 1u;
-    const bool bd = (__ldg(p.big + (d >> 5)) >> (d & 31)) & 1u;
-    if (bs && bd) return false;
-    la = bs ? p.big_label : p.map[s];
-    lb = bd ? p.big_label : p.map[d];
-  } else {
-    la = p.map[s];
-    lb = p.map[d];
+// Relabel a thread's ITEMS items with all label reads in flight together:
+// membership bits first (one load per endpoint), then the map for the
+// endpoints outside the largest component.  Writing the labels back to
+// shared memory only afterwards keeps the compiler from ordering each
+// item's loads behind the previous item's store.  keep[j] is cleared for
+// items whose endpoints land in the same component.
+template <int ITEMS>
+__device__ __forceinline__ void relabel_batch(const PassArgs& p, const uint32_t (&a)[ITEMS],
+                                              const uint32_t (&b)[ITEMS], bool (&keep)[ITEMS],
+                                              uint32_t (&la)[ITEMS], uint32_t (&lb)[ITEMS]) {
+  bool ina[ITEMS], inb[ITEMS];
+#pragma unroll
+  for (int j = 0; j < ITEMS; ++j) {
+    ina[j] = inb[j] = false;
+    if (p.big && keep[j]) {
+      ina[j] = (__ldg(p.big + (a[j] >> 5)) >> (a[j] & 31)) & 1u;
+      inb[j] = (__ldg(p.big + (b[j] >> 5)) >> (b[j] & 31)) & 1u;
+    }
   }
-  return la != lb;
+#pragma unroll
+  for (int j = 0; j < ITEMS; ++j) {
+    if (!keep[j]) continue;
+    if (ina[j] && inb[j]) {
+      keep[j] = false;
+      continue;
+    }
+    la[j] = ina[j] ? p.big_label : p.map[a[j]];
+    lb[j] = inb[j] ? p.big_label : p.map[b[j]];
+  }
+#pragma unroll
+  for (int j = 0; j < ITEMS; ++j)
+    if (keep[j] && la[j] == lb[j]) keep[j] = false;
 }
 
 template <int NOUT>
@@ -207,13 +225,19 @@ __device__ __forceinline__ void seg_pass_end(const uint64_t (&run)[NOUT], uint32
 // not 16-byte aligned is read with plain loads throughout.  Striped layout:
 // item j of thread t is tile item j*kBlock + t, so consecutive lanes read
 // consecutive records (conflict-free) and write consecutive output slots.
-constexpr uint32_t kDirTile = kItemsDir * kBlock;
-constexpr uint32_t kDirStageWords = kDirTile * 3;
-constexpr size_t kDirDynSmem = 2 * kDirStageWords * sizeof(uint32_t);
+// Items per thread is a tile-size knob (kamsta_cfg.items_per_thread: 8, 12
+// or 16; 8 by default, the fastest on GB300 at 2^26/2^30).
+constexpr uint32_t dir_tile(int items) { return static_cast<uint32_t>(items) * kBlock; }
+constexpr size_t dir_dyn_smem(int items) { return 2ull * dir_tile(items) * 3 * sizeof(uint32_t); }
+constexpr uint32_t kDirTile = dir_tile(kItemsDir);
+constexpr size_t kDirDynSmem = dir_dyn_smem(kItemsDir);
 
-template <int NOUT>
-__global__ void __launch_bounds__(kBlock, 3)
+template <int NOUT, int ITEMS = kItemsDir, bool MAPPED = false>
+__global__ void __launch_bounds__(kBlock, ITEMS <= 8 ? 4 : 3)
     k_pass_dir(const uint32_t* __restrict__ in, PassArgs p) {
+  constexpr uint32_t kDirTile = dir_tile(ITEMS);
+  constexpr uint32_t kDirStageWords = kDirTile * 3;
+  constexpr int kItemsDir = ITEMS;
   extern __shared__ __align__(128) uint32_t s_words[];  // two stages
   __shared__ __align__(8) uint64_t s_bar[2];
   __shared__ uint32_t s_ok;
@@ -286,24 +310,49 @@ __global__ void __launch_bounds__(kBlock, 3)
       }
     }
     uint8_t cls[kItemsDir];
+    if constexpr (!MAPPED) {  // original ids: no label reads
 #pragma unroll
-    for (int j = 0; j < kItemsDir; ++j) {
-      const uint32_t t = j * kBlock + threadIdx.x;
-      const uint32_t s = words[3 * t], d = words[3 * t + 1], wt = words[3 * t + 2];
-      cls[j] = 0xff;
-      if (t >= cnt || !(s < d) || d >= p.n) continue;
-      if (wt < p.wmin || wt > p.wmax) {
-        dropped_w += (wt > p.wmax) ? 1u : 0u;
-        continue;
+      for (int j = 0; j < kItemsDir; ++j) {
+        const uint32_t t = j * kBlock + threadIdx.x;
+        const uint32_t s = words[3 * t], d = words[3 * t + 1], wt = words[3 * t + 2];
+        cls[j] = 0xff;
+        if (t >= cnt || !(s < d) || d >= p.n) continue;
+        if (wt < p.wmin || wt > p.wmax) {
+          dropped_w += (wt > p.wmax) ? 1u : 0u;
+          continue;
+        }
+        ++cand;
+        cls[j] = weight_class<NOUT>(wt, p);
       }
-      ++cand;
-      if (p.map) {
-        uint32_t la, lb;
-        if (!relabel(p, s, d, la, lb)) continue;
-        words[3 * t] = la;  // item t belongs to this thread alone
-        words[3 * t + 1] = lb;
+    } else {
+      uint32_t ss[kItemsDir], dd[kItemsDir], ww[kItemsDir];
+      bool keep[kItemsDir];
+#pragma unroll
+      for (int j = 0; j < kItemsDir; ++j) {
+        const uint32_t t = j * kBlock + threadIdx.x;
+        ss[j] = words[3 * t];
+        dd[j] = words[3 * t + 1];
+        ww[j] = words[3 * t + 2];
+        keep[j] = false;
+        if (t >= cnt || !(ss[j] < dd[j]) || dd[j] >= p.n) continue;
+        if (ww[j] < p.wmin || ww[j] > p.wmax) {
+          dropped_w += (ww[j] > p.wmax) ? 1u : 0u;
+          continue;
+        }
+        ++cand;
+        keep[j] = true;
       }
-      cls[j] = weight_class<NOUT>(wt, p);
+      uint32_t la[kItemsDir], lb[kItemsDir];
+      relabel_batch<kItemsDir>(p, ss, dd, keep, la, lb);
+#pragma unroll
+      for (int j = 0; j < kItemsDir; ++j) {
+        cls[j] = 0xff;
+        if (!keep[j]) continue;
+        const uint32_t t = j * kBlock + threadIdx.x;
+        words[3 * t] = la[j];  // item t belongs to this thread alone
+        words[3 * t + 1] = lb[j];
+        cls[j] = weight_class<NOUT>(ww[j], p);
+      }
     }
     seg_tile_finish<NOUT, kItemsDir>(cls, run, p, [&](uint32_t t) {
       Rec r;
@@ -321,8 +370,10 @@ __global__ void __launch_bounds__(kBlock, 3)
 // items [lo + k*T, ...); thread 0 maps them to physical runs (at most a few,
 // as segments hold thousands of records) and copies each run with one bulk
 // copy into the tile's stage.
-constexpr uint32_t kRecTile = kItemsRec * kBlock;
-constexpr size_t kRecDynSmem = 2 * kRecTile * sizeof(Rec);
+constexpr uint32_t rec_tile(int items) { return static_cast<uint32_t>(items) * kBlock; }
+constexpr size_t rec_dyn_smem(int items) { return 2ull * rec_tile(items) * sizeof(Rec); }
+constexpr uint32_t kRecTile = rec_tile(kItemsRec);
+constexpr size_t kRecDynSmem = rec_dyn_smem(kItemsRec);
 constexpr int kMaxRuns = 16;
 
 // prefix[s] = records in segments < s (shared memory), built by the block
@@ -366,9 +417,13 @@ __device__ __forceinline__ uint32_t seg_find(const uint64_t* prefix, uint32_t ns
   return lo;
 }
 
-template <int NOUT>
-__global__ void __launch_bounds__(kBlock, 3)
+// ITEMS (records per thread, 4 or 8) is a tile knob: smaller tiles give more
+// resident CTAs for the latency-bound relabel passes.
+template <int NOUT, int ITEMS = kItemsRec>
+__global__ void __launch_bounds__(kBlock, ITEMS <= 4 ? 4 : 3)
     k_pass_seg(SegIn in, PassArgs p) {
+  constexpr uint32_t kRecTile = rec_tile(ITEMS);
+  constexpr int kItemsRec = ITEMS;
   extern __shared__ __align__(128) Rec s_rec[];  // two stages
   __shared__ uint64_t s_prefix[kMaxSeg + 1];
   __shared__ __align__(8) uint64_t s_bar[2];
@@ -449,23 +504,38 @@ __global__ void __launch_bounds__(kBlock, 3)
       __syncthreads();
     }
     uint8_t cls[kItemsRec];
+    uint32_t ra[kItemsRec], rb[kItemsRec], rw[kItemsRec];
+    bool keep[kItemsRec];
 #pragma unroll
     for (int j = 0; j < kItemsRec; ++j) {
       const uint32_t t = j * kBlock + threadIdx.x;
-      cls[j] = 0xff;
+      keep[j] = false;
+      ra[j] = rb[j] = rw[j] = 0;
       if (t >= cnt) continue;
       const Rec r = recs[t];
+      ra[j] = r.a;
+      rb[j] = r.b;
+      rw[j] = r.w;
       if (r.w < p.wmin || r.w > p.wmax) {
         dropped_w += (r.w > p.wmax) ? 1u : 0u;
         continue;
       }
       ++cand;
-      uint32_t la = r.a, lb = r.b;
-      if (p.map && !relabel(p, r.a, r.b, la, lb)) continue;
-      recs[t].a = la;
-      recs[t].b = lb;
-      cls[j] = weight_class<NOUT>(r.w, p);
+      keep[j] = true;
     }
+    if (p.map) {
+      uint32_t la[kItemsRec], lb[kItemsRec];
+      relabel_batch<kItemsRec>(p, ra, rb, keep, la, lb);
+#pragma unroll
+      for (int j = 0; j < kItemsRec; ++j) {
+        if (!keep[j]) continue;
+        const uint32_t t = j * kBlock + threadIdx.x;
+        recs[t].a = la[j];
+        recs[t].b = lb[j];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kItemsRec; ++j) cls[j] = keep[j] ? weight_class<NOUT>(rw[j], p) : 0xff;
     seg_tile_finish<NOUT, kItemsRec>(cls, run, p, [&](uint32_t t) { return recs[t]; });
   }
   seg_pass_end<NOUT>(run, dropped_w, cand, p);
@@ -535,31 +605,54 @@ __global__ void k_dedupe_mark(const uint64_t* __restrict__ keys, const uint32_t*
 // edges): every live vertex hooks onto the other endpoint of its minimum
 // edge; of a mutual pair the lower label stays root.  Vertices without an
 // incident edge are finished ("exhausted") and stay their own root.
+// Each thread takes kIlp vertices per step (stride apart) and issues their
+// loads level by level -- all minima, then all records, then all partner
+// minima -- so several independent random reads are in flight per thread.
+constexpr int kIlp = 4;
+
 __global__ void k_hook(uint32_t n, const uint64_t* __restrict__ minval,
                        const Rec* __restrict__ list, uint32_t* __restrict__ parent,
                        uint32_t* __restrict__ msfoid, uint32_t* err) {
-  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n;
-       v += gridDim.x * blockDim.x) {
-    const uint64_t val = minval[v];
-    if (val == kInf64) {
-      parent[v] = v;
-      msfoid[v] = kNone;
-      continue;
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; base < n;
+       base += kIlp * stride) {
+    uint64_t val[kIlp], mu[kIlp];
+    Rec r[kIlp];
+    uint32_t u[kIlp];
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k) {
+      const uint64_t v = base + k * stride;
+      val[k] = v < n ? minval[v] : kInf64;
     }
-    const Rec r = list[static_cast<uint32_t>(val)];
-    if (r.a != v && r.b != v) {
-      atomicOr(err, kErrHook);
-      parent[v] = v;
-      msfoid[v] = kNone;
-      continue;
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k)
+      if (val[k] != kInf64) r[k] = list[static_cast<uint32_t>(val[k])];
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k) {
+      mu[k] = kInf64;
+      u[k] = 0;
+      if (val[k] == kInf64) continue;
+      const uint32_t v = static_cast<uint32_t>(base + k * stride);
+      if (r[k].a != v && r[k].b != v) {
+        val[k] = kInf64;  // reported below, hooks nowhere
+        atomicOr(err, kErrHook);
+        continue;
+      }
+      u[k] = r[k].a ^ r[k].b ^ v;
+      mu[k] = minval[u[k]];
     }
-    const uint32_t u = r.a ^ r.b ^ v;
-    if (minval[u] == val && v < u) {
-      parent[v] = v;
-      msfoid[v] = kNone;
-    } else {
-      parent[v] = u;
-      msfoid[v] = r.oid;
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k) {
+      const uint64_t vv = base + k * stride;
+      if (vv >= n) continue;
+      const uint32_t v = static_cast<uint32_t>(vv);
+      if (val[k] == kInf64 || (mu[k] == val[k] && v < u[k])) {
+        parent[v] = v;
+        msfoid[v] = kNone;
+      } else {
+        parent[v] = u[k];
+        msfoid[v] = r[k].oid;
+      }
     }
   }
 }
@@ -568,18 +661,40 @@ __global__ void k_hook(uint32_t n, const uint64_t* __restrict__ minval,
 // 161-169) with path halving; every write stores an ancestor, so concurrent
 // updates stay correct.  Capped; the cap reports kErrJump.
 __global__ void k_jump(uint32_t n, uint32_t* parent, uint32_t* err) {
-  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n;
-       v += gridDim.x * blockDim.x) {
-    uint32_t x = v;
-    uint32_t p = ld_relaxed(parent + x);
-    if (p == x) continue;
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; base < n;
+       base += kIlp * stride) {
+    // kIlp halving walks side by side, one step at a time
+    uint32_t x[kIlp], p[kIlp];
+    bool run[kIlp];
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k) {
+      const uint64_t v = base + k * stride;
+      x[k] = static_cast<uint32_t>(v);
+      p[k] = v < n ? ld_relaxed(parent + v) : x[k];
+      run[k] = v < n && p[k] != x[k];
+    }
     uint32_t steps = 0;
     for (;;) {
-      const uint32_t gp = ld_relaxed(parent + p);
-      if (gp == p) break;
-      st_relaxed(parent + x, gp);
-      x = gp;
-      p = ld_relaxed(parent + x);
+      bool any = false;
+      uint32_t gp[kIlp];
+#pragma unroll
+      for (int k = 0; k < kIlp; ++k) gp[k] = run[k] ? ld_relaxed(parent + p[k]) : 0u;
+#pragma unroll
+      for (int k = 0; k < kIlp; ++k) {
+        if (!run[k]) continue;
+        if (gp[k] == p[k]) {
+          run[k] = false;
+          continue;
+        }
+        st_relaxed(parent + x[k], gp[k]);
+        x[k] = gp[k];
+        any = true;
+      }
+      if (!any) break;
+#pragma unroll
+      for (int k = 0; k < kIlp; ++k)
+        if (run[k]) p[k] = ld_relaxed(parent + x[k]);
       ++steps;
       // a cycle (never produced by a correct hook) must not keep the device
       // busy: one thread reaching the cap stops all others within 1024 steps
@@ -588,32 +703,11 @@ __global__ void k_jump(uint32_t n, uint32_t* parent, uint32_t* err) {
         break;
       }
     }
-    st_relaxed(parent + v, p);
-  }
-}
-
-// Second pointer-jumping pass.  Path halving lets a thread overwrite another
-// vertex's finished root pointer with an older ancestor, so after k_jump some
-// entries may still point one or two levels below the root.  Here every
-// thread only reads other entries and writes its own, so when the kernel
-// ends every vertex points at its root.
-__global__ void k_jump_finish(uint32_t n, uint32_t* parent, uint32_t* err) {
-  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n;
-       v += gridDim.x * blockDim.x) {
-    uint32_t p = ld_relaxed(parent + v);
-    if (p == v) continue;
-    uint32_t steps = 0;
-    for (;;) {
-      const uint32_t gp = ld_relaxed(parent + p);
-      if (gp == p) break;
-      p = gp;
-      ++steps;
-      if ((steps & 1023u) == 0 && (steps > kJumpCap || (ld_relaxed(err) & kErrJump))) {
-        atomicOr(err, kErrJump);
-        break;
-      }
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k) {
+      const uint64_t v = base + k * stride;
+      if (v < n && p[k] != static_cast<uint32_t>(v)) st_relaxed(parent + v, p[k]);
     }
-    st_relaxed(parent + v, p);
   }
 }
 
@@ -738,13 +832,52 @@ __global__ void __launch_bounds__(kBlock) k_vertex_write(VertexScanArgs p) {
 }
 
 // Label map of one round: dense id in round r -> dense id in round r+1, or
-// kNone for a finished vertex.
+// kNone for a finished vertex.  The root is found by following the parent
+// pointers that k_jump's path halving may have left a level or two short
+// (read only, capped like k_jump), so no separate pass is needed.
 __global__ void k_map(uint32_t n, const uint64_t* __restrict__ minval,
                       const uint32_t* __restrict__ parent,
-                      const uint32_t* __restrict__ newid, uint32_t* __restrict__ R) {
-  for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n;
-       v += gridDim.x * blockDim.x) {
-    R[v] = (minval[v] == kInf64 && parent[v] == v) ? kNone : newid[parent[v]];
+                      const uint32_t* __restrict__ newid, uint32_t* __restrict__ R,
+                      uint32_t* err) {
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; base < n;
+       base += kIlp * stride) {
+    uint32_t p[kIlp], q[kIlp];
+    bool live[kIlp];
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k) {
+      const uint64_t v = base + k * stride;
+      live[k] = v < n;
+      p[k] = live[k] ? parent[v] : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k) q[k] = live[k] ? parent[p[k]] : 0u;
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k) {
+      if (!live[k]) continue;
+      const uint32_t v = static_cast<uint32_t>(base + k * stride);
+      if (p[k] == v) {  // a root
+        q[k] = minval[v] == kInf64 ? kNone : v;
+        continue;
+      }
+      // follow pointers k_jump left short of the root (rare, capped)
+      uint32_t x = p[k], y = q[k], steps = 0;
+      while (y != x) {
+        x = y;
+        y = parent[x];
+        if ((++steps & 1023u) == 0 && (steps > kJumpCap || (ld_relaxed(err) & kErrJump))) {
+          atomicOr(err, kErrJump);
+          break;
+        }
+      }
+      q[k] = x;
+    }
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k) {
+      if (!live[k]) continue;
+      const uint64_t v = base + k * stride;
+      R[v] = q[k] == kNone ? kNone : newid[q[k]];
+    }
   }
 }
 
@@ -762,20 +895,41 @@ struct ChaseArgs {
 };
 
 __global__ void k_chase(ChaseArgs p) {
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < p.n0;
-       i += gridDim.x * blockDim.x) {
-    uint32_t x = i;
-    uint32_t rep = kNone;
-    for (uint32_t r = 0; r < p.rounds; ++r) {
-      const uint32_t y = p.R[r][x];
-      if (y == kNone) {
-        rep = p.orig[r][x];
-        break;
-      }
-      x = y;
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; base < p.n0;
+       base += kIlp * stride) {
+    // kIlp chains walked side by side, one round map at a time
+    uint32_t x[kIlp], rep[kIlp];
+    bool run[kIlp];
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k) {
+      const uint64_t i = base + k * stride;
+      run[k] = i < p.n0;
+      x[k] = static_cast<uint32_t>(i);
+      rep[k] = kNone;
     }
-    if (rep == kNone) rep = p.orig[p.rounds][x];
-    p.P[p.orig[0][i]] = rep;
+    for (uint32_t r = 0; r < p.rounds; ++r) {
+      uint32_t y[kIlp];
+#pragma unroll
+      for (int k = 0; k < kIlp; ++k) y[k] = run[k] ? p.R[r][x[k]] : 0u;
+#pragma unroll
+      for (int k = 0; k < kIlp; ++k) {
+        if (!run[k]) continue;
+        if (y[k] == kNone) {
+          rep[k] = p.orig[r][x[k]];
+          run[k] = false;
+        } else {
+          x[k] = y[k];
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k) {
+      const uint64_t i = base + k * stride;
+      if (i >= p.n0) continue;
+      const uint32_t r0 = rep[k] == kNone ? p.orig[p.rounds][x[k]] : rep[k];
+      p.P[p.orig[0][i]] = r0;
+    }
   }
 }
 
@@ -1001,11 +1155,22 @@ __global__ void k_sample_labels(uint32_t n, const uint32_t* __restrict__ D, uint
 __global__ void k_relabel_all(uint32_t n, uint32_t* __restrict__ P,
                               const uint32_t* __restrict__ dense_of,
                               uint32_t* __restrict__ D) {
-  for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n;
-       x += gridDim.x * blockDim.x) {
-    const uint32_t p = P[P[x]];
-    P[x] = p;
-    D[x] = dense_of[p];
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; base < n;
+       base += kIlp * stride) {
+    uint32_t p[kIlp], d[kIlp];
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k) p[k] = base + k * stride < n ? P[base + k * stride] : 0u;
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k) p[k] = base + k * stride < n ? P[p[k]] : 0u;
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k) d[k] = base + k * stride < n ? dense_of[p[k]] : 0u;
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k) {
+      if (base + k * stride >= n) continue;
+      P[base + k * stride] = p[k];
+      D[base + k * stride] = d[k];
+    }
   }
 }
 
@@ -1028,14 +1193,30 @@ __global__ void k_emit(uint64_t k, const uint32_t* __restrict__ msf,
                        uint32_t* __restrict__ out_words,
                        unsigned long long* weight) {
   uint64_t local = 0;
-  for (uint64_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k;
-       i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
-    const uint64_t o = static_cast<uint64_t>(msf[i]) * 3;
-    const uint32_t s = in_words[o], d = in_words[o + 1], w = in_words[o + 2];
-    out_words[3 * i] = s;
-    out_words[3 * i + 1] = d;
-    out_words[3 * i + 2] = w;
-    local += w;
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; base < k;
+       base += kIlp * stride) {
+    uint32_t s[kIlp], d[kIlp], w[kIlp];
+    uint64_t o[kIlp];
+#pragma unroll
+    for (int j = 0; j < kIlp; ++j)
+      o[j] = base + j * stride < k ? static_cast<uint64_t>(msf[base + j * stride]) * 3 : ~0ull;
+#pragma unroll
+    for (int j = 0; j < kIlp; ++j) {
+      if (o[j] == ~0ull) continue;
+      s[j] = in_words[o[j]];
+      d[j] = in_words[o[j] + 1];
+      w[j] = in_words[o[j] + 2];
+    }
+#pragma unroll
+    for (int j = 0; j < kIlp; ++j) {
+      if (o[j] == ~0ull) continue;
+      const uint64_t i = base + j * stride;
+      out_words[3 * i] = s[j];
+      out_words[3 * i + 1] = d[j];
+      out_words[3 * i + 2] = w[j];
+      local += w[j];
+    }
   }
   local = warp_sum(local);
   if (lane_id() == 0 && local) atomicAdd(weight, static_cast<unsigned long long>(local));

@@ -217,6 +217,8 @@ class Solve {
   bool tolerate_overflow_ = false;
   uint32_t launches_ = 0, rounds_ = 0, levels_ = 0, dedupe_passes_ = 0, row_scans_ = 0;
   bool final_contraction_ = false;  // rounds() of the last contraction (boruvka)
+  int dir_items_ = kItemsDir;        // items per thread of k_pass_dir (8, 12, 16)
+  int seg_items_ = kItemsRec;        // records per thread of k_pass_seg (4, 8)
   uint64_t alg_bytes_ = 0;
   double phase_ms_[KAMSTA_PHASES] = {};
   uint64_t phase_bytes_[KAMSTA_PHASES] = {};
@@ -402,10 +404,20 @@ kamsta_status Solve::pass(int phase, const SegList* src, const uint32_t* map, ui
                           bool validate) {
   const bool dir = src == nullptr;
   const uint64_t total = dir ? md_ : src->total;
-  const uint32_t tile = dir ? kDirTile : kRecTile;
-  const size_t dyn = dir ? kDirDynSmem : kRecDynSmem;
+  const int items = dir_items_;
+  const int sitems = seg_items_;
+  const uint32_t tile = dir ? dir_tile(items) : rec_tile(sitems);
+  const size_t dyn = dir ? dir_dyn_smem(items) : rec_dyn_smem(sitems);
+  const bool mapped = map != nullptr;
   const int per_sm =
-      dir ? blocks_per_sm(k_pass_dir<NOUT>, dyn) : blocks_per_sm(k_pass_seg<NOUT>, dyn);
+      !dir ? (sitems == 4 ? blocks_per_sm(k_pass_seg<NOUT, 4>, dyn)
+                          : blocks_per_sm(k_pass_seg<NOUT, 8>, dyn))
+      : mapped ? (items == 8    ? blocks_per_sm(k_pass_dir<NOUT, 8, true>, dyn)
+                  : items == 16 ? blocks_per_sm(k_pass_dir<NOUT, 16, true>, dyn)
+                                : blocks_per_sm(k_pass_dir<NOUT, 12, true>, dyn))
+               : (items == 8    ? blocks_per_sm(k_pass_dir<NOUT, 8, false>, dyn)
+                  : items == 16 ? blocks_per_sm(k_pass_dir<NOUT, 16, false>, dyn)
+                                : blocks_per_sm(k_pass_dir<NOUT, 12, false>, dyn));
   const uint64_t gmax = std::min<uint64_t>(kMaxSeg, uint64_t(per_sm) * sms_);
   uint64_t chunk = std::max<uint64_t>(1, (total + gmax - 1) / gmax);
   chunk = round_up(chunk, tile);
@@ -446,10 +458,22 @@ kamsta_status Solve::pass(int phase, const SegList* src, const uint32_t* map, ui
     a.validate = validate ? 1 : 0;
     a.aligned16 = aligned16_ ? 1 : 0;
     const int t0 = tick();
-    if (dir)
-      k_pass_dir<NOUT><<<G, kBlock, dyn, st_>>>(in_, a);
+    if (dir && mapped && items == 8)
+      k_pass_dir<NOUT, 8, true><<<G, kBlock, dyn, st_>>>(in_, a);
+    else if (dir && mapped && items == 16)
+      k_pass_dir<NOUT, 16, true><<<G, kBlock, dyn, st_>>>(in_, a);
+    else if (dir && mapped)
+      k_pass_dir<NOUT, 12, true><<<G, kBlock, dyn, st_>>>(in_, a);
+    else if (dir && items == 8)
+      k_pass_dir<NOUT, 8, false><<<G, kBlock, dyn, st_>>>(in_, a);
+    else if (dir && items == 16)
+      k_pass_dir<NOUT, 16, false><<<G, kBlock, dyn, st_>>>(in_, a);
+    else if (dir)
+      k_pass_dir<NOUT, 12, false><<<G, kBlock, dyn, st_>>>(in_, a);
+    else if (sitems == 4)
+      k_pass_seg<NOUT, 4><<<G, kBlock, dyn, st_>>>(src->in(), a);
     else
-      k_pass_seg<NOUT><<<G, kBlock, dyn, st_>>>(src->in(), a);
+      k_pass_seg<NOUT, 8><<<G, kBlock, dyn, st_>>>(src->in(), a);
     tock(phase, t0);
     CU_TRY(cudaGetLastError());
     for (int c = 0; c < NOUT; ++c)
@@ -577,7 +601,6 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
     const int tv = tick();
     k_hook<<<gv, kBlock, 0, st_>>>(nr, minv, cur->base, parent_, msfoid_, ctx_->d_err);
     k_jump<<<gv, kBlock, 0, st_>>>(nr, parent_, ctx_->d_err);
-    k_jump_finish<<<gv, kBlock, 0, st_>>>(nr, parent_, ctx_->d_err);
     uint32_t* onext = Obuf_ + ooff;
     VertexScanArgs va{};
     va.n = nr;
@@ -603,7 +626,7 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
     k_vertex_count<<<gvs, kBlock, 0, st_>>>(va);
     k_vertex_write<<<gvs, kBlock, 0, st_>>>(va);
     uint32_t* R = Rbuf_ + roff;
-    k_map<<<gv, kBlock, 0, st_>>>(nr, minv, parent_, newid_, R);
+    k_map<<<gv, kBlock, 0, st_>>>(nr, minv, parent_, newid_, R, ctx_->d_err);
     tock(KAMSTA_PHASE_ROUND_VERTS, tv);
     // relabel + self-loop removal + compaction + next-round minimum
     SegList* nxt = new_list();
@@ -618,7 +641,7 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
     account(KAMSTA_PHASE_ROUND_VERTS,
             uint64_t(nr) * ((8 + 16 + 8 + 8) + 16 + (4 + 8 + 4) + (8 + 4 + 4)) + n_next * 16 +
                 added * 8,
-            7);
+            6);
     if (debug_) {
       fprintf(stderr, "[kamsta debug] round %u: m=%llu n=%u -> m'=%llu n'=%llu forest+=%llu\n", r,
               (unsigned long long)m, nr, (unsigned long long)nxt->total,
@@ -984,19 +1007,47 @@ kamsta_status Solve::run(Algo algo, kamsta_wedge* d_out, SolveOut* out) {
   CU_TRY(cudaGetDevice(&dev));
   CU_TRY(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
   aligned16_ = (reinterpret_cast<uintptr_t>(in_) & 15u) == 0;
+  if (cfg_.items_per_thread == 8 || cfg_.items_per_thread == 12 || cfg_.items_per_thread == 16)
+    dir_items_ = static_cast<int>(cfg_.items_per_thread);
+  if (cfg_.seg_items_per_thread == 4 || cfg_.seg_items_per_thread == 8)
+    seg_items_ = static_cast<int>(cfg_.seg_items_per_thread);
   samples_ = ctx_->d_samples;
   {
     const char* dbg = std::getenv("KAMSTA_DEBUG_CHECKS");
     debug_ = dbg && dbg[0] == '1';
   }
   {  // per device context; cheap
-    const int dd = static_cast<int>(kDirDynSmem), dr = static_cast<int>(kRecDynSmem);
-    CU_TRY(cudaFuncSetAttribute(k_pass_dir<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, dd));
-    CU_TRY(cudaFuncSetAttribute(k_pass_dir<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, dd));
-    CU_TRY(cudaFuncSetAttribute(k_pass_dir<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, dd));
-    CU_TRY(cudaFuncSetAttribute(k_pass_seg<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, dr));
-    CU_TRY(cudaFuncSetAttribute(k_pass_seg<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, dr));
-    CU_TRY(cudaFuncSetAttribute(k_pass_seg<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, dr));
+    const int dr = static_cast<int>(rec_dyn_smem(8)), dr4 = static_cast<int>(rec_dyn_smem(4));
+    const int d8 = static_cast<int>(dir_dyn_smem(8)), d12 = static_cast<int>(dir_dyn_smem(12)),
+              d16 = static_cast<int>(dir_dyn_smem(16));
+    const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+#define KAMSTA_DIR_ATTR(N, I, M, D) \
+  CU_TRY(cudaFuncSetAttribute(k_pass_dir<N, I, M>, attr, D))
+    KAMSTA_DIR_ATTR(1, 8, false, d8);
+    KAMSTA_DIR_ATTR(2, 8, false, d8);
+    KAMSTA_DIR_ATTR(3, 8, false, d8);
+    KAMSTA_DIR_ATTR(1, 12, false, d12);
+    KAMSTA_DIR_ATTR(2, 12, false, d12);
+    KAMSTA_DIR_ATTR(3, 12, false, d12);
+    KAMSTA_DIR_ATTR(1, 16, false, d16);
+    KAMSTA_DIR_ATTR(2, 16, false, d16);
+    KAMSTA_DIR_ATTR(3, 16, false, d16);
+    KAMSTA_DIR_ATTR(1, 8, true, d8);
+    KAMSTA_DIR_ATTR(2, 8, true, d8);
+    KAMSTA_DIR_ATTR(3, 8, true, d8);
+    KAMSTA_DIR_ATTR(1, 12, true, d12);
+    KAMSTA_DIR_ATTR(2, 12, true, d12);
+    KAMSTA_DIR_ATTR(3, 12, true, d12);
+    KAMSTA_DIR_ATTR(1, 16, true, d16);
+    KAMSTA_DIR_ATTR(2, 16, true, d16);
+    KAMSTA_DIR_ATTR(3, 16, true, d16);
+#undef KAMSTA_DIR_ATTR
+    CU_TRY(cudaFuncSetAttribute(k_pass_seg<1, 8>, attr, dr));
+    CU_TRY(cudaFuncSetAttribute(k_pass_seg<2, 8>, attr, dr));
+    CU_TRY(cudaFuncSetAttribute(k_pass_seg<3, 8>, attr, dr));
+    CU_TRY(cudaFuncSetAttribute(k_pass_seg<1, 4>, attr, dr4));
+    CU_TRY(cudaFuncSetAttribute(k_pass_seg<2, 4>, attr, dr4));
+    CU_TRY(cudaFuncSetAttribute(k_pass_seg<3, 4>, attr, dr4));
   }
   KS_TRY(alloc_fixed());
   CU_TRY(cudaEventRecord(ctx_->ev0, st_));

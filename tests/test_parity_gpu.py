@@ -224,3 +224,15 @@ def test_row_scan_contraction_is_used_and_exact(kamsta, oracle):
     got = kamsta.boruvka(e, kamsta.AlgorithmConfig(local_preprocessing=1), n=n, stats=st)
     _check(oracle, got, e, n)
     assert st["row_scans"] >= 1
+
+
+@pytest.mark.parametrize("items,seg", [(8, 8), (12, 4), (16, 8), (8, 4)])
+def test_tile_sizes_agree(kamsta, oracle, items, seg):
+    """The tiles (entries / records per thread) change the schedule only."""
+    n, m = 1 << 18, 1 << 22
+    e = oracle.gen_gnm(n, m, 91)
+    for lp in (0, 1):
+        cfg = kamsta.AlgorithmConfig(local_preprocessing=lp, items_per_thread=items,
+                                     seg_items_per_thread=seg)
+        _check(oracle, kamsta.boruvka(e, cfg, n=n), e, n)
+        _check(oracle, kamsta.filter_boruvka(e, cfg, n=n), e, n)
