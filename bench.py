@@ -57,6 +57,8 @@ def parse_args():
     p.add_argument("--no-geometric", action="store_true",
                    help="skip filter-Boruvka on RGG-2D / RHG (n=2^24, degree 16)")
     p.add_argument("--geo-log-n", type=int, default=24)
+    p.add_argument("--tiles", default="auto",
+                   help="first-pass x list-pass items per thread, e.g. 8x4; auto = time each")
     p.add_argument("--batch-graphs", type=int, default=4096)
     p.add_argument("--batch-budget-gb", type=float, default=64.0)
     p.add_argument("--batch-steps", type=int, default=3)
@@ -439,13 +441,17 @@ def main():
     # autotune the first-pass tile (entries per thread) on this workload:
     # one untimed solve per candidate, the fastest is used for every step
     tiles = {}
-    for items, seg in ((8, 8), (12, 8), (16, 8), (8, 4), (12, 4)):
+    cands = ((8, 8), (12, 8), (16, 8), (8, 4), (12, 4))
+    if args.tiles != "auto":
+        cands = (tuple(int(x) for x in args.tiles.split("x")),)
+    for items, seg in cands:
         c = K.AlgorithmConfig(local_preprocessing=K.LocalPreprocessing(args.local_preprocessing),
                               items_per_thread=items, seg_items_per_thread=seg)
-        ctx.boruvka_dev(d_edges.data_ptr(), md, n, d_out.data_ptr(), c, stream=sh)
         st = {}
-        ctx.boruvka_dev(d_edges.data_ptr(), md, n, d_out.data_ptr(), c, stream=sh, stats=st)
-        tiles[f"{items}x{seg}"] = st["device_ms"]
+        if len(cands) > 1:
+            ctx.boruvka_dev(d_edges.data_ptr(), md, n, d_out.data_ptr(), c, stream=sh)
+            ctx.boruvka_dev(d_edges.data_ptr(), md, n, d_out.data_ptr(), c, stream=sh, stats=st)
+        tiles[f"{items}x{seg}"] = st.get("device_ms", 0.0)
     best = min(tiles, key=tiles.get)
     best_items, best_seg = (int(x) for x in best.split("x"))
     cfg = K.AlgorithmConfig(local_preprocessing=K.LocalPreprocessing(args.local_preprocessing),

@@ -144,21 +144,36 @@ __device__ __forceinline__ void seg_tile_finish(const uint8_t (&cls)[ITEMS], uin
   for (int j = 0; j < ITEMS; ++j) offs[j] = 0;
   tile_rank<NOUT, ITEMS, kBlock>(cls, offs, s_rank, s_tot);
   uint32_t min_mask = 0;  // class-0 items whose minimum must be fed
+  // one pass over the items; the class picks segment, size and capacity
+  // (all below 2^32: a segment holds at most one CTA's chunk)
+  Rec* segc[NOUT];
+  uint32_t runc[NOUT], capc[NOUT];
 #pragma unroll
   for (int c = 0; c < NOUT; ++c) {
-    const uint64_t cap = p.out[c].cap;
-    Rec* const seg = p.out[c].base + static_cast<uint64_t>(blockIdx.x) * cap;
+    capc[c] = static_cast<uint32_t>(p.out[c].cap);
+    segc[c] = p.out[c].base + static_cast<uint64_t>(blockIdx.x) * p.out[c].cap;
+    runc[c] = static_cast<uint32_t>(run[c]);
+  }
 #pragma unroll
-    for (int j = 0; j < ITEMS; ++j) {
-      if (cls[j] != c) continue;
-      const uint64_t local = run[c] + offs[j];
-      if (local >= cap) {
-        atomicOr(p.err, kErrOverflow);
-        continue;
+  for (int j = 0; j < ITEMS; ++j) {
+    const uint8_t c = cls[j];
+    if (c == 0xff) continue;
+    Rec* sg = segc[0];
+    uint32_t rb = runc[0], cp = capc[0];
+#pragma unroll
+    for (int k = 1; k < NOUT; ++k)
+      if (c == k) {
+        sg = segc[k];
+        rb = runc[k];
+        cp = capc[k];
       }
-      seg[local] = rec(j * kBlock + threadIdx.x);
-      if (c == 0) min_mask |= 1u << j;
+    const uint32_t local = rb + offs[j];
+    if (local >= cp) {
+      atomicOr(p.err, kErrOverflow);
+      continue;
     }
+    sg[local] = rec(j * kBlock + threadIdx.x);
+    if (c == 0) min_mask |= 1u << j;
   }
   if (p.minval != nullptr && min_mask) {
     const uint64_t seg0 = static_cast<uint64_t>(blockIdx.x) * p.out[0].cap + run[0];
