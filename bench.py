@@ -64,7 +64,7 @@ def parse_args():
     p.add_argument("--batch-steps", type=int, default=3)
     p.add_argument("--serve-requests", type=int, default=20000)
     p.add_argument("--serve-rate", type=float, default=0.0,
-                   help="Poisson arrival rate (requests/s); 0 = half the batched graphs/s")
+                   help="Poisson arrival rate (requests/s); 0 = 0.35 x the batched graphs/s")
     p.add_argument("--serve-plain-requests", type=int, default=2000,
                    help="requests replayed through sequential plain solves")
     return p.parse_args()
@@ -326,18 +326,16 @@ def run_batch(args, K, ctx, sh, seed):
             "weights": weights, "graphs_per_s": len(specs) / tb, "seq_ms": seq_ms}
 
 
-def run_serving(args, K, ctx, sh, b):
-    """Poisson arrivals of requests drawn from the batch graph mix, served by
-    kamsta_server (continuous batching under the memory budget), against the
-    same arrivals replayed through sequential plain solves."""
+def serve_once(args, K, b, rate, R, seed):
+    """R Poisson arrivals at `rate` drawn from the batch graphs, served by a
+    2-worker kamsta_server under the memory budget.  Returns the result dict
+    and the arrival times / graph indices (for the plain replay)."""
     import numpy as np
     import torch
     from kamsta_gb300 import workloads as W
     specs, edges, counts, weights = b["specs"], b["edges"], b["counts"], b["weights"]
-    rng = np.random.default_rng(args.seed + 17)
-    R = args.serve_requests
+    rng = np.random.default_rng(seed)
     gidx = rng.integers(0, len(specs), size=R)
-    rate = args.serve_rate or 0.5 * b["graphs_per_s"]
     arrivals = np.cumsum(rng.exponential(1.0 / rate, size=R))
     # one output region per request (requests of the same graph may overlap)
     ns = np.array([max(specs[g].n, 1) for g in gidx], dtype=np.int64)
@@ -358,7 +356,6 @@ def run_serving(args, K, ctx, sh, b):
     th = threading.Thread(target=collector, daemon=True)
     th.start()
     t_start = time.perf_counter()
-    sub_t = np.empty(R)
     for i in range(R):
         target = t_start + arrivals[i]
         while True:
@@ -368,11 +365,9 @@ def run_serving(args, K, ctx, sh, b):
             if target - now > 2e-3:
                 time.sleep(target - now - 1e-3)
         g = int(gidx[i])
-        sub_t[i] = time.perf_counter()
         srv.submit(edges[g].data_ptr(), counts[g], specs[g].n, base + 12 * int(offs[i]), tag=i)
     th.join(timeout=600)
     stop.set()
-    t_end = time.perf_counter()
     sst = srv.stats()
     srv.close()
     assert len(done) == R, f"serving: {len(done)} of {R} requests finished"
@@ -381,13 +376,40 @@ def run_serving(args, K, ctx, sh, b):
                 for i in range(R))
     span = max(done[i]["finish_us"] for i in range(R)) / 1e6 - min(
         done[i]["submit_us"] for i in range(R)) / 1e6
-    res = {"workload": f"{R} requests, Poisson arrivals, graphs drawn from the batch mix",
-           "rate_per_s": rate, "requests": R, "throughput": R / span, "unit": "graphs/s",
+    res = {"rate_per_s": rate, "requests": R, "throughput": R / span, "unit": "graphs/s",
            **W.percentiles(lat), "mean_ms": float(np.mean(lat)),
            "mean_batch": float(np.mean([done[i]["batch_size"] for i in range(R)])),
-           "waves": sst["waves"], "workers": 2, "budget_gb": args.batch_budget_gb,
-           "exact_vs_batch": bool(exact)}
+           "waves": sst["waves"], "exact_vs_batch": bool(exact)}
+    del out
+    return res, arrivals, gidx
+
+
+def run_serving(args, K, ctx, sh, b):
+    """Poisson arrivals of requests drawn from the batch graph mix, served by
+    kamsta_server (continuous batching under the memory budget), against the
+    same arrivals replayed through sequential plain solves; plus a light and
+    a heavy load point."""
+    import numpy as np
+    import torch
+    from kamsta_gb300 import workloads as W
+    specs, edges, counts = b["specs"], b["edges"], b["counts"]
+    R = args.serve_requests
+    rate = args.serve_rate or 0.35 * b["graphs_per_s"]
+    res, arrivals, gidx = serve_once(args, K, b, rate, R, args.seed + 17)
+    res = {"workload": f"{R} requests, Poisson arrivals, graphs drawn from the batch mix",
+           **res, "workers": 2, "budget_gb": args.batch_budget_gb,
+           "rate_rule": "0.35 x the batched graphs/s unless --serve-rate is given"}
+    if not args.serve_rate:
+        sweep = {}
+        for f in (0.2, 0.5):
+            r, _, _ = serve_once(args, K, b, f * b["graphs_per_s"], R // 2, args.seed + 29)
+            sweep[f"{f:.2f}x_batch_rate"] = {k: r[k] for k in
+                                             ("rate_per_s", "requests", "throughput", "p50_ms",
+                                              "p99_ms", "p99_9_ms", "mean_batch",
+                                              "exact_vs_batch")}
+        res["load_points"] = sweep
     # sequential plain solves under the same arrivals (FIFO, one at a time)
+    cfg = K.AlgorithmConfig(local_preprocessing=K.LocalPreprocessing(args.local_preprocessing))
     P = min(args.serve_plain_requests, R)
     lat_p = []
     t_free = 0.0
