@@ -96,9 +96,9 @@ typedef struct kamsta_cfg {
   uint32_t flags;              /* KAMSTA_FLAG_*                              */
   uint32_t dedupe_ratio;       /* auto dedupe when m_r > ratio * n_r (0=off) */
   uint64_t seed;               /* pivot-sampling seed                        */
-  uint32_t seg_items_per_thread; /* list-pass tile: 4 or 8 records per      */
-                               /* thread (0 = 4)                             */
-  uint32_t items_per_thread;   /* first-pass tile: 8, 12 or 16 directed      */
+  uint32_t seg_items_per_thread; /* list-pass tile: 2, 4 or 8 records per   */
+                               /* thread (0 = 2)                             */
+  uint32_t items_per_thread;   /* first-pass tile: 6, 8 or 12 directed       */
                                /* entries per thread (0 = 8)                 */
 } kamsta_cfg;
 

@@ -24,14 +24,14 @@ kamsta_status check_cfg(const kamsta_cfg* cfg) {
     return cfg->compression == KAMSTA_SEVEN_BIT_DIFF_ENCODING ? KAMSTA_E_UNSUPPORTED
                                                                : KAMSTA_E_INPUT;
   }
-  if (cfg->items_per_thread != 0 && cfg->items_per_thread != 8 && cfg->items_per_thread != 12 &&
-      cfg->items_per_thread != 16) {
-    set_error("items_per_thread: 0, 8, 12 or 16");
+  if (cfg->items_per_thread != 0 && cfg->items_per_thread != 6 && cfg->items_per_thread != 8 &&
+      cfg->items_per_thread != 12) {
+    set_error("items_per_thread: 0, 6, 8 or 12");
     return KAMSTA_E_INPUT;
   }
-  if (cfg->seg_items_per_thread != 0 && cfg->seg_items_per_thread != 4 &&
-      cfg->seg_items_per_thread != 8) {
-    set_error("seg_items_per_thread: 0, 4 or 8");
+  if (cfg->seg_items_per_thread != 0 && cfg->seg_items_per_thread != 2 &&
+      cfg->seg_items_per_thread != 4 && cfg->seg_items_per_thread != 8) {
+    set_error("seg_items_per_thread: 0, 2, 4 or 8");
     return KAMSTA_E_INPUT;
   }
   if (cfg->local_preprocessing < KAMSTA_NO_PREPROCESSING ||

@@ -18,7 +18,7 @@ namespace kamsta {
 
 constexpr int kBlock = 256;
 constexpr int kItemsDir = 8;    // directed 12-byte records per thread (default tile)
-constexpr int kItemsRec = 4;    // 16-byte records per thread (default tile)
+constexpr int kItemsRec = 2;    // 16-byte records per thread (default tile)
 constexpr int kItemsVtx = 8;    // vertices per thread in the vertex scans
 constexpr int kMaxOut = 3;      // weight classes materialised by one pass
 
@@ -240,8 +240,8 @@ __device__ __forceinline__ void seg_pass_end(const uint64_t (&run)[NOUT], uint32
 // not 16-byte aligned is read with plain loads throughout.  Striped layout:
 // item j of thread t is tile item j*kBlock + t, so consecutive lanes read
 // consecutive records (conflict-free) and write consecutive output slots.
-// Items per thread is a tile-size knob (kamsta_cfg.items_per_thread: 8, 12
-// or 16; 8 by default, the fastest on GB300 at 2^26/2^30).
+// Items per thread is a tile-size knob (kamsta_cfg.items_per_thread: 6, 8
+// or 12; 8 by default, the fastest on GB300 at 2^26/2^30).
 constexpr uint32_t dir_tile(int items) { return static_cast<uint32_t>(items) * kBlock; }
 constexpr size_t dir_dyn_smem(int items) { return 2ull * dir_tile(items) * 3 * sizeof(uint32_t); }
 constexpr uint32_t kDirTile = dir_tile(kItemsDir);
@@ -432,10 +432,10 @@ __device__ __forceinline__ uint32_t seg_find(const uint64_t* prefix, uint32_t ns
   return lo;
 }
 
-// ITEMS (records per thread, 4 or 8) is a tile knob: smaller tiles give more
-// resident CTAs for the latency-bound relabel passes.
+// ITEMS (records per thread, 2, 4 or 8) is a tile knob: smaller tiles give
+// more resident CTAs for the latency-bound relabel passes.
 template <int NOUT, int ITEMS = kItemsRec>
-__global__ void __launch_bounds__(kBlock, ITEMS <= 4 ? 4 : 3)
+__global__ void __launch_bounds__(kBlock, ITEMS <= 2 ? 5 : ITEMS <= 4 ? 4 : 3)
     k_pass_seg(SegIn in, PassArgs p) {
   constexpr uint32_t kRecTile = rec_tile(ITEMS);
   constexpr int kItemsRec = ITEMS;

@@ -217,8 +217,8 @@ class Solve {
   bool tolerate_overflow_ = false;
   uint32_t launches_ = 0, rounds_ = 0, levels_ = 0, dedupe_passes_ = 0, row_scans_ = 0;
   bool final_contraction_ = false;  // rounds() of the last contraction (boruvka)
-  int dir_items_ = kItemsDir;        // items per thread of k_pass_dir (8, 12, 16)
-  int seg_items_ = kItemsRec;        // records per thread of k_pass_seg (4, 8)
+  int dir_items_ = kItemsDir;        // items per thread of k_pass_dir (6, 8, 12)
+  int seg_items_ = kItemsRec;        // records per thread of k_pass_seg (2, 4, 8)
   uint64_t alg_bytes_ = 0;
   double phase_ms_[KAMSTA_PHASES] = {};
   uint64_t phase_bytes_[KAMSTA_PHASES] = {};
@@ -410,13 +410,14 @@ kamsta_status Solve::pass(int phase, const SegList* src, const uint32_t* map, ui
   const size_t dyn = dir ? dir_dyn_smem(items) : rec_dyn_smem(sitems);
   const bool mapped = map != nullptr;
   const int per_sm =
-      !dir ? (sitems == 4 ? blocks_per_sm(k_pass_seg<NOUT, 4>, dyn)
+      !dir ? (sitems == 2 ? blocks_per_sm(k_pass_seg<NOUT, 2>, dyn)
+              : sitems == 4 ? blocks_per_sm(k_pass_seg<NOUT, 4>, dyn)
                           : blocks_per_sm(k_pass_seg<NOUT, 8>, dyn))
       : mapped ? (items == 8    ? blocks_per_sm(k_pass_dir<NOUT, 8, true>, dyn)
-                  : items == 16 ? blocks_per_sm(k_pass_dir<NOUT, 16, true>, dyn)
+                  : items == 6  ? blocks_per_sm(k_pass_dir<NOUT, 6, true>, dyn)
                                 : blocks_per_sm(k_pass_dir<NOUT, 12, true>, dyn))
                : (items == 8    ? blocks_per_sm(k_pass_dir<NOUT, 8, false>, dyn)
-                  : items == 16 ? blocks_per_sm(k_pass_dir<NOUT, 16, false>, dyn)
+                  : items == 6  ? blocks_per_sm(k_pass_dir<NOUT, 6, false>, dyn)
                                 : blocks_per_sm(k_pass_dir<NOUT, 12, false>, dyn));
   const uint64_t gmax = std::min<uint64_t>(kMaxSeg, uint64_t(per_sm) * sms_);
   uint64_t chunk = std::max<uint64_t>(1, (total + gmax - 1) / gmax);
@@ -460,16 +461,18 @@ kamsta_status Solve::pass(int phase, const SegList* src, const uint32_t* map, ui
     const int t0 = tick();
     if (dir && mapped && items == 8)
       k_pass_dir<NOUT, 8, true><<<G, kBlock, dyn, st_>>>(in_, a);
-    else if (dir && mapped && items == 16)
-      k_pass_dir<NOUT, 16, true><<<G, kBlock, dyn, st_>>>(in_, a);
+    else if (dir && mapped && items == 6)
+      k_pass_dir<NOUT, 6, true><<<G, kBlock, dyn, st_>>>(in_, a);
     else if (dir && mapped)
       k_pass_dir<NOUT, 12, true><<<G, kBlock, dyn, st_>>>(in_, a);
     else if (dir && items == 8)
       k_pass_dir<NOUT, 8, false><<<G, kBlock, dyn, st_>>>(in_, a);
-    else if (dir && items == 16)
-      k_pass_dir<NOUT, 16, false><<<G, kBlock, dyn, st_>>>(in_, a);
+    else if (dir && items == 6)
+      k_pass_dir<NOUT, 6, false><<<G, kBlock, dyn, st_>>>(in_, a);
     else if (dir)
       k_pass_dir<NOUT, 12, false><<<G, kBlock, dyn, st_>>>(in_, a);
+    else if (sitems == 2)
+      k_pass_seg<NOUT, 2><<<G, kBlock, dyn, st_>>>(src->in(), a);
     else if (sitems == 4)
       k_pass_seg<NOUT, 4><<<G, kBlock, dyn, st_>>>(src->in(), a);
     else
@@ -1007,9 +1010,10 @@ kamsta_status Solve::run(Algo algo, kamsta_wedge* d_out, SolveOut* out) {
   CU_TRY(cudaGetDevice(&dev));
   CU_TRY(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
   aligned16_ = (reinterpret_cast<uintptr_t>(in_) & 15u) == 0;
-  if (cfg_.items_per_thread == 8 || cfg_.items_per_thread == 12 || cfg_.items_per_thread == 16)
+  if (cfg_.items_per_thread == 6 || cfg_.items_per_thread == 8 || cfg_.items_per_thread == 12)
     dir_items_ = static_cast<int>(cfg_.items_per_thread);
-  if (cfg_.seg_items_per_thread == 4 || cfg_.seg_items_per_thread == 8)
+  if (cfg_.seg_items_per_thread == 2 || cfg_.seg_items_per_thread == 4 ||
+      cfg_.seg_items_per_thread == 8)
     seg_items_ = static_cast<int>(cfg_.seg_items_per_thread);
   samples_ = ctx_->d_samples;
   {
@@ -1019,7 +1023,7 @@ kamsta_status Solve::run(Algo algo, kamsta_wedge* d_out, SolveOut* out) {
   {  // per device context; cheap
     const int dr = static_cast<int>(rec_dyn_smem(8)), dr4 = static_cast<int>(rec_dyn_smem(4));
     const int d8 = static_cast<int>(dir_dyn_smem(8)), d12 = static_cast<int>(dir_dyn_smem(12)),
-              d16 = static_cast<int>(dir_dyn_smem(16));
+              d6 = static_cast<int>(dir_dyn_smem(6));
     const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
 #define KAMSTA_DIR_ATTR(N, I, M, D) \
   CU_TRY(cudaFuncSetAttribute(k_pass_dir<N, I, M>, attr, D))
@@ -1029,23 +1033,27 @@ kamsta_status Solve::run(Algo algo, kamsta_wedge* d_out, SolveOut* out) {
     KAMSTA_DIR_ATTR(1, 12, false, d12);
     KAMSTA_DIR_ATTR(2, 12, false, d12);
     KAMSTA_DIR_ATTR(3, 12, false, d12);
-    KAMSTA_DIR_ATTR(1, 16, false, d16);
-    KAMSTA_DIR_ATTR(2, 16, false, d16);
-    KAMSTA_DIR_ATTR(3, 16, false, d16);
+    KAMSTA_DIR_ATTR(1, 6, false, d6);
+    KAMSTA_DIR_ATTR(2, 6, false, d6);
+    KAMSTA_DIR_ATTR(3, 6, false, d6);
     KAMSTA_DIR_ATTR(1, 8, true, d8);
     KAMSTA_DIR_ATTR(2, 8, true, d8);
     KAMSTA_DIR_ATTR(3, 8, true, d8);
     KAMSTA_DIR_ATTR(1, 12, true, d12);
     KAMSTA_DIR_ATTR(2, 12, true, d12);
     KAMSTA_DIR_ATTR(3, 12, true, d12);
-    KAMSTA_DIR_ATTR(1, 16, true, d16);
-    KAMSTA_DIR_ATTR(2, 16, true, d16);
-    KAMSTA_DIR_ATTR(3, 16, true, d16);
+    KAMSTA_DIR_ATTR(1, 6, true, d6);
+    KAMSTA_DIR_ATTR(2, 6, true, d6);
+    KAMSTA_DIR_ATTR(3, 6, true, d6);
 #undef KAMSTA_DIR_ATTR
     CU_TRY(cudaFuncSetAttribute(k_pass_seg<1, 8>, attr, dr));
     CU_TRY(cudaFuncSetAttribute(k_pass_seg<2, 8>, attr, dr));
     CU_TRY(cudaFuncSetAttribute(k_pass_seg<3, 8>, attr, dr));
     CU_TRY(cudaFuncSetAttribute(k_pass_seg<1, 4>, attr, dr4));
+    const int dr2 = static_cast<int>(rec_dyn_smem(2));
+    CU_TRY(cudaFuncSetAttribute(k_pass_seg<1, 2>, attr, dr2));
+    CU_TRY(cudaFuncSetAttribute(k_pass_seg<2, 2>, attr, dr2));
+    CU_TRY(cudaFuncSetAttribute(k_pass_seg<3, 2>, attr, dr2));
     CU_TRY(cudaFuncSetAttribute(k_pass_seg<2, 4>, attr, dr4));
     CU_TRY(cudaFuncSetAttribute(k_pass_seg<3, 4>, attr, dr4));
   }

@@ -226,7 +226,7 @@ def test_row_scan_contraction_is_used_and_exact(kamsta, oracle):
     assert st["row_scans"] >= 1
 
 
-@pytest.mark.parametrize("items,seg", [(8, 8), (12, 4), (16, 8), (8, 4)])
+@pytest.mark.parametrize("items,seg", [(8, 8), (12, 4), (6, 2), (8, 4)])
 def test_tile_sizes_agree(kamsta, oracle, items, seg):
     """The tiles (entries / records per thread) change the schedule only."""
     n, m = 1 << 18, 1 << 22
