@@ -55,7 +55,9 @@ def parse_args():
     p.add_argument("--no-batch", action="store_true", help="skip the batched-solve workload")
     p.add_argument("--no-serving", action="store_true", help="skip the serving workload")
     p.add_argument("--no-geometric", action="store_true",
-                   help="skip filter-Boruvka on RGG-2D / RHG (n=2^24, degree 16)")
+                   help="skip filter-Boruvka on the other graph families (n=2^24)")
+    p.add_argument("--families", default="rgg2d,rhg,rgg3d,rmat,grid2d",
+                   help="graph families of the geometric / skewed workload")
     p.add_argument("--geo-log-n", type=int, default=24)
     p.add_argument("--tiles", default="auto",
                    help="first-pass x list-pass items per thread, e.g. 8x4; auto = time each")
@@ -202,24 +204,50 @@ def run_reference(args, rep):
     return 0
 
 
-def run_geometric(args, K, ctx, sh, seed):
-    """filter-Boruvka on the geometric / skewed families: RGG-2D and RHG
-    (gamma 3), n=2^geo_log_n, average degree 16, generated on the device."""
+def _family_inputs(ctx, fam, L, seed, sh):
+    """Device generator call of one family at 2^L vertices (count, then
+    write); returns (edges, directed entries, n, description)."""
     import math
     import torch
-    n = 1 << args.geo_log_n
+    n = 1 << L
+    if fam == "rgg2d":
+        r = math.sqrt(16.0 / (math.pi * n))
+        gen = lambda **kw: ctx.gen_rgg2d_dev(n, r, seed, 254, stream=sh, **kw)  # noqa: E731
+        desc = f"rgg2d n=2^{L}, average degree 16"
+    elif fam == "rhg":
+        gen = lambda **kw: ctx.gen_rhg_dev(n, 3.0, 16.0, seed, 254, stream=sh, **kw)  # noqa: E731
+        desc = f"rhg n=2^{L}, average degree 16, gamma 3"
+    elif fam == "rgg3d":
+        r = (3.0 * 16.0 / (4.0 * math.pi * n)) ** (1.0 / 3.0)
+        gen = lambda **kw: ctx.gen_rgg3d_dev(n, r, seed, 254, stream=sh, **kw)  # noqa: E731
+        desc = f"rgg3d n=2^{L}, average degree 16"
+    elif fam == "rmat":
+        gen = lambda **kw: ctx.gen_rmat_dev(L, 8 << L, seed, 0.57, 0.19, 0.19, 254,  # noqa: E731
+                                            stream=sh, **kw)
+        desc = f"rmat n=2^{L}, 2^{L + 3} samples (a, b, c) = (0.57, 0.19, 0.19), ids unpermuted"
+    elif fam == "grid2d":
+        side = 1 << (L // 2)
+        n = side * (n // side)
+        gen = lambda **kw: ctx.gen_grid_dev(side, n // side, 1, 1.0, True, seed, 254,  # noqa: E731
+                                            stream=sh, **kw)
+        desc = f"grid2d {side} x {n // side} periodic, p = 1"
+    else:
+        raise ValueError(fam)
+    md = gen()
+    d = torch.empty((max(md, 1), 3), dtype=torch.int32, device="cuda")
+    gen(d_out=d.data_ptr(), capacity=md)
+    return d, md, n, desc + ", weights U[1,254]"
+
+
+def run_geometric(args, K, ctx, sh, seed):
+    """filter-Boruvka on the geometric / skewed families (RGG-2D, RHG gamma 3,
+    RGG-3D, R-MAT, periodic 2-D grid) at n=2^geo_log_n, generated on the
+    device."""
+    import torch
     res = {}
-    for fam in ("rgg2d", "rhg"):
+    for fam in args.families.split(","):
         t0 = time.perf_counter()
-        if fam == "rgg2d":
-            r = math.sqrt(16.0 / (math.pi * n))
-            md = ctx.gen_rgg2d_dev(n, r, seed, 254, stream=sh)
-            d = torch.empty((md, 3), dtype=torch.int32, device="cuda")
-            ctx.gen_rgg2d_dev(n, r, seed, 254, d.data_ptr(), md, stream=sh)
-        else:
-            md = ctx.gen_rhg_dev(n, 3.0, 16.0, seed, 254, stream=sh)
-            d = torch.empty((md, 3), dtype=torch.int32, device="cuda")
-            ctx.gen_rhg_dev(n, 3.0, 16.0, seed, 254, d.data_ptr(), md, stream=sh)
+        d, md, n, desc = _family_inputs(ctx, fam, args.geo_log_n, seed, sh)
         torch.cuda.synchronize()
         gen_s = time.perf_counter() - t0
         out = torch.empty((n, 3), dtype=torch.int32, device="cuda")
@@ -239,8 +267,7 @@ def run_geometric(args, K, ctx, sh, seed):
             ws.add(st["total_weight"])
             ks.add(k)
         med = statistics.median(ms)
-        res[fam] = {"workload": f"{fam} n=2^{args.geo_log_n}, average degree 16"
-                                + (", gamma 3" if fam == "rhg" else "") + ", weights U[1,254]",
+        res[fam] = {"workload": desc,
                     "algorithm": "filter_boruvka (filter_hybridBoruvka), default config",
                     "directed_entries": md, "value": md / (med / 1e3), "unit": UNIT,
                     "ms_per_step": med, "forest_edges": ks.pop(), "forest_weight": ws.pop(),

@@ -397,7 +397,7 @@ kamsta_status kamsta_gen_gnm_dev(kamsta_ctx* ctx, uint32_t n, uint64_t m,
  * edge count is data dependent: with d_out == NULL the call only counts
  * (*m_directed_out = entries needed); with capacity < that count it returns
  * KAMSTA_E_INPUT and the count.  Stand-in for get_rgg2D
- * (benchmarks/mst_benchmarks.hpp:134-142). */
+ * (benchmarks/mst_benchmarks.hpp:133-139). */
 kamsta_status kamsta_gen_rgg2d_dev(kamsta_ctx* ctx, uint32_t n, double radius,
                                    uint64_t seed, uint32_t max_weight,
                                    kamsta_wedge* d_out, uint64_t capacity,
@@ -407,11 +407,41 @@ kamsta_status kamsta_gen_rgg2d_dev(kamsta_ctx* ctx, uint32_t n, double radius,
  * degree.  Counting / capacity convention as kamsta_gen_rgg2d_dev.  The
  * per-point coordinates are computed on the host with the C library's
  * acosh/exp/sinh; the pair test runs on the device.  Stand-in for get_rhg
- * (benchmarks/mst_benchmarks.hpp:143-158). */
+ * (benchmarks/mst_benchmarks.hpp:152-158). */
 kamsta_status kamsta_gen_rhg_dev(kamsta_ctx* ctx, uint32_t n, double gamma,
                                  double avg_degree, uint64_t seed, uint32_t max_weight,
                                  kamsta_wedge* d_out, uint64_t capacity,
                                  uint64_t* m_directed_out, kamsta_stream stream);
+/* Lattice of x * y * z vertices (z = 1: the 2-D grid), vertex (i, j, k) =
+ * id (k y + j) x + i, joined to its -1 / +1 steps along each axis (modulo
+ * the side when `periodic`); each edge kept with probability p (p >= 1: all,
+ * as the reference's benchmark calls it).  Counting / capacity convention as
+ * kamsta_gen_rgg2d_dev.  Stand-in for get_grid2D / get_grid3D
+ * (benchmarks/mst_benchmarks.hpp:159-180). */
+kamsta_status kamsta_gen_grid_dev(kamsta_ctx* ctx, uint32_t x, uint32_t y, uint32_t z,
+                                  double p, int periodic, uint64_t seed,
+                                  uint32_t max_weight, kamsta_wedge* d_out,
+                                  uint64_t capacity, uint64_t* m_directed_out,
+                                  kamsta_stream stream);
+/* 3-D random geometric graph in the unit cube (radius in [0, 1]; for an
+ * expected degree d away from the border, radius = cbrt(3 d / (4 pi n))).
+ * Counting / capacity convention as kamsta_gen_rgg2d_dev.  Stand-in for
+ * get_rgg3D (benchmarks/mst_benchmarks.hpp:140-146). */
+kamsta_status kamsta_gen_rgg3d_dev(kamsta_ctx* ctx, uint32_t n, double radius,
+                                   uint64_t seed, uint32_t max_weight,
+                                   kamsta_wedge* d_out, uint64_t capacity,
+                                   uint64_t* m_directed_out, kamsta_stream stream);
+/* R-MAT graph on 2^log_n vertices (log_n <= 31): `samples` (< 2^32 - 4096)
+ * recursive quadrant descents with probabilities a, b, c and d = 1 - a - b -
+ * c (Graph 500: 0.57, 0.19, 0.19); the graph = the distinct pairs u != v,
+ * ids not permuted (the hubs have the smallest ids).  Counting / capacity
+ * convention as kamsta_gen_rgg2d_dev.  Stand-in for
+ * get_rmat_edges_evenly_distributed (benchmarks/mst_benchmarks.hpp:147-151). */
+kamsta_status kamsta_gen_rmat_dev(kamsta_ctx* ctx, uint32_t log_n, uint64_t samples,
+                                  double a, double b, double c, uint64_t seed,
+                                  uint32_t max_weight, kamsta_wedge* d_out,
+                                  uint64_t capacity, uint64_t* m_directed_out,
+                                  kamsta_stream stream);
 
 #ifdef __cplusplus
 } /* extern "C" */

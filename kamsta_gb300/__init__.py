@@ -392,6 +392,40 @@ class Context:
                                        int(capacity), C.byref(cnt), C.c_void_p(stream or 0)))
         return int(cnt.value)
 
+    def gen_grid_dev(self, x: int, y: int, z: int = 1, p: float = 1.0, periodic: bool = True,
+                     seed: int = 1, max_weight: int = 254, d_out: int = 0, capacity: int = 0,
+                     stream=0) -> int:
+        """Device lattice x * y * z (z = 1: the 2-D grid), +-1 steps along
+        each axis, wrapping when `periodic`, each edge kept with probability
+        p.  With d_out == 0 it only counts; returns the directed entries."""
+        cnt = C.c_uint64(0)
+        check(lib().kamsta_gen_grid_dev(self._h, int(x), int(y), int(z), float(p), int(periodic),
+                                        int(seed), int(max_weight), C.c_void_p(d_out or 0),
+                                        int(capacity), C.byref(cnt), C.c_void_p(stream or 0)))
+        return int(cnt.value)
+
+    def gen_rgg3d_dev(self, n: int, radius: float, seed: int, max_weight: int = 254,
+                      d_out: int = 0, capacity: int = 0, stream=0) -> int:
+        """Device 3-D random geometric graph in the unit cube.  With
+        d_out == 0 it only counts; returns the directed entries."""
+        cnt = C.c_uint64(0)
+        check(lib().kamsta_gen_rgg3d_dev(self._h, int(n), float(radius), int(seed),
+                                         int(max_weight), C.c_void_p(d_out or 0), int(capacity),
+                                         C.byref(cnt), C.c_void_p(stream or 0)))
+        return int(cnt.value)
+
+    def gen_rmat_dev(self, log_n: int, samples: int, seed: int, a: float = 0.57,
+                     b: float = 0.19, c: float = 0.19, max_weight: int = 254, d_out: int = 0,
+                     capacity: int = 0, stream=0) -> int:
+        """Device R-MAT graph on 2^log_n vertices from `samples` samples.
+        With d_out == 0 it only counts; returns the directed entries."""
+        cnt = C.c_uint64(0)
+        check(lib().kamsta_gen_rmat_dev(self._h, int(log_n), int(samples), float(a), float(b),
+                                        float(c), int(seed), int(max_weight),
+                                        C.c_void_p(d_out or 0), int(capacity), C.byref(cnt),
+                                        C.c_void_p(stream or 0)))
+        return int(cnt.value)
+
     def load_wedge9_dev(self, paths, symmetrize: bool = True, stream=0):
         """Stream the reference's 9-byte binary edge files to the device.
         Returns (edges tensor (m, 3) int32 on cuda, m_directed, n)."""

@@ -159,6 +159,11 @@ SIGNATURES = {
     "kamsta_gen_rgg2d_dev": (I32, [P, U32, C.c_double, U64, U32, P, U64, C.POINTER(U64), P]),
     "kamsta_gen_rhg_dev": (I32, [P, U32, C.c_double, C.c_double, U64, U32, P, U64,
                                  C.POINTER(U64), P]),
+    "kamsta_gen_grid_dev": (I32, [P, U32, U32, U32, C.c_double, C.c_int, U64, U32, P, U64,
+                                  C.POINTER(U64), P]),
+    "kamsta_gen_rgg3d_dev": (I32, [P, U32, C.c_double, U64, U32, P, U64, C.POINTER(U64), P]),
+    "kamsta_gen_rmat_dev": (I32, [P, U32, U64, C.c_double, C.c_double, C.c_double, U64, U32, P,
+                                  U64, C.POINTER(U64), P]),
     "kamsta_mst_boruvka_noalloc": (I32, [P, U64, U32, P, C.POINTER(U64), C.POINTER(U64), P]),
     "kamsta_mst_batch_dev": (I32, [P, C.POINTER(GraphDesc), U32, C.POINTER(Cfg), U64,
                                    C.POINTER(BatchStats), P]),

@@ -1,6 +1,6 @@
 // gen_rhg.cu -- threshold random hyperbolic graph generator.
 //
-// Stand-in for KaGen's get_rhg (benchmarks/mst_benchmarks.hpp:143-158), which
+// Stand-in for KaGen's get_rhg (benchmarks/mst_benchmarks.hpp:152-158), which
 // the reference tree does not vendor; the reference exposes --gamma
 // (mst_benchmarks.hpp:71).  Definition (shared with the oracle's CPU
 // generator, oracle/oracle.cpp):
@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "gen_scratch.cuh"
 #include "solver.cuh"
 #include "sort_gen.cuh"
 
@@ -178,33 +179,6 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-struct DevBuf {
-  void* p = nullptr;
-  cudaStream_t st = nullptr;
-  cudaMemPool_t pool = nullptr;
-  ~DevBuf() {
-    if (p) {
-      if (pool) cudaFreeAsync(p, st);
-      else cudaFree(p);
-    }
-  }
-  template <typename T>
-  cudaError_t alloc(kamsta_ctx* ctx, cudaStream_t s, T** out, uint64_t count) {
-    st = s;
-    pool = ctx ? ctx->pool : nullptr;
-    const size_t bytes = std::max<uint64_t>(count, 1) * sizeof(T);
-    cudaError_t e = pool ? cudaMallocFromPoolAsync(&p, bytes, pool, s) : cudaMalloc(&p, bytes);
-    *out = static_cast<T*>(p);
-    return e;
-  }
-};
-
-#define RHG_TRY(x)                                        \
-  do {                                                    \
-    const cudaError_t e_ = (x);                           \
-    if (e_ != cudaSuccess) return cuda_status(e_, #x);    \
-  } while (0)
-
 }  // namespace
 
 kamsta_status gen_rhg(kamsta_ctx* ctx, uint32_t n, double gamma, double avg_degree, uint64_t seed,
@@ -258,56 +232,56 @@ kamsta_status gen_rhg(kamsta_ctx* ctx, uint32_t n, double gamma, double avg_degr
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int grid = sms * 8;
-  DevBuf bk, bk2, bp, bp2, bin4, bout4, bst, bdeg, boff, bcnt, bstat, bsmall;
+  GenBuf bk, bk2, bp, bp2, bin4, bout4, bst, bdeg, boff, bcnt, bstat, bsmall;
   uint64_t *keys, *keys2, *status;
   uint32_t *perm, *perm2, *bstart, *deg, *off, *counts;
   double *in4, *out4;
   unsigned long long* small;
-  RHG_TRY(bk.alloc(ctx, st, &keys, n));
-  RHG_TRY(bk2.alloc(ctx, st, &keys2, n));
-  RHG_TRY(bp.alloc(ctx, st, &perm, n));
-  RHG_TRY(bp2.alloc(ctx, st, &perm2, n));
-  RHG_TRY(bin4.alloc(ctx, st, &in4, 4 * uint64_t(n)));
-  RHG_TRY(bout4.alloc(ctx, st, &out4, 4 * uint64_t(n)));
-  RHG_TRY(bst.alloc(ctx, st, &bstart, kBands + 1));
+  GEN_CHECK(bk.alloc(ctx, st, &keys, n));
+  GEN_CHECK(bk2.alloc(ctx, st, &keys2, n));
+  GEN_CHECK(bp.alloc(ctx, st, &perm, n));
+  GEN_CHECK(bp2.alloc(ctx, st, &perm2, n));
+  GEN_CHECK(bin4.alloc(ctx, st, &in4, 4 * uint64_t(n)));
+  GEN_CHECK(bout4.alloc(ctx, st, &out4, 4 * uint64_t(n)));
+  GEN_CHECK(bst.alloc(ctx, st, &bstart, kBands + 1));
   const RadixScratch rs = radix_scratch_bytes(n);
-  RHG_TRY(bcnt.alloc(ctx, st, &counts, std::max<uint64_t>(rs.counts, n)));
-  RHG_TRY(bstat.alloc(ctx, st, &status, std::max<uint64_t>(rs.status, n / 2048 + 2)));
-  RHG_TRY(bsmall.alloc(ctx, st, &small, 8));
+  GEN_CHECK(bcnt.alloc(ctx, st, &counts, std::max<uint64_t>(rs.counts, n)));
+  GEN_CHECK(bstat.alloc(ctx, st, &status, std::max<uint64_t>(rs.status, n / 2048 + 2)));
+  GEN_CHECK(bsmall.alloc(ctx, st, &small, 8));
   uint32_t* ticket = reinterpret_cast<uint32_t*>(small + 4);
   uint32_t* err = reinterpret_cast<uint32_t*>(small + 5);
-  RHG_TRY(cudaMemsetAsync(small, 0, 8 * sizeof(unsigned long long), st));
-  RHG_TRY(cudaMemcpyAsync(keys, hkey.data(), sizeof(uint64_t) * n, cudaMemcpyHostToDevice, st));
-  RHG_TRY(cudaMemcpyAsync(in4, h4.data(), sizeof(double) * 4 * uint64_t(n),
+  GEN_CHECK(cudaMemsetAsync(small, 0, 8 * sizeof(unsigned long long), st));
+  GEN_CHECK(cudaMemcpyAsync(keys, hkey.data(), sizeof(uint64_t) * n, cudaMemcpyHostToDevice, st));
+  GEN_CHECK(cudaMemcpyAsync(in4, h4.data(), sizeof(double) * 4 * uint64_t(n),
                           cudaMemcpyHostToDevice, st));
   {
     std::vector<uint32_t> iota(n);
     for (uint32_t i = 0; i < n; ++i) iota[i] = i;
-    RHG_TRY(cudaMemcpyAsync(perm, iota.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, st));
+    GEN_CHECK(cudaMemcpyAsync(perm, iota.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, st));
     int alt = 0;
-    RHG_TRY(radix_sort_pairs_u32(st, keys, keys2, perm, perm2, n, 62, counts, status, ticket, err,
+    GEN_CHECK(radix_sort_pairs_u32(st, keys, keys2, perm, perm2, n, 62, counts, status, ticket, err,
                                  &alt, sms));
     if (alt) {
       std::swap(keys, keys2);
       std::swap(perm, perm2);
     }
-    RHG_TRY(cudaStreamSynchronize(st));  // iota (pageable) is done
+    GEN_CHECK(cudaStreamSynchronize(st));  // iota (pageable) is done
   }
   k_rhg_place<<<grid, 256, 0, st>>>(perm, n, in4, out4);
   k_rhg_bands<<<1, 32, 0, st>>>(keys, n, bstart);
   RhgView v{out4, out4 + n, out4 + 2 * uint64_t(n), out4 + 3 * uint64_t(n), keys};
-  RHG_TRY(bdeg.alloc(ctx, st, &deg, n));
-  RHG_TRY(boff.alloc(ctx, st, &off, n));
+  GEN_CHECK(bdeg.alloc(ctx, st, &deg, n));
+  GEN_CHECK(boff.alloc(ctx, st, &off, n));
   k_rhg_edges<false><<<grid, 256, 0, st>>>(v, n, bt, bstart, coshR, deg, nullptr, wseed,
                                            max_weight, nullptr);
-  RHG_TRY(exclusive_scan_u32(st, deg, off, n, status, ticket, err, sms));
-  RHG_TRY(sum_u32(st, deg, n, small, sms));
+  GEN_CHECK(exclusive_scan_u32(st, deg, off, n, status, ticket, err, sms));
+  GEN_CHECK(sum_u32(st, deg, n, small, sms));
   unsigned long long total = 0;
   uint32_t herr = 0;
-  RHG_TRY(cudaMemcpyAsync(&total, small, sizeof(total), cudaMemcpyDeviceToHost, st));
-  RHG_TRY(cudaMemcpyAsync(&herr, err, sizeof(herr), cudaMemcpyDeviceToHost, st));
-  RHG_TRY(cudaStreamSynchronize(st));
-  RHG_TRY(cudaGetLastError());
+  GEN_CHECK(cudaMemcpyAsync(&total, small, sizeof(total), cudaMemcpyDeviceToHost, st));
+  GEN_CHECK(cudaMemcpyAsync(&herr, err, sizeof(herr), cudaMemcpyDeviceToHost, st));
+  GEN_CHECK(cudaStreamSynchronize(st));
+  GEN_CHECK(cudaGetLastError());
   if (herr) {
     set_error("gen_rhg: device wait cap reached");
     return KAMSTA_E_NOCONVERGE;
@@ -324,8 +298,8 @@ kamsta_status gen_rhg(kamsta_ctx* ctx, uint32_t n, double gamma, double avg_degr
   }
   k_rhg_edges<true><<<grid, 256, 0, st>>>(v, n, bt, bstart, coshR, deg, off, wseed, max_weight,
                                           reinterpret_cast<uint32_t*>(d_out));
-  RHG_TRY(cudaGetLastError());
-  RHG_TRY(cudaStreamSynchronize(st));
+  GEN_CHECK(cudaGetLastError());
+  GEN_CHECK(cudaStreamSynchronize(st));
   return KAMSTA_OK;
 }
 

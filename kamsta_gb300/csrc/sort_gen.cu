@@ -1,7 +1,7 @@
 // sort_gen.cu -- host side of the radix sort and the device G(n,m) generator.
 //
 // The generator stands in for KaGen's get_gnm (benchmarks/mst_benchmarks.hpp:
-// 121-132), which the reference tree does not vendor.  Its definition is
+// 126-132), which the reference tree does not vendor.  Its definition is
 // shared with the oracle's CPU generator (oracle/oracle.cpp):
 //   mix64 = SplitMix64's output function; base = mix64(seed);
 //   candidate i: u = hi64(mix64(base + 2i) * n), v = hi64(mix64(base + 2i + 1) * n);
@@ -334,7 +334,7 @@ kamsta_status gen_gnm(kamsta_ctx* ctx, uint32_t n, uint64_t m, uint64_t seed, ui
 
 // ---------------------------------------------------------------------------
 // 2-D random geometric graph.  Stand-in for KaGen's get_rgg2D
-// (benchmarks/mst_benchmarks.hpp:134-142); the definition is shared with the
+// (benchmarks/mst_benchmarks.hpp:133-139); the definition is shared with the
 // oracle's CPU generator (oracle/oracle.cpp):
 //   base = mix64(seed ^ 0x5247473244); point i: x = mix64(base + 2i) >> 33,
 //   y = mix64(base + 2i + 1) >> 33 (31-bit integers); R = floor(radius * 2^31);

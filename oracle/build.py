@@ -10,11 +10,11 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
-SRC = [os.path.join(HERE, "oracle.cpp")]
+SRC = [os.path.join(HERE, "oracle.cpp"), os.path.join(HERE, "gen_grid_rmat.cpp")]
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
-    deps = SRC + [os.path.join(HERE, "oracle.h"),
+    deps = SRC + [os.path.join(HERE, "oracle.h"), os.path.join(HERE, "gen_common.h"),
                   os.path.join(HERE, "..", "include", "kamsta_gpu.h")]
     if not force and os.path.exists(LIB):
         t = os.path.getmtime(LIB)

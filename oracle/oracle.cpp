@@ -3,6 +3,7 @@
 // TEST INFRASTRUCTURE ONLY (see oracle.h).  Reference citations are paths in
 // the KaMSTa source tree.
 #include "oracle.h"
+#include "gen_common.h"
 
 #include <omp.h>
 
@@ -373,19 +374,6 @@ extern "C" int oracle_boruvka_filter(const kamsta_wedge* edges,
 //                uniform m-subset of all unordered pairs);
 //   weight      = 1 + hi64(mix64(wseed ^ key) * max_weight),
 //                wseed = mix64(seed ^ 0x6a09e667f3bcc909).
-namespace gen {
-
-inline uint64_t mix64(uint64_t z) {
-  z += 0x9e3779b97f4a7c15ull;
-  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
-  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
-  return z ^ (z >> 31);
-}
-inline uint64_t hi64(uint64_t a, uint64_t b) {
-  return static_cast<uint64_t>((static_cast<unsigned __int128>(a) * b) >> 64);
-}
-
-}  // namespace gen
 
 extern "C" int oracle_gen_gnm(uint32_t n, uint64_t m, uint64_t seed,
                               uint32_t max_weight, kamsta_wedge* out,
@@ -470,7 +458,7 @@ extern "C" int oracle_gen_gnm(uint32_t n, uint64_t m, uint64_t seed,
 
 // ---------------------------------------------------------------------------
 // Seeded 2-D random geometric graph (stand-in for KaGen's get_rgg2D,
-// benchmarks/mst_benchmarks.hpp:134-142, which the reference tree does not
+// benchmarks/mst_benchmarks.hpp:133-139, which the reference tree does not
 // vendor).  The definition, shared with the device generator
 // kamsta_gen_rgg2d_dev:
 //   base = mix64(seed ^ 0x5247473244ull); point i (i < n) has 31-bit integer
@@ -573,7 +561,7 @@ extern "C" int oracle_gen_rgg2d(uint32_t n, double radius, uint64_t seed, uint32
 
 // ---------------------------------------------------------------------------
 // Seeded threshold random hyperbolic graph (stand-in for KaGen's get_rhg,
-// benchmarks/mst_benchmarks.hpp:143-158).  The definition, shared with the
+// benchmarks/mst_benchmarks.hpp:152-158).  The definition, shared with the
 // device generator kamsta_gen_rhg_dev:
 //   alpha = (gamma - 1) / 2 (gamma > 2), xi = alpha / (alpha - 1/2),
 //   disk radius R = max(1, 2 ln(2 xi^2 n / (pi k))) (the asymptotic

@@ -22,6 +22,12 @@
  *                              to kamsta_gen_rgg2d_dev.
  *   oracle_gen_rhg          -- seeded threshold random hyperbolic graph;
  *                              bit-identical to kamsta_gen_rhg_dev.
+ *   oracle_gen_grid         -- 2-D / 3-D lattice (gen_grid_rmat.cpp);
+ *                              bit-identical to kamsta_gen_grid_dev.
+ *   oracle_gen_rgg3d        -- seeded 3-D random geometric graph;
+ *                              bit-identical to kamsta_gen_rgg3d_dev.
+ *   oracle_gen_rmat         -- seeded R-MAT graph; bit-identical to
+ *                              kamsta_gen_rmat_dev.
  *
  * Parity status: the reference ships no golden vectors (its only test,
  * tests/test_sets.sh, checks the MSF weight against this same Kruskal).
@@ -72,6 +78,25 @@ int oracle_gen_rgg2d(uint32_t n, double radius, uint64_t seed, uint32_t max_weig
 int oracle_gen_rhg(uint32_t n, double gamma, double avg_degree, uint64_t seed,
                    uint32_t max_weight, kamsta_wedge* out, uint64_t capacity,
                    uint64_t* m_directed_out);
+
+/* Lattice X x Y x Z (Z = 1: 2-D), +-1 steps along each axis, wrapping when
+ * `periodic`, each edge kept with probability p.  Return convention as
+ * oracle_gen_rgg2d. */
+int oracle_gen_grid(uint32_t x, uint32_t y, uint32_t z, double p, int periodic, uint64_t seed,
+                    uint32_t max_weight, kamsta_wedge* out, uint64_t capacity,
+                    uint64_t* m_directed_out);
+
+/* Seeded 3-D random geometric graph in the unit cube.  Return convention as
+ * oracle_gen_rgg2d. */
+int oracle_gen_rgg3d(uint32_t n, double radius, uint64_t seed, uint32_t max_weight,
+                     kamsta_wedge* out, uint64_t capacity, uint64_t* m_directed_out);
+
+/* Seeded R-MAT graph on 2^log_n vertices from `samples` samples with
+ * quadrant probabilities a, b, c (d = 1 - a - b - c).  Return convention as
+ * oracle_gen_rgg2d. */
+int oracle_gen_rmat(uint32_t log_n, uint64_t samples, double a, double b, double c,
+                    uint64_t seed, uint32_t max_weight, kamsta_wedge* out, uint64_t capacity,
+                    uint64_t* m_directed_out);
 
 /* Number of OpenMP threads the oracle uses when threads == 0. */
 int oracle_max_threads(void);

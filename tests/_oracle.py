@@ -29,6 +29,11 @@ def lib():
         L.oracle_gen_rgg2d.argtypes = [U32, C.c_double, U64, U32, P, U64, C.POINTER(U64)]
         L.oracle_gen_rhg.argtypes = [U32, C.c_double, C.c_double, U64, U32, P, U64,
                                      C.POINTER(U64)]
+        L.oracle_gen_grid.argtypes = [U32, U32, U32, C.c_double, C.c_int, U64, U32, P, U64,
+                                      C.POINTER(U64)]
+        L.oracle_gen_rgg3d.argtypes = [U32, C.c_double, U64, U32, P, U64, C.POINTER(U64)]
+        L.oracle_gen_rmat.argtypes = [U32, U64, C.c_double, C.c_double, C.c_double, U64, U32, P,
+                                      U64, C.POINTER(U64)]
         L.oracle_max_threads.restype = C.c_int
         _lib = L
     return _lib
@@ -66,6 +71,39 @@ def gen_rhg(n: int, gamma: float, avg_degree: float, seed: int,
                               cnt.value, C.byref(cnt))
     assert rc == 0
     return out[: cnt.value]
+
+
+def _counted(fn, *args):
+    """Runs a count-then-write oracle generator: a counting call, then the
+    write into an array of that size."""
+    cnt = C.c_uint64()
+    rc = fn(*args, None, 0, C.byref(cnt))
+    if rc not in (0, 2):
+        raise ValueError(f"{fn.__name__}: bad arguments")
+    out = np.empty(max(cnt.value, 1), WEDGE)
+    rc = fn(*args, out.ctypes.data, cnt.value, C.byref(cnt))
+    assert rc == 0
+    return out[: cnt.value]
+
+
+def gen_grid(x: int, y: int, z: int = 1, p: float = 1.0, periodic: bool = True, seed: int = 1,
+             max_weight: int = 254) -> np.ndarray:
+    return _counted(lib().oracle_gen_grid, x, y, z, p, int(periodic), seed, max_weight)
+
+
+def gen_rgg3d(n: int, radius: float, seed: int, max_weight: int = 254) -> np.ndarray:
+    return _counted(lib().oracle_gen_rgg3d, n, radius, seed, max_weight)
+
+
+def gen_rmat(log_n: int, samples: int, seed: int, a: float = 0.57, b: float = 0.19,
+             c: float = 0.19, max_weight: int = 254) -> np.ndarray:
+    return _counted(lib().oracle_gen_rmat, log_n, samples, a, b, c, seed, max_weight)
+
+
+def rgg3d_radius(n: int, avg_degree: float) -> float:
+    """Radius giving an expected degree `avg_degree` away from the border."""
+    import math
+    return (3.0 * avg_degree / (4.0 * math.pi * n)) ** (1.0 / 3.0)
 
 
 def rgg_radius(n: int, avg_degree: float) -> float:

@@ -93,3 +93,84 @@ def test_filter_boruvka_geometric_config_exactness(kamsta, oracle, family):
          else oracle.gen_rhg(n, 3.0, 16, 2024))
     from tests.test_parity_gpu import _check
     _check(oracle, kamsta.filter_boruvka(e, kamsta.AlgorithmConfig(), n=n), e, n)
+
+
+def _dev_counted(kamsta, gen, *args):
+    """Count, allocate, write: the counting convention of the generators."""
+    import torch
+    md = gen(*args)
+    d = torch.empty((max(md, 1), 3), dtype=torch.int32, device="cuda")
+    assert gen(*args, d_out=d.data_ptr(), capacity=md) == md
+    torch.cuda.synchronize()
+    return d[:md].cpu().numpy().view(np.uint32).reshape(-1).view(kamsta.WEDGE)
+
+
+@pytest.mark.parametrize("X,Y,Z,p,periodic", [(1, 1, 1, 1.0, True), (2, 2, 2, 1.0, True),
+                                              (5, 3, 1, 1.0, False), (7, 1, 1, 1.0, True),
+                                              (1024, 1024, 1, 1.0, True),
+                                              (64, 64, 64, 1.0, True), (300, 200, 1, 0.7, False),
+                                              (40, 50, 60, 0.45, True)])
+def test_grid_matches_oracle(kamsta, oracle, X, Y, Z, p, periodic):
+    ctx = kamsta.Context(0)
+    got = _dev_counted(kamsta, lambda **kw: ctx.gen_grid_dev(X, Y, Z, p, periodic, 21, 254, **kw))
+    assert np.array_equal(got, oracle.gen_grid(X, Y, Z, p, periodic, 21))
+
+
+@pytest.mark.parametrize("n,deg,seed", [(1, 8.0, 1), (2, 8.0, 2), (300, 8.0, 3),
+                                        (1 << 16, 16.0, 4), (1 << 18, 10.0, 5)])
+def test_rgg3d_matches_oracle(kamsta, oracle, n, deg, seed):
+    ctx = kamsta.Context(0)
+    r = oracle.rgg3d_radius(n, deg)
+    got = _dev_counted(kamsta, lambda **kw: ctx.gen_rgg3d_dev(n, r, seed, 254, **kw))
+    assert np.array_equal(got, oracle.gen_rgg3d(n, r, seed))
+
+
+@pytest.mark.parametrize("L,samples,seed,abc", [(1, 10, 1, (0.57, 0.19, 0.19)),
+                                                (10, 3000, 3, (0.57, 0.19, 0.19)),
+                                                (16, 1 << 20, 4, (0.57, 0.19, 0.19)),
+                                                (20, 1 << 22, 5, (0.45, 0.15, 0.15)),
+                                                (12, 1 << 16, 6, (0.25, 0.25, 0.25))])
+def test_rmat_matches_oracle(kamsta, oracle, L, samples, seed, abc):
+    ctx = kamsta.Context(0)
+    got = _dev_counted(kamsta, lambda **kw: ctx.gen_rmat_dev(L, samples, seed, *abc, 254, **kw))
+    assert np.array_equal(got, oracle.gen_rmat(L, samples, seed, *abc))
+
+
+def test_generator_capacity_errors(kamsta):
+    import torch
+    ctx = kamsta.Context(0)
+    for gen in (lambda **kw: ctx.gen_grid_dev(30, 30, 1, **kw),
+                lambda **kw: ctx.gen_rgg3d_dev(4000, 0.1, 1, **kw),
+                lambda **kw: ctx.gen_rmat_dev(12, 1 << 14, 1, **kw)):
+        md = gen()
+        assert md > 10
+        d = torch.empty((md, 3), dtype=torch.int32, device="cuda")
+        with pytest.raises(kamsta.KamstaError):
+            gen(d_out=d.data_ptr(), capacity=md - 1)
+    with pytest.raises(kamsta.KamstaError):
+        ctx.gen_rmat_dev(32, 10, 1)
+    with pytest.raises(kamsta.KamstaError):
+        ctx.gen_rmat_dev(10, 10, 1, 0.6, 0.3, 0.2)
+    with pytest.raises(kamsta.KamstaError):
+        ctx.gen_grid_dev(1 << 16, 1 << 16, 1)
+
+
+@pytest.mark.parametrize("algo", ["boruvka_plain", "boruvka_local", "filter_boruvka",
+                                  "filter_dedupe"])
+@pytest.mark.parametrize("family", ["grid2d", "grid3d", "rgg3d", "rmat"])
+def test_mst_on_more_families(kamsta, oracle, algo, family):
+    """MSF parity on lattices (many equal-weight ties, long paths), 3-D
+    geometric graphs and R-MAT (hubs at the smallest ids, isolated
+    vertices)."""
+    from tests.test_parity_gpu import _check, _configs
+    fn, cfg = _configs(kamsta)[algo]
+    if family == "grid2d":
+        n, e = 300 * 200, oracle.gen_grid(300, 200, 1, 0.8, True, 3, 8)
+    elif family == "grid3d":
+        n, e = 40 * 40 * 40, oracle.gen_grid(40, 40, 40, 1.0, False, 4, 4)
+    elif family == "rgg3d":
+        n = 1 << 17
+        e = oracle.gen_rgg3d(n, oracle.rgg3d_radius(n, 12), 5)
+    else:
+        n, e = 1 << 18, oracle.gen_rmat(18, 1 << 22, 6)
+    _check(oracle, fn(e, cfg, n=n), e, n)

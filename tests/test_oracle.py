@@ -211,3 +211,142 @@ def test_rhg_properties(oracle):
     deg = np.bincount(e["src"], minlength=n)
     assert 8 < len(e) / n < 32        # near the target average degree
     assert deg.max() > 20 * len(e) / n  # power law: hubs
+
+
+def _weight(wseed, a, b, wmax=254):
+    canon = (min(a, b) << 32) | max(a, b)
+    return 1 + ((_mix64(wseed ^ canon) * wmax) >> 64)
+
+
+def _py_grid(X, Y, Z, p, periodic, seed, wmax=254):
+    """Set-based restatement of the lattice definition (small sizes only)."""
+    pseed = _mix64(seed ^ 0x47524944)
+    wseed = _mix64(seed ^ 0x6A09E667F3BCC909)
+    pthr = int(p * 9007199254740992.0) if 0.0 < p < 1.0 else 0
+    pairs = set()
+    for z in range(Z):
+        for y in range(Y):
+            for x in range(X):
+                v = (z * Y + y) * X + x
+                for axis, side in enumerate((X, Y, Z)):
+                    for step in (-1, 1):
+                        c = [x, y, z]
+                        t = c[axis] + step
+                        if not 0 <= t < side:
+                            if not periodic:
+                                continue
+                            t %= side
+                        c[axis] = t
+                        u = (c[2] * Y + c[1]) * X + c[0]
+                        if u == v:
+                            continue
+                        canon = (min(u, v) << 32) | max(u, v)
+                        if p < 1.0 and (_mix64(pseed ^ canon) >> 11) >= pthr:
+                            continue
+                        pairs.add((v, u))
+    return [(a, b, _weight(wseed, a, b, wmax)) for a, b in sorted(pairs)]
+
+
+@pytest.mark.parametrize("X,Y,Z,p,periodic", [(1, 1, 1, 1.0, True), (2, 1, 1, 1.0, True),
+                                              (2, 2, 2, 1.0, True), (5, 3, 1, 1.0, False),
+                                              (4, 3, 2, 1.0, True), (6, 5, 1, 0.6, True),
+                                              (3, 4, 5, 0.3, False), (7, 1, 1, 1.0, True)])
+def test_grid_matches_definition(oracle, X, Y, Z, p, periodic):
+    e = oracle.gen_grid(X, Y, Z, p, periodic, 11)
+    got = [(int(a), int(b), int(w)) for a, b, w in zip(e["src"], e["dst"], e["w"])]
+    assert got == _py_grid(X, Y, Z, p, periodic, 11)
+
+
+def test_grid_edge_counts():
+    """Closed forms: a periodic torus with sides >= 3 is 2d-regular; the open
+    box has sum over axes of (side - 1) * (other sides) edges."""
+    from tests import _oracle as oracle
+    assert len(oracle.gen_grid(64, 32, 1)) == 4 * 64 * 32
+    assert len(oracle.gen_grid(8, 9, 10)) == 6 * 8 * 9 * 10
+    assert len(oracle.gen_grid(8, 9, 10, periodic=False)) == 2 * (7 * 90 + 8 * 8 * 10 + 9 * 72)
+
+
+def _py_rgg3d(n, radius, seed, wmax=254):
+    """All-pairs restatement of the RGG-3D definition (small n only)."""
+    base = _mix64(seed ^ 0x5247473344)
+    wseed = _mix64(seed ^ 0x6A09E667F3BCC909)
+    R = 0 if radius <= 0 else (1 << 31) if radius >= 1 else int(radius * 2147483648.0)
+    cap = 1
+    while (cap + 1) ** 3 <= n:
+        cap += 1
+    cap = min(cap, 1024)
+    G = cap if R == 0 else max(1, min((1 << 31) // R, cap))
+    M = 1 << 64
+    pts = []
+    for i in range(n):
+        x, y, z = (_mix64((base + 3 * i + a) % M) >> 33 for a in range(3))
+        cell = (((z * G) >> 31) * G + ((y * G) >> 31)) * G + ((x * G) >> 31)
+        pts.append((cell, i, x, y, z))
+    pts.sort()
+    out = []
+    for j, pj in enumerate(pts):
+        for k, pk in enumerate(pts):
+            if k != j and sum((pj[a] - pk[a]) ** 2 for a in (2, 3, 4)) <= R * R:
+                out.append((j, k, _weight(wseed, j, k, wmax)))
+    return out
+
+
+@pytest.mark.parametrize("n,radius,seed", [(1, 0.5, 1), (30, 0.3, 2), (200, 0.2, 3),
+                                           (64, 1.0, 4), (90, 0.0, 5)])
+def test_rgg3d_matches_definition(oracle, n, radius, seed):
+    e = oracle.gen_rgg3d(n, radius, seed)
+    got = [(int(a), int(b), int(w)) for a, b, w in zip(e["src"], e["dst"], e["w"])]
+    assert got == _py_rgg3d(n, radius, seed)
+
+
+def test_rgg3d_properties(oracle):
+    n = 1 << 15
+    e = oracle.gen_rgg3d(n, oracle.rgg3d_radius(n, 16), 7)
+    s, d = e["src"].astype(np.uint64), e["dst"].astype(np.uint64)
+    k = (s << np.uint64(32)) | d
+    assert np.all(k[1:] > k[:-1])
+    assert np.array_equal(np.sort((d << np.uint64(32)) | s), k)
+    assert 12.0 < len(e) / n < 16.5  # the cube's faces lower the mean degree
+
+
+def _py_rmat(L, samples, seed, a=0.57, b=0.19, c=0.19, wmax=254):
+    """Sample-by-sample restatement of the R-MAT definition."""
+    import math
+    base = _mix64(seed ^ 0x524D4154)
+    wseed = _mix64(seed ^ 0x6A09E667F3BCC909)
+    t = [min(1 << 32, math.floor(x * 4294967296.0)) for x in (a, a + b, a + b + c)]
+    per = (L + 1) // 2
+    pairs = set()
+    for i in range(samples):
+        u = v = 0
+        for lvl in range(L):
+            h = _mix64((base + i * per + lvl // 2) % (1 << 64))
+            r = h >> 32 if lvl % 2 == 0 else h & 0xFFFFFFFF
+            q = 0 if r < t[0] else 1 if r < t[1] else 2 if r < t[2] else 3
+            u, v = 2 * u + (q >> 1), 2 * v + (q & 1)
+        if u != v:
+            pairs.add((min(u, v), max(u, v)))
+    d = sorted([(x, y) for x, y in pairs] + [(y, x) for x, y in pairs])
+    return [(x, y, _weight(wseed, x, y, wmax)) for x, y in d]
+
+
+@pytest.mark.parametrize("L,samples,seed,abc", [(1, 10, 1, (0.57, 0.19, 0.19)),
+                                                (5, 100, 2, (0.57, 0.19, 0.19)),
+                                                (10, 3000, 3, (0.57, 0.19, 0.19)),
+                                                (9, 2000, 4, (0.25, 0.25, 0.25)),
+                                                (7, 500, 5, (0.0, 0.5, 0.5)),
+                                                (6, 300, 6, (1.0, 0.0, 0.0))])
+def test_rmat_matches_definition(oracle, L, samples, seed, abc):
+    e = oracle.gen_rmat(L, samples, seed, *abc)
+    got = [(int(x), int(y), int(w)) for x, y, w in zip(e["src"], e["dst"], e["w"])]
+    assert got == _py_rmat(L, samples, seed, *abc)
+
+
+def test_rmat_properties(oracle):
+    e = oracle.gen_rmat(16, 1 << 19, 9)
+    s, d = e["src"].astype(np.uint64), e["dst"].astype(np.uint64)
+    k = (s << np.uint64(32)) | d
+    assert np.all(k[1:] > k[:-1])
+    assert np.array_equal(np.sort((d << np.uint64(32)) | s), k)
+    deg = np.bincount(e["src"], minlength=1 << 16)
+    assert deg[0] == deg.max() and deg[0] > 100 * len(e) / (1 << 16)  # hub at id 0
