@@ -623,6 +623,17 @@ def main():
 
         for _ in range(max(1, args.warmup)):
             e2e_step()
+        # the host link's copy rate on this machine, for reading the e2e number:
+        # 4 GiB of the pinned input copied back over the (identical) device copy
+        link_rows = min(md, (4 << 30) // 12)
+        c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        link = []
+        for _ in range(3):
+            c0.record(stream)
+            d_edges[:link_rows].copy_(h_edges[:link_rows], non_blocking=True)
+            c1.record(stream)
+            torch.cuda.synchronize()
+            link.append(link_rows * 12 / (c0.elapsed_time(c1) * 1e6))
         rep.barrier()
         t0 = time.perf_counter()
         for _ in range(args.steps):
@@ -633,6 +644,7 @@ def main():
         line["e2e"] = {"value": args.gpus * md * args.steps / dt, "unit": UNIT,
                        "h2d_bytes_per_step": md * 12, "d2h_bytes_per_step": ke * 12,
                        "ms_per_step": dt / args.steps * 1e3,
+                       "h2d_link_gbs": max(link),
                        "api": "kamsta_mst_boruvka (host buffers, pinned input and output)"}
         del h_edges, h_out
 

@@ -625,9 +625,13 @@ __global__ void k_dedupe_mark(const uint64_t* __restrict__ keys, const uint32_t*
 // minima -- so several independent random reads are in flight per thread.
 constexpr int kIlp = 4;
 
+// With hook_w set (the first round over original ids, whose forest edges
+// are emitted directly), msfoid receives the partner and hook_w the weight
+// instead of the input position.
 __global__ void k_hook(uint32_t n, const uint64_t* __restrict__ minval,
                        const Rec* __restrict__ list, uint32_t* __restrict__ parent,
-                       uint32_t* __restrict__ msfoid, uint32_t* err) {
+                       uint32_t* __restrict__ msfoid, uint32_t* __restrict__ hook_w,
+                       uint32_t* err) {
   const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
   for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; base < n;
        base += kIlp * stride) {
@@ -666,7 +670,12 @@ __global__ void k_hook(uint32_t n, const uint64_t* __restrict__ minval,
         msfoid[v] = kNone;
       } else {
         parent[v] = u[k];
-        msfoid[v] = r[k].oid;
+        if (hook_w) {
+          msfoid[v] = u[k];
+          hook_w[v] = r[k].w;
+        } else {
+          msfoid[v] = r[k].oid;
+        }
       }
     }
   }
@@ -749,6 +758,13 @@ struct VertexScanArgs {
   uint32_t* cta_counts;  // 2 per CTA: roots, hooked
   unsigned long long* counts;  // [0] roots, [1] forest edges (totals)
   uint32_t* err;
+  // direct emission (first round over original ids): forest edge k of the
+  // round is written as (min, max, w) at direct_out[3k..], from the partner
+  // in msfoid and the weight in hook_w; the weights are summed into
+  // direct_weight.  Null: msf_out receives input positions as usual.
+  uint32_t* direct_out;
+  const uint32_t* hook_w;
+  unsigned long long* direct_weight;
 };
 
 __device__ __forceinline__ uint32_t vertex_class(const VertexScanArgs& p, uint32_t v) {
@@ -806,6 +822,7 @@ __global__ void __launch_bounds__(kBlock) k_vertex_write(VertexScanArgs p) {
   const uint32_t hi = min(lo + p.chunk, p.n);
   const uint32_t lane = lane_id(), warp = threadIdx.x >> 5, lt = lanemask_lt();
   uint32_t run0 = s_base[0], run1 = s_base[1];
+  uint64_t wsum = 0;
   for (uint32_t v0 = lo; v0 < hi; v0 += kBlock) {  // rows of kBlock vertices, in order
     const uint32_t v = v0 + threadIdx.x;
     const uint32_t c = v < hi ? vertex_class(p, v) : 2u;
@@ -836,13 +853,25 @@ __global__ void __launch_bounds__(kBlock) k_vertex_write(VertexScanArgs p) {
       }
     } else if (c == 1) {
       const uint32_t k = pre1 + __popc(b1 & lt);
-      if (k < p.msf_cap)
-        p.msf_out[k] = p.msfoid[v];
-      else
+      if (k >= p.msf_cap) {
         atomicOr(p.err, kErrOverflow);
+      } else if (p.direct_out) {
+        const uint32_t u = p.msfoid[v], w = p.hook_w[v];
+        uint32_t* o = p.direct_out + 3ull * k;
+        o[0] = v < u ? v : u;
+        o[1] = v < u ? u : v;
+        o[2] = w;
+        wsum += w;
+      } else {
+        p.msf_out[k] = p.msfoid[v];
+      }
     }
     run0 += tot0;
     run1 += tot1;
+  }
+  if (p.direct_out) {
+    wsum = warp_sum(wsum);
+    if (lane == 0 && wsum) atomicAdd(p.direct_weight, static_cast<unsigned long long>(wsum));
   }
 }
 
@@ -1206,7 +1235,11 @@ __global__ void k_fill64(uint64_t n, uint64_t* __restrict__ a, uint64_t v) {
 __global__ void k_emit(uint64_t k, const uint32_t* __restrict__ msf,
                        const uint32_t* __restrict__ in_words,
                        uint32_t* __restrict__ out_words,
-                       unsigned long long* weight) {
+                       unsigned long long* weight,
+                       const unsigned long long* __restrict__ add_weight) {
+  // add_weight: the weight of forest edges written elsewhere (direct emission)
+  if (add_weight && blockIdx.x == 0 && threadIdx.x == 0 && *add_weight)
+    atomicAdd(weight, *add_weight);
   uint64_t local = 0;
   const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
   for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; base < k;

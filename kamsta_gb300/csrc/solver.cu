@@ -236,6 +236,14 @@ class Solve {
   uint32_t* big_ = nullptr;         // membership bitmap of the largest component
   uint32_t nreps_ = 0;
   uint64_t msf_count_ = 0;
+  // Direct emission: the first round over original ids (the first pass's
+  // lightest class) writes its forest edges to the output itself, so the
+  // final emit gathers only the later rounds' edges from the input.
+  kamsta_wedge* d_out_ = nullptr;
+  uint32_t* hookw_ = nullptr;           // weight of each hooked vertex's edge
+  unsigned long long* dweight_ = nullptr;  // weight of the directly written edges
+  bool direct_emit_ = false;            // the next round may emit directly
+  uint64_t direct_count_ = 0;           // forest edges written directly
   std::vector<uint32_t> bounds_;        // ascending weight-class bounds
   std::vector<uint32_t> samples_host_;  // sorted weight sample of the input
 };
@@ -247,7 +255,7 @@ kamsta_status Solve::alloc_fixed() {
   const uint64_t n = n_;
   size_t bytes = 0;
   auto add = [&](uint64_t count, size_t sz) { bytes += round_up(count * sz, 256); };
-  for (int i = 0; i < 9; ++i) add(n + 1, 4);  // P D V Vn dense parent msfoid newid msf
+  for (int i = 0; i < 10; ++i) add(n + 1, 4);  // P D V Vn dense parent msfoid newid msf hookw
   add(2 * n + 64, 4);                         // Rbuf
   add(n + 64, 4);                             // Obuf
   add(n + 1, 8);
@@ -255,6 +263,7 @@ kamsta_status Solve::alloc_fixed() {
   add(kMaxSeg + 1, 8);
   add(2 * kMaxSeg, 4);
   add(n / 32 + 2, 4);
+  add(4, 8);  // dweight
   CU_TRY(ctx_->fixed.reserve(bytes + 4096));
   Arena& A = ctx_->fixed;
   P_ = A.take<uint32_t>(n + 1);
@@ -266,6 +275,7 @@ kamsta_status Solve::alloc_fixed() {
   msfoid_ = A.take<uint32_t>(n + 1);
   newid_ = A.take<uint32_t>(n + 1);
   msf_ = A.take<uint32_t>(n + 1);
+  hookw_ = A.take<uint32_t>(n + 1);
   Rbuf_ = A.take<uint32_t>(2 * n + 64);
   Obuf_ = A.take<uint32_t>(n + 64);
   minA_ = A.take<uint64_t>(n + 1);
@@ -273,7 +283,8 @@ kamsta_status Solve::alloc_fixed() {
   prefix_ = A.take<uint64_t>(kMaxSeg + 1);
   cta_counts_ = A.take<uint32_t>(2 * kMaxSeg);
   big_ = A.take<uint32_t>(n / 32 + 2);
-  if (!big_) {
+  dweight_ = A.take<unsigned long long>(4);
+  if (!big_ || !dweight_) {
     set_error("internal: fixed arena too small");
     return KAMSTA_E_OOM;
   }
@@ -374,9 +385,11 @@ kamsta_status Solve::debug_list(const char* where, const SegList& L, uint64_t nl
 }
 
 kamsta_status Solve::debug_forest(const char* where, uint64_t count) {
-  if (!debug_ || count == 0) return KAMSTA_OK;
-  std::vector<uint32_t> h(count);
-  CU_TRY(cudaMemcpyAsync(h.data(), msf_, count * 4, cudaMemcpyDeviceToHost, st_));
+  // input positions are recorded after the directly written edges only
+  if (!debug_ || count <= direct_count_) return KAMSTA_OK;
+  std::vector<uint32_t> h(count - direct_count_);
+  CU_TRY(cudaMemcpyAsync(h.data(), msf_ + direct_count_, h.size() * 4, cudaMemcpyDeviceToHost,
+                         st_));
   CU_TRY(cudaStreamSynchronize(st_));
   std::sort(h.begin(), h.end());
   for (size_t i = 1; i < h.size(); ++i)
@@ -602,7 +615,11 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
     CU_TRY(cudaMemsetAsync(ctx_->d_counters + kCVertex, 0, sizeof(DevCounters), st_));
     const int gv = grid_for(nr);
     const int tv = tick();
-    k_hook<<<gv, kBlock, 0, st_>>>(nr, minv, cur->base, parent_, msfoid_, ctx_->d_err);
+    // direct emission needs original ids (the first round of the first
+    // contraction) and an empty forest so far
+    const bool direct = direct_emit_ && r == 0 && msf_count_ == 0 && n_ >= 2;
+    k_hook<<<gv, kBlock, 0, st_>>>(nr, minv, cur->base, parent_, msfoid_,
+                                   direct ? hookw_ : nullptr, ctx_->d_err);
     k_jump<<<gv, kBlock, 0, st_>>>(nr, parent_, ctx_->d_err);
     uint32_t* onext = Obuf_ + ooff;
     VertexScanArgs va{};
@@ -626,6 +643,12 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
     va.cta_counts = cta_counts_;
     va.counts = ctx_->d_counters[kCVertex].cnt;
     va.err = ctx_->d_err;
+    if (direct) {
+      va.direct_out = reinterpret_cast<uint32_t*>(d_out_);
+      va.hook_w = hookw_;
+      va.direct_weight = dweight_;
+      va.msf_cap = n_ - 1;  // the caller's output capacity
+    }
     k_vertex_count<<<gvs, kBlock, 0, st_>>>(va);
     k_vertex_write<<<gvs, kBlock, 0, st_>>>(va);
     uint32_t* R = Rbuf_ + roff;
@@ -643,8 +666,9 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
     // id/orig/minimum per root, edge id per hooked vertex; map: 3 reads + 1 write
     account(KAMSTA_PHASE_ROUND_VERTS,
             uint64_t(nr) * ((8 + 16 + 8 + 8) + 16 + (4 + 8 + 4) + (8 + 4 + 4)) + n_next * 16 +
-                added * 8,
+                added * (direct ? 4 + 4 + 4 + 12 : 8),
             6);
+    if (direct) direct_count_ = added;
     if (debug_) {
       fprintf(stderr, "[kamsta debug] round %u: m=%llu n=%u -> m'=%llu n'=%llu forest+=%llu\n", r,
               (unsigned long long)m, nr, (unsigned long long)nxt->total,
@@ -930,7 +954,10 @@ kamsta_status Solve::run_boruvka() {
   const int steps = nmat + std::max(0, K - nmat + 1);
   int step = 0;
   final_contraction_ = ++step == steps;
-  KS_TRY(rounds(C[0], true));
+  direct_emit_ = d_out_ != nullptr && forest_bits_ == nullptr;
+  const kamsta_status first = rounds(C[0], true);
+  direct_emit_ = false;
+  KS_TRY(first);
   for (int c = 1; c < nmat; ++c) {
     final_contraction_ = ++step == steps;
     KS_TRY(contract(C[c], 0, 0xffffffffu, 1.0));
@@ -1075,6 +1102,9 @@ kamsta_status Solve::run(Algo algo, kamsta_wedge* d_out, SolveOut* out) {
   account(KAMSTA_PHASE_FINALIZE, uint64_t(n_) * 12, 3);
   nreps_ = n_;
   msf_count_ = 0;
+  d_out_ = d_out;
+  direct_count_ = 0;
+  CU_TRY(cudaMemsetAsync(dweight_, 0, sizeof(unsigned long long), st_));
   CU_TRY(cudaMemsetAsync(ctx_->d_err, 0, sizeof(uint32_t), st_));
   KS_TRY(algo == Algo::kBoruvka ? run_boruvka() : run_filter_boruvka());
   // forest output
@@ -1086,12 +1116,14 @@ kamsta_status Solve::run(Algo algo, kamsta_wedge* d_out, SolveOut* out) {
     tock(KAMSTA_PHASE_EMIT, tm);
     account(KAMSTA_PHASE_EMIT, msf_count_ * (4 + 4 + 8), 1);
   } else if (msf_count_ > 0) {
+    // edges [0, direct_count_) are in d_out already; k_emit adds their weight
+    const uint64_t k0 = direct_count_;
     const int tm = tick();
-    k_emit<<<grid_for(msf_count_), kBlock, 0, st_>>>(msf_count_, msf_, in_,
-                                                      reinterpret_cast<uint32_t*>(d_out),
-                                                      &ctx_->d_counters[kCMisc].weight);
+    k_emit<<<grid_for(msf_count_ - k0), kBlock, 0, st_>>>(
+        msf_count_ - k0, msf_ + k0, in_, reinterpret_cast<uint32_t*>(d_out) + 3 * k0,
+        &ctx_->d_counters[kCMisc].weight, k0 ? dweight_ : nullptr);
     tock(KAMSTA_PHASE_EMIT, tm);
-    account(KAMSTA_PHASE_EMIT, msf_count_ * (4 + 12 + 12), 1);
+    account(KAMSTA_PHASE_EMIT, (msf_count_ - k0) * (4 + 12 + 12), 1);
   }
   CU_TRY(cudaEventRecord(ctx_->ev1, st_));
   KS_TRY(fetch_counters());
