@@ -67,6 +67,10 @@ struct PassArgs {
   SegOut out[kMaxOut];
   uint64_t* minval;
   uint32_t min_checked;  // filter minimum updates by a cached read (hub-heavy passes)
+  // Minimum keys (w << 32 | partner) instead of (w << 32 | list position):
+  // the first pass over original ids, without parallel edges, where a
+  // vertex's canonical (w, min, max) order is its (w, partner) order.
+  uint32_t min_partner;
   uint64_t total;  // logical input items
   uint64_t chunk;  // logical items per CTA (a multiple of the tile size)
   unsigned long long* counts;  // [0] dropped above wmax, [1] items that reached the map
@@ -182,9 +186,14 @@ __device__ __forceinline__ void seg_tile_finish(const uint8_t (&cls)[ITEMS], uin
       for (int j = 0; j < ITEMS; ++j) {
         if (!((min_mask >> j) & 1u)) continue;
         const Rec r = rec(j * kBlock + threadIdx.x);
-        const uint64_t v = (static_cast<uint64_t>(r.w) << 32) | (seg0 + offs[j]);
-        red_min(&p.minval[r.a], v);
-        red_min(&p.minval[r.b], v);
+        const uint64_t wk = static_cast<uint64_t>(r.w) << 32;
+        if (p.min_partner) {
+          red_min(&p.minval[r.a], wk | r.b);
+          red_min(&p.minval[r.b], wk | r.a);
+        } else {
+          red_min(&p.minval[r.a], wk | (seg0 + offs[j]));
+          red_min(&p.minval[r.b], wk | (seg0 + offs[j]));
+        }
       }
     } else {
       constexpr int G = 4;  // items per batch of filter reads
@@ -202,9 +211,11 @@ __device__ __forceinline__ void seg_tile_finish(const uint8_t (&cls)[ITEMS], uin
         for (int q = 0; q < G && g + q < ITEMS; ++q) {
           if (!((min_mask >> (g + q)) & 1u)) continue;
           const Rec r = rec((g + q) * kBlock + threadIdx.x);
-          const uint64_t v = (static_cast<uint64_t>(r.w) << 32) | (seg0 + offs[g + q]);
-          if (v < cur[2 * q]) red_min(&p.minval[r.a], v);
-          if (v < cur[2 * q + 1]) red_min(&p.minval[r.b], v);
+          const uint64_t wk = static_cast<uint64_t>(r.w) << 32;
+          const uint64_t va = p.min_partner ? (wk | r.b) : (wk | (seg0 + offs[g + q]));
+          const uint64_t vb = p.min_partner ? (wk | r.a) : (wk | (seg0 + offs[g + q]));
+          if (va < cur[2 * q]) red_min(&p.minval[r.a], va);
+          if (vb < cur[2 * q + 1]) red_min(&p.minval[r.b], vb);
         }
       }
     }
@@ -625,14 +636,48 @@ __global__ void k_dedupe_mark(const uint64_t* __restrict__ keys, const uint32_t*
 // minima -- so several independent random reads are in flight per thread.
 constexpr int kIlp = 4;
 
-// With hook_w set (the first round over original ids, whose forest edges
-// are emitted directly), msfoid receives the partner and hook_w the weight
-// instead of the input position.
+// Hook every vertex along its minimum edge (determine_mst_edges,
+// mst_utils_plain.hpp:31-64); a mutual minimum roots the lower id.  With
+// `partner_keys` (the first round over original ids, whose minima are
+// (w << 32 | partner) keys) the partner comes from the key and no record is
+// gathered; otherwise the key's low word is the record's list position and
+// msfoid receives the record's input position.
 __global__ void k_hook(uint32_t n, const uint64_t* __restrict__ minval,
                        const Rec* __restrict__ list, uint32_t* __restrict__ parent,
-                       uint32_t* __restrict__ msfoid, uint32_t* __restrict__ hook_w,
-                       uint32_t* err) {
+                       uint32_t* __restrict__ msfoid, uint32_t partner_keys, uint32_t* err) {
   const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  if (partner_keys) {
+    for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; base < n;
+         base += kIlp * stride) {
+      uint64_t val[kIlp], mu[kIlp];
+#pragma unroll
+      for (int k = 0; k < kIlp; ++k) {
+        const uint64_t v = base + k * stride;
+        val[k] = v < n ? minval[v] : kInf64;
+      }
+#pragma unroll
+      for (int k = 0; k < kIlp; ++k) {
+        mu[k] = kInf64;
+        if (val[k] == kInf64) continue;
+        const uint32_t u = static_cast<uint32_t>(val[k]);
+        if (u >= n) {
+          val[k] = kInf64;
+          atomicOr(err, kErrHook);
+          continue;
+        }
+        mu[k] = minval[u];
+      }
+#pragma unroll
+      for (int k = 0; k < kIlp; ++k) {
+        const uint64_t vv = base + k * stride;
+        if (vv >= n) continue;
+        const uint32_t v = static_cast<uint32_t>(vv), u = static_cast<uint32_t>(val[k]);
+        const uint64_t back = (val[k] & 0xffffffff00000000ull) | v;  // u's key if mutual
+        parent[v] = (val[k] == kInf64 || (mu[k] == back && v < u)) ? v : u;
+      }
+    }
+    return;
+  }
   for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; base < n;
        base += kIlp * stride) {
     uint64_t val[kIlp], mu[kIlp];
@@ -670,12 +715,7 @@ __global__ void k_hook(uint32_t n, const uint64_t* __restrict__ minval,
         msfoid[v] = kNone;
       } else {
         parent[v] = u[k];
-        if (hook_w) {
-          msfoid[v] = u[k];
-          hook_w[v] = r[k].w;
-        } else {
-          msfoid[v] = r[k].oid;
-        }
+        msfoid[v] = r[k].oid;
       }
     }
   }
@@ -758,12 +798,11 @@ struct VertexScanArgs {
   uint32_t* cta_counts;  // 2 per CTA: roots, hooked
   unsigned long long* counts;  // [0] roots, [1] forest edges (totals)
   uint32_t* err;
-  // direct emission (first round over original ids): forest edge k of the
-  // round is written as (min, max, w) at direct_out[3k..], from the partner
-  // in msfoid and the weight in hook_w; the weights are summed into
-  // direct_weight.  Null: msf_out receives input positions as usual.
+  // direct emission (first round over original ids, minima as (w << 32 |
+  // partner) keys): forest edge k of the round is written as (min, max, w)
+  // at direct_out[3k..] from the hooked vertex's key, and the weights are
+  // summed into direct_weight.  Null: msf_out receives input positions.
   uint32_t* direct_out;
-  const uint32_t* hook_w;
   unsigned long long* direct_weight;
 };
 
@@ -856,7 +895,8 @@ __global__ void __launch_bounds__(kBlock) k_vertex_write(VertexScanArgs p) {
       if (k >= p.msf_cap) {
         atomicOr(p.err, kErrOverflow);
       } else if (p.direct_out) {
-        const uint32_t u = p.msfoid[v], w = p.hook_w[v];
+        const uint64_t key = p.minval[v];
+        const uint32_t u = static_cast<uint32_t>(key), w = static_cast<uint32_t>(key >> 32);
         uint32_t* o = p.direct_out + 3ull * k;
         o[0] = v < u ? v : u;
         o[1] = v < u ? u : v;

@@ -240,9 +240,8 @@ class Solve {
   // lightest class) writes its forest edges to the output itself, so the
   // final emit gathers only the later rounds' edges from the input.
   kamsta_wedge* d_out_ = nullptr;
-  uint32_t* hookw_ = nullptr;           // weight of each hooked vertex's edge
   unsigned long long* dweight_ = nullptr;  // weight of the directly written edges
-  bool direct_emit_ = false;            // the next round may emit directly
+  bool direct_emit_ = false;  // the first pass keys minima by partner; round 0 emits
   uint64_t direct_count_ = 0;           // forest edges written directly
   std::vector<uint32_t> bounds_;        // ascending weight-class bounds
   std::vector<uint32_t> samples_host_;  // sorted weight sample of the input
@@ -255,7 +254,7 @@ kamsta_status Solve::alloc_fixed() {
   const uint64_t n = n_;
   size_t bytes = 0;
   auto add = [&](uint64_t count, size_t sz) { bytes += round_up(count * sz, 256); };
-  for (int i = 0; i < 10; ++i) add(n + 1, 4);  // P D V Vn dense parent msfoid newid msf hookw
+  for (int i = 0; i < 9; ++i) add(n + 1, 4);  // P D V Vn dense parent msfoid newid msf
   add(2 * n + 64, 4);                         // Rbuf
   add(n + 64, 4);                             // Obuf
   add(n + 1, 8);
@@ -275,7 +274,6 @@ kamsta_status Solve::alloc_fixed() {
   msfoid_ = A.take<uint32_t>(n + 1);
   newid_ = A.take<uint32_t>(n + 1);
   msf_ = A.take<uint32_t>(n + 1);
-  hookw_ = A.take<uint32_t>(n + 1);
   Rbuf_ = A.take<uint32_t>(2 * n + 64);
   Obuf_ = A.take<uint32_t>(n + 64);
   minA_ = A.take<uint64_t>(n + 1);
@@ -464,6 +462,7 @@ kamsta_status Solve::pass(int phase, const SegList* src, const uint32_t* map, ui
     // original ids (no map): few updates per address, reductions go straight
     // out; relabelled lists have hub components, so updates are filtered
     a.min_checked = map != nullptr ? 1u : 0u;
+    a.min_partner = (direct_emit_ && src == nullptr && map == nullptr) ? 1u : 0u;
     a.total = total;
     a.chunk = chunk;
     a.counts = ctx_->d_counters[kCEdge].cnt;
@@ -615,11 +614,11 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
     CU_TRY(cudaMemsetAsync(ctx_->d_counters + kCVertex, 0, sizeof(DevCounters), st_));
     const int gv = grid_for(nr);
     const int tv = tick();
-    // direct emission needs original ids (the first round of the first
-    // contraction) and an empty forest so far
-    const bool direct = direct_emit_ && r == 0 && msf_count_ == 0 && n_ >= 2;
-    k_hook<<<gv, kBlock, 0, st_>>>(nr, minv, cur->base, parent_, msfoid_,
-                                   direct ? hookw_ : nullptr, ctx_->d_err);
+    // the first round of the first contraction: original ids, minima keyed
+    // by partner (first pass), forest edges written directly
+    const bool direct = direct_emit_ && r == 0;
+    k_hook<<<gv, kBlock, 0, st_>>>(nr, minv, cur->base, parent_, msfoid_, direct ? 1u : 0u,
+                                   ctx_->d_err);
     k_jump<<<gv, kBlock, 0, st_>>>(nr, parent_, ctx_->d_err);
     uint32_t* onext = Obuf_ + ooff;
     VertexScanArgs va{};
@@ -645,7 +644,6 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
     va.err = ctx_->d_err;
     if (direct) {
       va.direct_out = reinterpret_cast<uint32_t*>(d_out_);
-      va.hook_w = hookw_;
       va.direct_weight = dweight_;
       va.msf_cap = n_ - 1;  // the caller's output capacity
     }
@@ -663,10 +661,12 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
     const uint64_t added = ctx_->h_counters[kCVertex].cnt[1];
     // hook: minimum, record gather, partner minimum, parent + edge id;
     // jump: parent reads/writes; scan: parent, minimum, orig per vertex and
-    // id/orig/minimum per root, edge id per hooked vertex; map: 3 reads + 1 write
+    // id/orig/minimum per root, edge id per hooked vertex; map: 3 reads + 1 write.
+    // The direct first round gathers no record and writes no edge id; it
+    // reads each hooked vertex's key and writes its 12-byte forest edge.
     account(KAMSTA_PHASE_ROUND_VERTS,
             uint64_t(nr) * ((8 + 16 + 8 + 8) + 16 + (4 + 8 + 4) + (8 + 4 + 4)) + n_next * 16 +
-                added * (direct ? 4 + 4 + 4 + 12 : 8),
+                added * (direct ? 8 + 12 : 8) - (direct ? uint64_t(nr) * 20 : 0),
             6);
     if (direct) direct_count_ = added;
     if (debug_) {
@@ -935,6 +935,9 @@ kamsta_status Solve::run_boruvka() {
     for (int c = 0; c < nmat; ++c)
       frac[c] = sample_share(samples_host_, c == 0 ? 0u : b[c - 1] + 1, b[c]);
   const bool validate = (cfg_.flags & KAMSTA_FLAG_VALIDATE) != 0;
+  // direct emission: the first pass keys the round-0 minima by partner and
+  // the first round writes its forest edges to the output
+  direct_emit_ = d_out_ != nullptr && forest_bits_ == nullptr && n_ >= 2 && msf_count_ == 0;
   switch (nmat) {
     case 1:
       KS_TRY(pass<1>(KAMSTA_PHASE_FIRST_PASS, nullptr, nullptr, 0, wmax0, nullptr, C, frac, minA_,
@@ -954,7 +957,6 @@ kamsta_status Solve::run_boruvka() {
   const int steps = nmat + std::max(0, K - nmat + 1);
   int step = 0;
   final_contraction_ = ++step == steps;
-  direct_emit_ = d_out_ != nullptr && forest_bits_ == nullptr;
   const kamsta_status first = rounds(C[0], true);
   direct_emit_ = false;
   KS_TRY(first);
