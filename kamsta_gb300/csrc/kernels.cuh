@@ -806,21 +806,55 @@ struct VertexScanArgs {
   unsigned long long* direct_weight;
 };
 
-__device__ __forceinline__ uint32_t vertex_class(const VertexScanArgs& p, uint32_t v) {
-  if (v >= p.n) return 2;
-  const uint32_t par = p.parent[v];
+// Vertices per thread per step of the compaction kernels: the loads of a
+// step's vertices are all in flight before any is used, and one ranking
+// (two barriers) covers kScanItems * kBlock vertices.
+constexpr int kScanItems = 4;
+
+// Class of vertex v from its parent and minimum: 0 = live root, 1 = hooked,
+// 0xff = finished (a root without edges) or outside the range.
+__device__ __forceinline__ uint8_t vertex_class(uint32_t v, uint32_t par, uint64_t minv) {
   if (par != v) return 1;
-  return p.minval[v] != kInf64 ? 0u : 2u;
+  return minv != kInf64 ? 0 : 0xff;
+}
+
+// Loads and classes of one step: item j of thread t is vertex r0 + j*kBlock
+// + t (so ranking by (j, t) is vertex order).  The minimum is read for the
+// roots, and for every vertex when `all_min` is set.
+__device__ __forceinline__ void vertex_step(const VertexScanArgs& p, uint32_t r0, uint32_t hi,
+                                            bool all_min, uint8_t (&cls)[kScanItems],
+                                            uint64_t (&mv)[kScanItems]) {
+  uint32_t par[kScanItems];
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    const uint32_t v = r0 + j * kBlock + threadIdx.x;
+    par[j] = v < hi ? p.parent[v] : v;
+  }
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    const uint32_t v = r0 + j * kBlock + threadIdx.x;
+    mv[j] = (v < hi && (all_min || par[j] == v)) ? p.minval[v] : kInf64;
+  }
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    const uint32_t v = r0 + j * kBlock + threadIdx.x;
+    cls[j] = v < hi ? vertex_class(v, par[j], mv[j]) : 0xff;
+  }
 }
 
 __global__ void __launch_bounds__(kBlock) k_vertex_count(VertexScanArgs p) {
   const uint32_t lo = blockIdx.x * p.chunk;
   const uint32_t hi = min(lo + p.chunk, p.n);
   uint32_t c0 = 0, c1 = 0;
-  for (uint32_t v = lo + threadIdx.x; v < hi; v += kBlock) {
-    const uint32_t c = vertex_class(p, v);
-    c0 += c == 0;
-    c1 += c == 1;
+  for (uint32_t r0 = lo; r0 < hi; r0 += kScanItems * kBlock) {
+    uint8_t cls[kScanItems];
+    uint64_t mv[kScanItems];
+    vertex_step(p, r0, hi, false, cls, mv);
+#pragma unroll
+    for (int j = 0; j < kScanItems; ++j) {
+      c0 += cls[j] == 0;
+      c1 += cls[j] == 1;
+    }
   }
   __shared__ uint32_t s_c[2];
   if (threadIdx.x < 2) s_c[threadIdx.x] = 0;
@@ -842,7 +876,8 @@ __global__ void __launch_bounds__(kBlock) k_vertex_count(VertexScanArgs p) {
 
 __global__ void __launch_bounds__(kBlock) k_vertex_write(VertexScanArgs p) {
   __shared__ uint32_t s_base[2];
-  __shared__ uint32_t s_w[2][kBlock / 32];
+  __shared__ uint32_t s_rank[2 * kScanItems * (kBlock / 32)];
+  __shared__ uint32_t s_tot[2];
   if (threadIdx.x < 32) {  // bases: counts of the CTAs before this one
     uint32_t b0 = 0, b1 = 0;
     for (uint32_t c = threadIdx.x; c < blockIdx.x; c += 32) {
@@ -859,59 +894,60 @@ __global__ void __launch_bounds__(kBlock) k_vertex_write(VertexScanArgs p) {
   __syncthreads();
   const uint32_t lo = blockIdx.x * p.chunk;
   const uint32_t hi = min(lo + p.chunk, p.n);
-  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5, lt = lanemask_lt();
+  const bool direct = p.direct_out != nullptr;
   uint32_t run0 = s_base[0], run1 = s_base[1];
   uint64_t wsum = 0;
-  for (uint32_t v0 = lo; v0 < hi; v0 += kBlock) {  // rows of kBlock vertices, in order
-    const uint32_t v = v0 + threadIdx.x;
-    const uint32_t c = v < hi ? vertex_class(p, v) : 2u;
-    const uint32_t b0 = __ballot_sync(kFull, c == 0), b1 = __ballot_sync(kFull, c == 1);
-    if (lane == 0) {
-      s_w[0][warp] = __popc(b0);
-      s_w[1][warp] = __popc(b1);
-    }
-    __syncthreads();
-    uint32_t pre0 = run0, pre1 = run1, tot0 = 0, tot1 = 0;
+  for (uint32_t r0 = lo; r0 < hi; r0 += kScanItems * kBlock) {  // steps in vertex order
+    uint8_t cls[kScanItems];
+    uint64_t mv[kScanItems];
+    vertex_step(p, r0, hi, direct, cls, mv);
+    uint32_t offs[kScanItems];
 #pragma unroll
-    for (int w = 0; w < kBlock / 32; ++w) {
-      const uint32_t x0 = s_w[0][w], x1 = s_w[1][w];
-      pre0 += static_cast<uint32_t>(w) < warp ? x0 : 0u;
-      pre1 += static_cast<uint32_t>(w) < warp ? x1 : 0u;
-      tot0 += x0;
-      tot1 += x1;
+    for (int j = 0; j < kScanItems; ++j) offs[j] = 0;
+    tile_rank<2, kScanItems, kBlock>(cls, offs, s_rank, s_tot);
+    const uint32_t tot0 = s_tot[0], tot1 = s_tot[1];
+    // the per-class loads of all items first, then the writes
+    uint32_t carry[kScanItems];
+#pragma unroll
+    for (int j = 0; j < kScanItems; ++j) {
+      const uint32_t v = r0 + j * kBlock + threadIdx.x;
+      carry[j] = cls[j] == 0 ? p.orig_cur[v] : (cls[j] == 1 && !direct) ? p.msfoid[v] : 0u;
     }
-    __syncthreads();
-    if (c == 0) {
-      const uint32_t id = pre0 + __popc(b0 & lt);
-      if (id < p.orig_cap) {
-        p.newid[v] = id;
-        p.orig_next[id] = p.orig_cur[v];
-        p.minval_next[id] = kInf64;
-      } else {
-        atomicOr(p.err, kErrOverflow);
-      }
-    } else if (c == 1) {
-      const uint32_t k = pre1 + __popc(b1 & lt);
-      if (k >= p.msf_cap) {
-        atomicOr(p.err, kErrOverflow);
-      } else if (p.direct_out) {
-        const uint64_t key = p.minval[v];
-        const uint32_t u = static_cast<uint32_t>(key), w = static_cast<uint32_t>(key >> 32);
-        uint32_t* o = p.direct_out + 3ull * k;
-        o[0] = v < u ? v : u;
-        o[1] = v < u ? u : v;
-        o[2] = w;
-        wsum += w;
-      } else {
-        p.msf_out[k] = p.msfoid[v];
+#pragma unroll
+    for (int j = 0; j < kScanItems; ++j) {
+      const uint32_t v = r0 + j * kBlock + threadIdx.x;
+      if (cls[j] == 0) {
+        const uint32_t id = run0 + offs[j];
+        if (id < p.orig_cap) {
+          p.newid[v] = id;
+          p.orig_next[id] = carry[j];
+          p.minval_next[id] = kInf64;
+        } else {
+          atomicOr(p.err, kErrOverflow);
+        }
+      } else if (cls[j] == 1) {
+        const uint32_t k = run1 + offs[j];
+        if (k >= p.msf_cap) {
+          atomicOr(p.err, kErrOverflow);
+        } else if (direct) {
+          const uint32_t u = static_cast<uint32_t>(mv[j]), w = static_cast<uint32_t>(mv[j] >> 32);
+          uint32_t* o = p.direct_out + 3ull * k;
+          o[0] = v < u ? v : u;
+          o[1] = v < u ? u : v;
+          o[2] = w;
+          wsum += w;
+        } else {
+          p.msf_out[k] = carry[j];
+        }
       }
     }
     run0 += tot0;
     run1 += tot1;
+    __syncthreads();  // s_rank / s_tot are reused by the next step
   }
-  if (p.direct_out) {
+  if (direct) {
     wsum = warp_sum(wsum);
-    if (lane == 0 && wsum) atomicAdd(p.direct_weight, static_cast<unsigned long long>(wsum));
+    if (lane_id() == 0 && wsum) atomicAdd(p.direct_weight, static_cast<unsigned long long>(wsum));
   }
 }
 
@@ -1032,13 +1068,37 @@ struct RepScanArgs {
   uint32_t* err;
 };
 
+// Representatives of one step (kScanItems vertices per thread, item j of
+// thread t = entry r0 + j*kBlock + t): keep[j] iff V[i] is still its own
+// final label.
+__device__ __forceinline__ void rep_step(const RepScanArgs& p, uint32_t r0, uint32_t hi,
+                                         uint8_t (&cls)[kScanItems],
+                                         uint32_t (&v)[kScanItems]) {
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    const uint32_t i = r0 + j * kBlock + threadIdx.x;
+    v[j] = i < hi ? p.V[i] : 0u;
+  }
+  uint32_t pv[kScanItems];
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    const uint32_t i = r0 + j * kBlock + threadIdx.x;
+    pv[j] = i < hi ? p.P[v[j]] : ~v[j];
+  }
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) cls[j] = pv[j] == v[j] ? 0 : 0xff;
+}
+
 __global__ void __launch_bounds__(kBlock) k_rep_count(RepScanArgs p) {
   const uint32_t lo = blockIdx.x * p.chunk;
   const uint32_t hi = min(lo + p.chunk, p.n);
   uint32_t c0 = 0;
-  for (uint32_t i = lo + threadIdx.x; i < hi; i += kBlock) {
-    const uint32_t v = p.V[i];
-    c0 += p.P[v] == v;
+  for (uint32_t r0 = lo; r0 < hi; r0 += kScanItems * kBlock) {
+    uint8_t cls[kScanItems];
+    uint32_t v[kScanItems];
+    rep_step(p, r0, hi, cls, v);
+#pragma unroll
+    for (int j = 0; j < kScanItems; ++j) c0 += cls[j] == 0;
   }
   __shared__ uint32_t s_c;
   if (threadIdx.x == 0) s_c = 0;
@@ -1054,7 +1114,8 @@ __global__ void __launch_bounds__(kBlock) k_rep_count(RepScanArgs p) {
 
 __global__ void __launch_bounds__(kBlock) k_rep_write(RepScanArgs p) {
   __shared__ uint32_t s_base;
-  __shared__ uint32_t s_w[kBlock / 32];
+  __shared__ uint32_t s_rank[kScanItems * (kBlock / 32)];
+  __shared__ uint32_t s_tot[1];
   if (threadIdx.x < 32) {
     uint32_t b = 0;
     for (uint32_t c = threadIdx.x; c < blockIdx.x; c += 32) b += p.cta_counts[c];
@@ -1064,28 +1125,25 @@ __global__ void __launch_bounds__(kBlock) k_rep_write(RepScanArgs p) {
   __syncthreads();
   const uint32_t lo = blockIdx.x * p.chunk;
   const uint32_t hi = min(lo + p.chunk, p.n);
-  const uint32_t lane = lane_id(), warp = threadIdx.x >> 5, lt = lanemask_lt();
   uint32_t run = s_base;
-  for (uint32_t i0 = lo; i0 < hi; i0 += kBlock) {
-    const uint32_t i = i0 + threadIdx.x;
-    const uint32_t v = i < hi ? p.V[i] : 0u;
-    const bool keep = i < hi && p.P[v] == v;
-    const uint32_t b = __ballot_sync(kFull, keep);
-    if (lane == 0) s_w[warp] = __popc(b);
-    __syncthreads();
-    uint32_t pre = run, tot = 0;
+  for (uint32_t r0 = lo; r0 < hi; r0 += kScanItems * kBlock) {
+    uint8_t cls[kScanItems];
+    uint32_t v[kScanItems];
+    rep_step(p, r0, hi, cls, v);
+    uint32_t offs[kScanItems];
 #pragma unroll
-    for (int w = 0; w < kBlock / 32; ++w) {
-      pre += static_cast<uint32_t>(w) < warp ? s_w[w] : 0u;
-      tot += s_w[w];
-    }
-    __syncthreads();
-    if (keep) {
-      const uint32_t k = pre + __popc(b & lt);
-      p.Vout[k] = v;
-      p.dense_of[v] = k;
+    for (int j = 0; j < kScanItems; ++j) offs[j] = 0;
+    tile_rank<1, kScanItems, kBlock>(cls, offs, s_rank, s_tot);
+    const uint32_t tot = s_tot[0];
+#pragma unroll
+    for (int j = 0; j < kScanItems; ++j) {
+      if (cls[j] != 0) continue;
+      const uint32_t k = run + offs[j];
+      p.Vout[k] = v[j];
+      p.dense_of[v[j]] = k;
     }
     run += tot;
+    __syncthreads();  // s_rank / s_tot are reused by the next step
   }
 }
 
