@@ -724,7 +724,12 @@ __global__ void k_hook(uint32_t n, const uint64_t* __restrict__ minval,
 // Pointer jumping to the roots (update_parents, gbbs_reimplementation.hpp:
 // 161-169) with path halving; every write stores an ancestor, so concurrent
 // updates stay correct.  Capped; the cap reports kErrJump.
-__global__ void k_jump(uint32_t n, uint32_t* parent, uint32_t* err) {
+// Each walk ends at its start vertex's root (the walk stops on a vertex that
+// is its own parent), which is written to root_out[v] -- by v's thread
+// alone, so unlike parent[v] it is never overwritten with a nearer ancestor
+// by another walk.
+__global__ void k_jump(uint32_t n, uint32_t* parent, uint32_t* __restrict__ root_out,
+                       uint32_t* err) {
   const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
   for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; base < n;
        base += kIlp * stride) {
@@ -770,7 +775,9 @@ __global__ void k_jump(uint32_t n, uint32_t* parent, uint32_t* err) {
 #pragma unroll
     for (int k = 0; k < kIlp; ++k) {
       const uint64_t v = base + k * stride;
-      if (v < n && p[k] != static_cast<uint32_t>(v)) st_relaxed(parent + v, p[k]);
+      if (v >= n) continue;
+      if (p[k] != static_cast<uint32_t>(v)) st_relaxed(parent + v, p[k]);
+      root_out[v] = p[k];
     }
   }
 }
@@ -952,51 +959,32 @@ __global__ void __launch_bounds__(kBlock) k_vertex_write(VertexScanArgs p) {
 }
 
 // Label map of one round: dense id in round r -> dense id in round r+1, or
-// kNone for a finished vertex.  The root is found by following the parent
-// pointers that k_jump's path halving may have left a level or two short
-// (read only, capped like k_jump), so no separate pass is needed.
+// kNone for a finished vertex (a root without edges).  R holds each
+// vertex's root on entry (k_jump) and its new label on return: one gather
+// of the root's new id per hooked vertex.
 __global__ void k_map(uint32_t n, const uint64_t* __restrict__ minval,
-                      const uint32_t* __restrict__ parent,
-                      const uint32_t* __restrict__ newid, uint32_t* __restrict__ R,
-                      uint32_t* err) {
+                      const uint32_t* __restrict__ newid, uint32_t* __restrict__ R) {
   const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
   for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; base < n;
        base += kIlp * stride) {
-    uint32_t p[kIlp], q[kIlp];
-    bool live[kIlp];
+    uint32_t rt[kIlp];
 #pragma unroll
     for (int k = 0; k < kIlp; ++k) {
       const uint64_t v = base + k * stride;
-      live[k] = v < n;
-      p[k] = live[k] ? parent[v] : 0u;
+      rt[k] = v < n ? R[v] : 0u;
     }
-#pragma unroll
-    for (int k = 0; k < kIlp; ++k) q[k] = live[k] ? parent[p[k]] : 0u;
+    uint32_t q[kIlp];
 #pragma unroll
     for (int k = 0; k < kIlp; ++k) {
-      if (!live[k]) continue;
-      const uint32_t v = static_cast<uint32_t>(base + k * stride);
-      if (p[k] == v) {  // a root
-        q[k] = minval[v] == kInf64 ? kNone : v;
-        continue;
-      }
-      // follow pointers k_jump left short of the root (rare, capped)
-      uint32_t x = p[k], y = q[k], steps = 0;
-      while (y != x) {
-        x = y;
-        y = parent[x];
-        if ((++steps & 1023u) == 0 && (steps > kJumpCap || (ld_relaxed(err) & kErrJump))) {
-          atomicOr(err, kErrJump);
-          break;
-        }
-      }
-      q[k] = x;
-    }
-#pragma unroll
-    for (int k = 0; k < kIlp; ++k) {
-      if (!live[k]) continue;
       const uint64_t v = base + k * stride;
-      R[v] = q[k] == kNone ? kNone : newid[q[k]];
+      q[k] = kNone;
+      if (v >= n) continue;
+      if (rt[k] != static_cast<uint32_t>(v) || minval[v] != kInf64) q[k] = newid[rt[k]];
+    }
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k) {
+      const uint64_t v = base + k * stride;
+      if (v < n) R[v] = q[k];
     }
   }
 }

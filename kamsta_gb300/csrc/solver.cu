@@ -619,7 +619,8 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
     const bool direct = direct_emit_ && r == 0;
     k_hook<<<gv, kBlock, 0, st_>>>(nr, minv, cur->base, parent_, msfoid_, direct ? 1u : 0u,
                                    ctx_->d_err);
-    k_jump<<<gv, kBlock, 0, st_>>>(nr, parent_, ctx_->d_err);
+    uint32_t* R = Rbuf_ + roff;
+    k_jump<<<gv, kBlock, 0, st_>>>(nr, parent_, R, ctx_->d_err);
     uint32_t* onext = Obuf_ + ooff;
     VertexScanArgs va{};
     va.n = nr;
@@ -649,8 +650,7 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
     }
     k_vertex_count<<<gvs, kBlock, 0, st_>>>(va);
     k_vertex_write<<<gvs, kBlock, 0, st_>>>(va);
-    uint32_t* R = Rbuf_ + roff;
-    k_map<<<gv, kBlock, 0, st_>>>(nr, minv, parent_, newid_, R, ctx_->d_err);
+    k_map<<<gv, kBlock, 0, st_>>>(nr, minv, newid_, R);
     tock(KAMSTA_PHASE_ROUND_VERTS, tv);
     // relabel + self-loop removal + compaction + next-round minimum
     SegList* nxt = new_list();
