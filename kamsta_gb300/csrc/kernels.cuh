@@ -4,13 +4,13 @@
 //   compute_min_edges             mst_utils_common.hpp:84-105     -> fused into k_pass_*
 //   determine_mst_edges(_exhausted) mst_utils_cut_edges.hpp:102-166 -> k_hook
 //   update_parents                gbbs_reimplementation.hpp:161-169 -> k_jump
-//   add_new_mst_edges_to_mst_array gbbs_reimplementation.hpp:137-159 -> k_vertex_scan
-//   compactify_vertices           mst_utils_common.hpp:122-132    -> k_vertex_scan
+//   add_new_mst_edges_to_mst_array gbbs_reimplementation.hpp:137-159 -> k_vertex_count/write
+//   compactify_vertices           mst_utils_common.hpp:122-132    -> k_vertex_count/write
 //   relabel_edges + filter_out_self_loops  mst_utils_plain.hpp:7-29,
 //                                 mst_utils_common.hpp:157-175    -> k_pass_seg
 //   localMST::partition / filter  mst_utils_filter.hpp:39-126     -> k_pass_dir / k_pass_seg
 //   final parent shortcut         local_mst_respecting_cut_edges.hpp:199-203
-//                                                                  -> k_chase + k_relabel_all
+//                                                                  -> k_compose + k_rep_* + k_relabel_all
 #pragma once
 #include "common.cuh"
 
@@ -19,7 +19,6 @@ namespace kamsta {
 constexpr int kBlock = 256;
 constexpr int kItemsDir = 8;    // directed 12-byte records per thread (default tile)
 constexpr int kItemsRec = 2;    // 16-byte records per thread (default tile)
-constexpr int kItemsVtx = 8;    // vertices per thread in the vertex scans
 constexpr int kMaxOut = 3;      // weight classes materialised by one pass
 
 // ---------------------------------------------------------------------------
@@ -989,61 +988,42 @@ __global__ void k_map(uint32_t n, const uint64_t* __restrict__ minval,
   }
 }
 
-// Final labels of one Boruvka call: follow the round maps of every round-0
-// vertex to its finished component and write that component's original
-// representative into P.
+// Final labels of one Boruvka call, composed backwards over the round maps.
+// For round r (vertices x < n_r), the map R_r holds x's round-(r+1) label or
+// kNone once x's component is finished; afterwards R_r[x] holds the original
+// representative of x's final component:
+//   F_r[x] = R_r[x] == kNone ? orig_r[x] : F_{r+1}[R_r[x]],
+// with F_rounds = orig_rounds (the components left after the last round).
+// Launched for r = rounds-1 down to 0, so each map is read and gathered
+// once (sum of n_r gathers, not n_0 walks through every round).  For r = 0
+// the result goes to P at each vertex's original id instead.
 constexpr int kMaxRounds = 40;
-struct ChaseArgs {
-  uint32_t n0;
-  uint32_t rounds;
-  const uint32_t* R[kMaxRounds];
-  const uint32_t* orig[kMaxRounds + 1];
-  uint32_t* P;
-  uint32_t* err;
-};
-
-__global__ void k_chase(ChaseArgs p) {
+__global__ void k_compose(uint32_t n, uint32_t* __restrict__ R, const uint32_t* __restrict__ next,
+                          const uint32_t* __restrict__ orig, uint32_t* __restrict__ P) {
   const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
-  for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; base < p.n0;
+  for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; base < n;
        base += kIlp * stride) {
-    // kIlp chains walked side by side, one round map at a time
-    uint32_t x[kIlp], rep[kIlp];
-    bool run[kIlp];
+    uint32_t y[kIlp], o[kIlp];
 #pragma unroll
     for (int k = 0; k < kIlp; ++k) {
-      const uint64_t i = base + k * stride;
-      run[k] = i < p.n0;
-      x[k] = static_cast<uint32_t>(i);
-      rep[k] = kNone;
+      const uint64_t x = base + k * stride;
+      y[k] = x < n ? R[x] : kNone;
+      o[k] = x < n ? orig[x] : 0u;
     }
-    for (uint32_t r = 0; r < p.rounds; ++r) {
-      uint32_t y[kIlp];
 #pragma unroll
-      for (int k = 0; k < kIlp; ++k) y[k] = run[k] ? p.R[r][x[k]] : 0u;
-#pragma unroll
-      for (int k = 0; k < kIlp; ++k) {
-        if (!run[k]) continue;
-        if (y[k] == kNone) {
-          rep[k] = p.orig[r][x[k]];
-          run[k] = false;
-        } else {
-          x[k] = y[k];
-        }
-      }
-    }
+    for (int k = 0; k < kIlp; ++k)
+      if (y[k] != kNone) y[k] = next[y[k]];
 #pragma unroll
     for (int k = 0; k < kIlp; ++k) {
-      const uint64_t i = base + k * stride;
-      if (i >= p.n0) continue;
-      const uint32_t r0 = rep[k] == kNone ? p.orig[p.rounds][x[k]] : rep[k];
-      p.P[p.orig[0][i]] = r0;
+      const uint64_t x = base + k * stride;
+      if (x >= n) continue;
+      const uint32_t f = y[k] == kNone ? o[k] : y[k];
+      if (P) P[o[k]] = f;
+      else R[x] = f;
     }
   }
 }
 
-// New representative list of the call (V' = {v in V : P[v] == v}, stable)
-// and the dense numbering of those representatives; count + write kernels
-// over per-CTA chunks as for the vertex scan.
 struct RepScanArgs {
   uint32_t n;
   uint32_t chunk;

@@ -594,9 +594,11 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
   uint32_t nr = n0;
   uint64_t* minv = minA_;
   uint64_t* minn = minB_;
-  ChaseArgs ca{};
-  ca.n0 = n0;
-  ca.orig[0] = V_;
+  // per round: its map, its vertices' original representatives, its size
+  uint32_t* maps[kMaxRounds];
+  const uint32_t* origs[kMaxRounds + 1];
+  uint32_t sizes[kMaxRounds];
+  origs[0] = V_;
   size_t roff = 0, ooff = 0;
   uint32_t r = 0;
   const uint32_t* orig_cur = V_;
@@ -681,8 +683,9 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
       set_error("internal: forest larger than n-1");
       return KAMSTA_E_CUDA;
     }
-    ca.R[r] = R;
-    ca.orig[r + 1] = onext;
+    maps[r] = R;
+    sizes[r] = nr;
+    origs[r + 1] = onext;
     roff += nr;
     ooff += n_next;
     orig_cur = onext;
@@ -697,11 +700,14 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
   rounds_ += r;
   if (r == 0) return KAMSTA_OK;  // nothing contracted; labels unchanged
   if (final_contraction_) return KAMSTA_OK;  // no later pass needs the labels
-  ca.rounds = r;
-  ca.P = P_;
-  ca.err = ctx_->d_err;
   const int tf = tick();
-  k_chase<<<grid_for(n0), kBlock, 0, st_>>>(ca);
+  uint64_t composed = 0;
+  for (int k = static_cast<int>(r) - 1; k >= 0; --k) {
+    const uint32_t* next = k + 1 == static_cast<int>(r) ? origs[r] : maps[k + 1];
+    k_compose<<<grid_for(sizes[k]), kBlock, 0, st_>>>(sizes[k], maps[k], next, origs[k],
+                                                      k == 0 ? P_ : nullptr);
+    composed += sizes[k];
+  }
   CU_TRY(cudaMemsetAsync(ctx_->d_counters + kCRep, 0, sizeof(DevCounters), st_));
   RepScanArgs ra{};
   ra.n = n0;
@@ -724,8 +730,10 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
   tock(KAMSTA_PHASE_FINALIZE, tf);
   CU_TRY(cudaGetLastError());
   KS_TRY(fetch_counters());
-  account(KAMSTA_PHASE_FINALIZE,
-          uint64_t(n0) * (4 * r + 12) + uint64_t(n0) * 16 + uint64_t(n_) * 16, 4);
+  // compose: map + orig read, one gather, one write per round vertex; rep
+  // scan: 16 per level vertex; relabel_all: 16 per vertex
+  account(KAMSTA_PHASE_FINALIZE, composed * 16 + uint64_t(n0) * 16 + uint64_t(n_) * 16,
+          static_cast<uint32_t>(r) + 3);
   nreps_ = static_cast<uint32_t>(ctx_->h_counters[kCRep].cnt[0]);
   std::swap(V_, Vn_);
   return KAMSTA_OK;
