@@ -236,3 +236,82 @@ def test_tile_sizes_agree(kamsta, oracle, items, seg):
                                      seg_items_per_thread=seg)
         _check(oracle, kamsta.boruvka(e, cfg, n=n), e, n)
         _check(oracle, kamsta.filter_boruvka(e, cfg, n=n), e, n)
+
+
+def _disjoint_dense(kamsta, comps, size, seed, wmax):
+    """`comps` disjoint complete graphs of `size` vertices, weights U[1, wmax],
+    both directions, (src, dst)-sorted: every component contracts to one
+    vertex within a few rounds while most of its edges are still listed."""
+    rng = np.random.default_rng(seed)
+    iu, ju = np.triu_indices(size, 1)
+    base = (np.arange(comps, dtype=np.int64) * size)[:, None]
+    u = (base + iu[None, :]).ravel()
+    v = (base + ju[None, :]).ravel()
+    w = rng.integers(1, wmax + 1, len(u))
+    s, d, ww = np.concatenate([u, v]), np.concatenate([v, u]), np.concatenate([w, w])
+    order = np.lexsort((d, s))
+    e = np.empty(len(s), kamsta.WEDGE)
+    e["src"], e["dst"], e["w"] = s[order], d[order], ww[order]
+    return e, comps * size
+
+
+@pytest.mark.parametrize("algo", ["boruvka_plain", "boruvka_local", "filter_boruvka",
+                                  "filter_boruvka_t1"])
+@pytest.mark.parametrize("case", ["gnm_dense", "gnm_large", "cliques", "cliques_ties", "rhg",
+                                  "rmat"])
+def test_parallel_edge_heavy_graphs(kamsta, oracle, algo, case):
+    """Graphs whose contraction leaves many parallel edges between few
+    components (dense G(n,m), disjoint cliques with and without weight ties,
+    hubs) give the oracle's forest."""
+    fn, cfg = _configs(kamsta)[algo]
+    if case == "gnm_dense":
+        n = 1 << 14
+        e = oracle.gen_gnm(n, 1 << 21, 41)
+    elif case == "gnm_large":
+        n = 1 << 20
+        e = oracle.gen_gnm(n, 1 << 24, 42)
+    elif case == "cliques":
+        e, n = _disjoint_dense(kamsta, 2048, 48, 43, 254)
+    elif case == "cliques_ties":
+        e, n = _disjoint_dense(kamsta, 1024, 64, 44, 3)
+    elif case == "rhg":
+        n = 1 << 18
+        e = oracle.gen_rhg(n, 2.6, 32.0, 45)
+    else:
+        n = 1 << 18
+        e = oracle.gen_rmat(18, 1 << 23, 46)
+    _check(oracle, fn(e, cfg, n=n), e, n)
+
+
+def _clique_path(kamsta, k, size, links, seed):
+    """k cliques of `size` vertices (weight 5) on a path, neighbours joined
+    by `links` distinct random vertex pairs of weights U[6, 254].  The
+    cliques contract first; the heavier class then starts with k vertices
+    and about k * links parallel records, most of which die within two
+    rounds as the path contracts."""
+    rng = np.random.default_rng(seed)
+    iu, ju = np.triu_indices(size, 1)
+    base = (np.arange(k, dtype=np.int64) * size)[:, None]
+    u = [(base + iu[None, :]).ravel()]
+    v = [(base + ju[None, :]).ravel()]
+    w = [np.full(u[0].shape, 5)]
+    for c in range(k - 1):
+        pairs = rng.choice(size * size, links, replace=False)
+        u.append(c * size + pairs // size)
+        v.append((c + 1) * size + pairs % size)
+        w.append(rng.integers(6, 255, links))
+    u, v, w = np.concatenate(u), np.concatenate(v), np.concatenate(w)
+    s, d, ww = np.concatenate([u, v]), np.concatenate([v, u]), np.concatenate([w, w])
+    order = np.lexsort((d, s))
+    e = np.empty(len(s), kamsta.WEDGE)
+    e["src"], e["dst"], e["w"] = s[order], d[order], ww[order]
+    return e, k * size
+
+
+@pytest.mark.parametrize("algo", ["boruvka_plain", "boruvka_local", "filter_boruvka"])
+def test_clique_path(kamsta, oracle, algo):
+    """Tied clique weights, then a path of heavy multi-links: the forest
+    stays the oracle's (the (w, min, max) order decides the ties)."""
+    fn, cfg = _configs(kamsta)[algo]
+    e, n = _clique_path(kamsta, 1024, 32, 256, 47)
+    _check(oracle, fn(e, cfg, n=n), e, n)
