@@ -251,27 +251,37 @@ def run_geometric(args, K, ctx, sh, seed):
         torch.cuda.synchronize()
         gen_s = time.perf_counter() - t0
         out = torch.empty((n, 3), dtype=torch.int32, device="cuda")
-        cfg = K.AlgorithmConfig()
-        ctx.filter_boruvka_dev(d.data_ptr(), md, n, out.data_ptr(), cfg, stream=sh)
-        torch.cuda.synchronize()
-        ms, ws, ks = [], set(), set()
-        for _ in range(max(3, args.steps)):
-            st = {}
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(torch.cuda.current_stream())
-            k = ctx.filter_boruvka_dev(d.data_ptr(), md, n, out.data_ptr(), cfg, stream=sh,
-                                       stats=st)
-            e1.record(torch.cuda.current_stream())
+
+        def timed(cfg):
+            ctx.filter_boruvka_dev(d.data_ptr(), md, n, out.data_ptr(), cfg, stream=sh)
             torch.cuda.synchronize()
-            ms.append(e0.elapsed_time(e1))
-            ws.add(st["total_weight"])
-            ks.add(k)
-        med = statistics.median(ms)
+            ms, ws, ks = [], set(), set()
+            for _ in range(max(3, args.steps)):
+                st = {}
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(torch.cuda.current_stream())
+                k = ctx.filter_boruvka_dev(d.data_ptr(), md, n, out.data_ptr(), cfg, stream=sh,
+                                           stats=st)
+                e1.record(torch.cuda.current_stream())
+                torch.cuda.synchronize()
+                ms.append(e0.elapsed_time(e1))
+                ws.add(st["total_weight"])
+                ks.add(k)
+            return statistics.median(ms), ws, ks
+
+        # local preprocessing 1 is the reference benchmark's default
+        # (local_kernelization_level, benchmarks/mst_benchmarks.hpp:84); 0 runs
+        # the filter recursion itself
+        med, ws, ks = timed(K.AlgorithmConfig(local_preprocessing=1))
+        med0, ws0, ks0 = timed(K.AlgorithmConfig(local_preprocessing=0))
         res[fam] = {"workload": desc,
-                    "algorithm": "filter_boruvka (filter_hybridBoruvka), default config",
+                    "algorithm": "filter_boruvka (filter_hybridBoruvka), local_preprocessing=1",
                     "directed_entries": md, "value": md / (med / 1e3), "unit": UNIT,
-                    "ms_per_step": med, "forest_edges": ks.pop(), "forest_weight": ws.pop(),
-                    "deterministic": len(ws) == 0 and len(ks) == 0,
+                    "ms_per_step": med, "forest_edges": next(iter(ks)),
+                    "forest_weight": next(iter(ws)),
+                    "deterministic": len(ws) == 1 and len(ks) == 1 and ws == ws0 and ks == ks0,
+                    "no_preprocessing_ms": med0,
                     "generation_s": gen_s}
         del d, out
         torch.cuda.empty_cache()

@@ -1132,11 +1132,13 @@ __global__ void k_big_bitmap(uint32_t n, const uint32_t* __restrict__ D, uint32_
 // all but a few vertices, an edge of the directed input survives the
 // relabel pass (endpoint labels differ) only if one endpoint lies outside
 // that component.  Those edges are found by scanning the input rows of the
-// outside vertices -- the input is (src, dst)-sorted, so a row is two binary
-// searches away -- instead of streaming the whole input.  Each surviving
-// edge is reported with the position of its src<dst copy (oid), exactly the
-// record the streaming pass would have kept; sorting by oid restores the
-// streaming pass's order.
+// outside vertices -- the input is (src, dst)-sorted, so a row is one
+// search away -- instead of streaming the whole input.  A record carries
+// the position of either copy of its edge (the emit writes (min, max, w)
+// whichever it is) and a key (min id << b | max id); sorting by the key
+// restores the streaming pass's order, which is the order of the src < dst
+// copies.  With `canon` set (the batch's forest bitmap, which needs the
+// src < dst copy's position) the position of that copy is searched for.
 
 // Vertices outside the largest component (bit 0 in `big`), any order.
 __global__ void k_outside_big(uint32_t n, const uint32_t* __restrict__ big, uint32_t* __restrict__ out,
@@ -1159,7 +1161,8 @@ __global__ void k_outside_big(uint32_t n, const uint32_t* __restrict__ big, uint
   }
 }
 
-// first directed entry with src >= v (entries [0, md) sorted by src)
+// first directed entry with src >= v (entries [0, md) sorted by src); one
+// thread
 __device__ __forceinline__ uint64_t row_begin(const uint32_t* __restrict__ in, uint64_t md,
                                               uint32_t v) {
   uint64_t lo = 0, hi = md;
@@ -1170,27 +1173,62 @@ __device__ __forceinline__ uint64_t row_begin(const uint32_t* __restrict__ in, u
   return lo;
 }
 
+// The same with the whole warp: 32 probes per step shrink the range 33-fold,
+// so a row of 2^31 entries is found in 7 dependent steps instead of 31.
+// Called by all 32 lanes with the same v; every lane returns the answer.
+__device__ __forceinline__ uint64_t row_begin_warp(const uint32_t* __restrict__ in, uint64_t md,
+                                                   uint32_t v) {
+  const uint32_t lane = lane_id();
+  uint64_t lo = 0, hi = md;  // the answer lies in [lo, hi]
+  while (hi - lo > 32) {
+    const uint64_t span = hi - lo;
+    const uint64_t p = lo + span * (lane + 1) / 33;  // in [lo, hi), increasing in lane
+    const uint32_t c = __popc(__ballot_sync(kFull, in[3 * p] < v));  // a prefix of lanes
+    const uint64_t below = __shfl_sync(kFull, p, c == 0 ? 0 : c - 1);
+    const uint64_t above = __shfl_sync(kFull, p, c == 32 ? 31 : c);
+    if (c == 0) hi = above;
+    else if (c == 32) lo = below + 1;
+    else {
+      lo = below + 1;
+      hi = above;
+    }
+  }
+  const uint64_t q = lo + lane;
+  const bool less = q < hi && in[3 * q] < v;
+  return lo + __popc(__ballot_sync(kFull, less));
+}
+
 // One warp per outside vertex v: every entry (v, d, w) of its row with w in
 // [wmin, wmax] whose relabelled endpoints differ; d outside too and d < v:
-// reported from d's row; d inside and d < v: the oid is found in d's row.
-// WRITE = false counts, WRITE = true writes records at atomic slots.
+// reported from d's row.  WRITE = false counts and stores each row's start
+// in row_lo; WRITE = true writes records and keys at atomic slots.
 template <bool WRITE>
 __global__ void k_row_scan(const uint32_t* __restrict__ in, uint64_t md, uint32_t n,
-                           const uint32_t* __restrict__ S, uint32_t ns,
+                           const uint32_t* __restrict__ S, uint32_t ns, uint32_t* __restrict__ row_lo,
                            const uint32_t* __restrict__ D, const uint32_t* __restrict__ big,
-                           uint32_t big_label, uint32_t wmin, uint32_t wmax, Rec* __restrict__ out,
+                           uint32_t big_label, uint32_t wmin, uint32_t wmax, uint32_t canon,
+                           uint32_t key_bits, Rec* __restrict__ out, uint64_t* __restrict__ keys,
                            uint64_t cap, unsigned long long* count, uint32_t* err) {
   const uint32_t lane = lane_id();
   const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
   for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < ns; k += warps) {
     const uint32_t v = S[k];
-    const uint64_t lo = row_begin(in, md, v), hi = row_begin(in, md, v + 1);
+    uint64_t lo;
+    if (WRITE) {
+      lo = row_lo[k];
+    } else {
+      lo = row_begin_warp(in, md, v);
+      if (lane == 0) row_lo[k] = static_cast<uint32_t>(lo);
+    }
     const uint32_t la = D[v];
-    for (uint64_t i0 = lo; i0 < hi; i0 += 32) {
+    for (uint64_t i0 = lo;; i0 += 32) {
       const uint64_t i = i0 + lane;
+      const bool in_row = i < md && in[3 * i] == v;  // a prefix of lanes
+      if (!__any_sync(kFull, in_row)) break;
       bool keep = false;
       Rec r;
-      if (i < hi) {
+      uint64_t key = 0;
+      if (in_row) {
         const uint32_t d = in[3 * i + 1], w = in[3 * i + 2];
         if (d < n && d != v && w >= wmin && w <= wmax) {
           const bool d_big = (__ldg(big + (d >> 5)) >> (d & 31)) & 1u;
@@ -1199,16 +1237,20 @@ __global__ void k_row_scan(const uint32_t* __restrict__ in, uint64_t md, uint32_
             if (v < d) {
               keep = true;
               r = Rec{la, lb, w, static_cast<uint32_t>(i)};
+              key = (static_cast<uint64_t>(v) << key_bits) | d;
             } else if (d_big) {
-              // the src<dst copy (d, v) sits in d's row, sorted by dst
-              uint64_t a = row_begin(in, md, d), b = row_begin(in, md, d + 1);
-              while (a < b) {
-                const uint64_t mid = (a + b) >> 1;
-                if (in[3 * mid + 1] < v) a = mid + 1; else b = mid;
-              }
-              if (a < md && in[3 * a] == d && in[3 * a + 1] == v) {
-                keep = true;
-                r = Rec{lb, la, w, static_cast<uint32_t>(a)};
+              keep = true;
+              r = Rec{lb, la, w, static_cast<uint32_t>(i)};
+              key = (static_cast<uint64_t>(d) << key_bits) | v;
+              if (WRITE && canon) {
+                // the src<dst copy (d, v) sits in d's row, sorted by dst
+                uint64_t a = row_begin(in, md, d), b = row_begin(in, md, d + 1);
+                while (a < b) {
+                  const uint64_t mid = (a + b) >> 1;
+                  if (in[3 * mid + 1] < v) a = mid + 1; else b = mid;
+                }
+                if (a < md && in[3 * a] == d && in[3 * a + 1] == v) r.oid = static_cast<uint32_t>(a);
+                else atomicOr(err, kErrRange);  // the input lacks (d, v)
               }
             }
           }
@@ -1221,8 +1263,12 @@ __global__ void k_row_scan(const uint32_t* __restrict__ in, uint64_t md, uint32_
       base = __shfl_sync(kFull, base, 0);
       if (WRITE && keep) {
         const uint64_t slot = base + __popc(bal & lanemask_lt());
-        if (slot < cap) out[slot] = r;
-        else atomicOr(err, kErrOverflow);
+        if (slot < cap) {
+          out[slot] = r;
+          keys[slot] = key;
+        } else {
+          atomicOr(err, kErrOverflow);
+        }
       }
     }
   }
@@ -1230,27 +1276,36 @@ __global__ void k_row_scan(const uint32_t* __restrict__ in, uint64_t md, uint32_
 
 __global__ void k_set_u32(uint32_t* p, uint32_t v) { *p = v; }
 
-// oid keys of the collected records (for the sort back into input order)
-__global__ void k_rec_oid_keys(const Rec* __restrict__ r, uint64_t k, uint64_t* __restrict__ keys,
-                               uint32_t* __restrict__ idx) {
+__global__ void k_iota_u32(uint64_t k, uint32_t* __restrict__ idx) {
   for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < k;
-       i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
-    keys[i] = r[i].oid;
+       i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
     idx[i] = static_cast<uint32_t>(i);
-  }
 }
 
-// out[p] = in[idx[p]] and the round-0 minimum with position p
+// out[p] = in[idx[p]] and the round-0 minimum with position p.  Nearly every
+// record has the largest component (`hub`) as one endpoint: its minimum is
+// reduced in registers and per warp, one atomic per warp; the other
+// endpoints' updates are filtered by a read.
 __global__ void k_rec_place_min(const Rec* __restrict__ in, const uint32_t* __restrict__ idx,
-                                uint64_t k, Rec* __restrict__ out, uint64_t* minval) {
+                                uint64_t k, Rec* __restrict__ out, uint64_t* minval,
+                                uint32_t hub) {
+  uint64_t hub_min = kInf64;
   for (uint64_t p = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; p < k;
        p += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
     const Rec r = in[idx[p]];
     out[p] = r;
     const uint64_t v = (static_cast<uint64_t>(r.w) << 32) | p;
-    red_min(&minval[r.a], v);
-    red_min(&minval[r.b], v);
+    if (r.a == hub) hub_min = v < hub_min ? v : hub_min;
+    else if (v < ld_weak(&minval[r.a])) red_min(&minval[r.a], v);
+    if (r.b == hub) hub_min = v < hub_min ? v : hub_min;
+    else if (v < ld_weak(&minval[r.b])) red_min(&minval[r.b], v);
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const uint64_t y = __shfl_xor_sync(kFull, hub_min, o);
+    hub_min = y < hub_min ? y : hub_min;
+  }
+  if (lane_id() == 0 && hub_min != kInf64) red_min(&minval[hub], hub_min);
 }
 
 // D at `count` pseudo-random vertices (for picking the largest component).
@@ -1296,8 +1351,9 @@ __global__ void k_fill64(uint64_t n, uint64_t* __restrict__ a, uint64_t v) {
     a[x] = v;
 }
 
-// Forest output: gather the src<dst input copy of every forest edge and sum
-// the weights.
+// Forest output: gather the input copy of every forest edge (the src<dst
+// copy, or for row-scan records possibly the other one), write it as
+// (min, max, w) and sum the weights.
 __global__ void k_emit(uint64_t k, const uint32_t* __restrict__ msf,
                        const uint32_t* __restrict__ in_words,
                        uint32_t* __restrict__ out_words,
@@ -1326,8 +1382,8 @@ __global__ void k_emit(uint64_t k, const uint32_t* __restrict__ msf,
     for (int j = 0; j < kIlp; ++j) {
       if (o[j] == ~0ull) continue;
       const uint64_t i = base + j * stride;
-      out_words[3 * i] = s[j];
-      out_words[3 * i + 1] = d[j];
+      out_words[3 * i] = s[j] < d[j] ? s[j] : d[j];  // either copy of the edge
+      out_words[3 * i + 1] = s[j] < d[j] ? d[j] : s[j];
       out_words[3 * i + 2] = w[j];
       local += w[j];
     }

@@ -838,8 +838,8 @@ kamsta_status Solve::contract_rows(uint32_t wmin, uint32_t wmax, SegList* E, boo
   *done = false;
   // the vertices outside the largest component
   const uint32_t cap_s = std::max<uint32_t>(1u << 16, n_ / 32);
-  void* smem = nullptr;
-  CU_TRY(cudaMallocFromPoolAsync(&smem, sizeof(uint32_t) * cap_s, ctx_->pool, st_));
+  void* smem = nullptr;  // outside vertices, then their row starts
+  CU_TRY(cudaMallocFromPoolAsync(&smem, sizeof(uint32_t) * 2 * uint64_t(cap_s), ctx_->pool, st_));
   struct Free {
     void* p;
     cudaStream_t s;
@@ -848,6 +848,7 @@ kamsta_status Solve::contract_rows(uint32_t wmin, uint32_t wmax, SegList* E, boo
     }
   } fs{smem, st_};
   uint32_t* S = static_cast<uint32_t*>(smem);
+  uint32_t* row_lo = S + cap_s;
   const int t0 = tick();
   CU_TRY(cudaMemsetAsync(ctx_->d_counters + kCMisc, 0, sizeof(DevCounters), st_));
   unsigned long long* cnt = &ctx_->d_counters[kCMisc].cnt[0];
@@ -856,9 +857,15 @@ kamsta_status Solve::contract_rows(uint32_t wmin, uint32_t wmax, SegList* E, boo
   const uint64_t ns = ctx_->h_counters[kCMisc].cnt[0];
   if (ns > cap_s) return KAMSTA_OK;  // too many: stream the input instead
   const int grid = grid_for(std::max<uint64_t>(ns * 32, 1));
-  // count, then write the surviving edges
-  k_row_scan<false><<<grid, kBlock, 0, st_>>>(in_, md_, n_, S, static_cast<uint32_t>(ns), D_,
-                                              big_, big_label_, wmin, wmax, nullptr, 0,
+  // records are ordered by (min id << key_bits | max id); the batch's forest
+  // bitmap needs the src<dst copy's position in each record
+  uint32_t key_bits = 1;
+  while (key_bits < 32 && (1ull << key_bits) < n_) ++key_bits;
+  const uint32_t canon = forest_bits_ != nullptr ? 1u : 0u;
+  // count (and find the rows), then write the surviving edges
+  k_row_scan<false><<<grid, kBlock, 0, st_>>>(in_, md_, n_, S, static_cast<uint32_t>(ns), row_lo,
+                                              D_, big_, big_label_, wmin, wmax, canon, key_bits,
+                                              nullptr, nullptr, 0,
                                               &ctx_->d_counters[kCMisc].cnt[1], ctx_->d_err);
   KS_TRY(fetch_counters());
   const uint64_t k = ctx_->h_counters[kCMisc].cnt[1];
@@ -879,19 +886,19 @@ kamsta_status Solve::contract_rows(uint32_t wmin, uint32_t wmax, SegList* E, boo
     uint32_t* idx2 = reinterpret_cast<uint32_t*>(m + rb + 2 * kb + ib);
     uint32_t* counts = reinterpret_cast<uint32_t*>(m + rb + 2 * kb + 2 * ib);
     uint64_t* status = reinterpret_cast<uint64_t*>(m + rb + 2 * kb + 2 * ib + cb);
-    k_row_scan<true><<<grid, kBlock, 0, st_>>>(in_, md_, n_, S, static_cast<uint32_t>(ns), D_,
-                                               big_, big_label_, wmin, wmax, tmp, k,
-                                               &ctx_->d_counters[kCMisc].cnt[2], ctx_->d_err);
-    k_rec_oid_keys<<<grid_for(k), kBlock, 0, st_>>>(tmp, k, keys, idx);
+    k_row_scan<true><<<grid, kBlock, 0, st_>>>(in_, md_, n_, S, static_cast<uint32_t>(ns), row_lo,
+                                               D_, big_, big_label_, wmin, wmax, canon, key_bits,
+                                               tmp, keys, k, &ctx_->d_counters[kCMisc].cnt[2],
+                                               ctx_->d_err);
+    k_iota_u32<<<grid_for(k), kBlock, 0, st_>>>(k, idx);
     int alt = 0;
-    uint32_t bits = 1;
-    while (bits < 64 && (1ull << bits) < md_) ++bits;
-    cudaError_t e = radix_sort_pairs_u32(st_, keys, keys2, idx, idx2, k, static_cast<int>(bits),
-                                         counts, status, &ctx_->d_counters[kCMisc].ticket,
-                                         ctx_->d_err, &alt, sms_);
+    cudaError_t e = radix_sort_pairs_u32(st_, keys, keys2, idx, idx2, k,
+                                         static_cast<int>(2 * key_bits), counts, status,
+                                         &ctx_->d_counters[kCMisc].ticket, ctx_->d_err, &alt,
+                                         sms_);
     if (e != cudaSuccess) return cuda_status(e, "radix sort (row scan)");
     if (alt) std::swap(idx, idx2);
-    k_rec_place_min<<<grid_for(k), kBlock, 0, st_>>>(tmp, idx, k, E->base, minA_);
+    k_rec_place_min<<<grid_for(k), kBlock, 0, st_>>>(tmp, idx, k, E->base, minA_, big_label_);
     k_set_u32<<<1, 1, 0, st_>>>(E->d_count, static_cast<uint32_t>(k));
     KS_TRY(fetch_counters());  // also: the scratch above is released after use
   }
