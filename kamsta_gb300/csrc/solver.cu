@@ -75,6 +75,11 @@ void Arena::release() {
   } while (0)
 
 static inline size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+// Entries per thread of the mapped (relabelling) passes over the directed
+// input when the first pass uses 8: the mapped 8-entry kernel spills (its
+// label gathers need registers); 6 entries do not (R-MAT 2^24 class pass
+// 1.98 -> 1.36 ms, RHG 1.55 -> 1.35 ms).
+constexpr int kMappedDirItems = 6;
 static inline uint32_t ceil_div(uint64_t a, uint64_t b) {
   return static_cast<uint32_t>((a + b - 1) / b);
 }
@@ -415,7 +420,7 @@ kamsta_status Solve::pass(int phase, const SegList* src, const uint32_t* map, ui
                           bool validate) {
   const bool dir = src == nullptr;
   const uint64_t total = dir ? md_ : src->total;
-  const int items = dir_items_;
+  const int items = (map != nullptr && dir_items_ == 8) ? kMappedDirItems : dir_items_;
   const int sitems = seg_items_;
   const uint32_t tile = dir ? dir_tile(items) : rec_tile(sitems);
   const size_t dyn = dir ? dir_dyn_smem(items) : rec_dyn_smem(sitems);
