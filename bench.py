@@ -646,15 +646,18 @@ def main():
             link.append(link_rows * 12 / (c0.elapsed_time(c1) * 1e6))
         rep.barrier()
         t0 = time.perf_counter()
+        step_ms = []
         for _ in range(args.steps):
+            ts = time.perf_counter()
             ke = e2e_step()
+            step_ms.append(round((time.perf_counter() - ts) * 1e3, 2))
         dt = time.perf_counter() - t0
         dt = rep.max(dt)
         assert ke == forest and stc.total_weight == per_step[-1]["total_weight"]
         line["e2e"] = {"value": args.gpus * md * args.steps / dt, "unit": UNIT,
                        "h2d_bytes_per_step": md * 12, "d2h_bytes_per_step": ke * 12,
                        "ms_per_step": dt / args.steps * 1e3,
-                       "h2d_link_gbs": max(link),
+                       "h2d_link_gbs": max(link), "step_ms": step_ms,
                        "api": "kamsta_mst_boruvka (host buffers, pinned input and output)"}
         del h_edges, h_out
 

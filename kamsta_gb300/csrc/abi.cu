@@ -77,22 +77,6 @@ thread_local DefaultCtx g_default;
 // Host-to-device copy of a large input as pieces alternating between the
 // context's two streams (two copy engines in flight); the main stream waits
 // for both before the solve.
-cudaError_t copy_in(kamsta_ctx* ctx, void* dst, const void* src, size_t bytes) {
-  constexpr size_t kPiece = 256ull << 20;
-  if (bytes <= 2 * kPiece)
-    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
-  cudaError_t e = cudaEventRecord(ctx->ev_fork, ctx->stream);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->aux, ctx->ev_fork, 0);
-  for (size_t off = 0, k = 0; e == cudaSuccess && off < bytes; off += kPiece, ++k) {
-    const size_t len = std::min(kPiece, bytes - off);
-    e = cudaMemcpyAsync(static_cast<char*>(dst) + off, static_cast<const char*>(src) + off, len,
-                        cudaMemcpyHostToDevice, (k & 1) ? ctx->aux : ctx->stream);
-  }
-  if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_join, ctx->aux);
-  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0);
-  return e;
-}
-
 kamsta_status solve_host(Algo algo, const kamsta_wedge* edges, uint64_t m, uint32_t n,
                          const kamsta_cfg* cfg, kamsta_wedge* out, uint64_t* out_count,
                          kamsta_stats* stats) {
@@ -117,17 +101,41 @@ kamsta_status solve_host(Algo algo, const kamsta_wedge* edges, uint64_t m, uint3
   if (e != cudaSuccess) return cuda_status(e, "device buffers for host input");
   kamsta_wedge* din = ctx->io.take<kamsta_wedge>(m);
   kamsta_wedge* dout = ctx->io.take<kamsta_wedge>(std::max<uint64_t>(n, 1));
-  e = copy_in(ctx, din, edges, m * sizeof(kamsta_wedge));
-  if (e != cudaSuccess) return cuda_status(e, "cudaMemcpyAsync(H2D)");
+  // the input in pieces on the aux stream, so the solve can start on the
+  // first ones (the solve's stream waits for each piece's event)
+  HostIo io;
+  io.pieces = kInputPieces;
+  io.piece_ev = ctx->piece_ev;
+  io.copy_stream = ctx->aux;
+  io.host_out = out;
+  io.ev_early = ctx->ev_early;
+  const uint64_t per = (m + kInputPieces - 1) / kInputPieces;
+  for (int k = 0; k < kInputPieces; ++k) {
+    const uint64_t b = std::min<uint64_t>(m, k * per), en = std::min<uint64_t>(m, b + per);
+    io.piece_end[k] = en;
+    if (en > b) {
+      e = cudaMemcpyAsync(din + b, edges + b, (en - b) * sizeof(kamsta_wedge),
+                          cudaMemcpyHostToDevice, ctx->aux);
+      if (e != cudaSuccess) return cuda_status(e, "cudaMemcpyAsync(H2D)");
+    }
+    e = cudaEventRecord(ctx->piece_ev[k], ctx->aux);
+    if (e != cudaSuccess) return cuda_status(e, "cudaEventRecord");
+  }
   SolveOut so;
-  s = solve_device(ctx, algo, din, m, n, c, dout, &so, stats, ctx->stream);
-  if (s != KAMSTA_OK) return s;
-  if (so.count) {
-    e = cudaMemcpyAsync(out, dout, so.count * sizeof(kamsta_wedge), cudaMemcpyDeviceToHost,
+  s = solve_device(ctx, algo, din, m, n, c, dout, &so, stats, ctx->stream, nullptr, &io);
+  if (s != KAMSTA_OK) {
+    cudaStreamSynchronize(ctx->aux);  // no copy may outlive the call
+    return s;
+  }
+  // the edges not sent early (the first round's went out during the solve)
+  if (so.count > io.early) {
+    e = cudaMemcpyAsync(out + io.early, dout + io.early,
+                        (so.count - io.early) * sizeof(kamsta_wedge), cudaMemcpyDeviceToHost,
                         ctx->stream);
     if (e != cudaSuccess) return cuda_status(e, "cudaMemcpyAsync(D2H)");
   }
   e = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->aux);
   if (e != cudaSuccess) return cuda_status(e, "cudaStreamSynchronize");
   if (c.flags & KAMSTA_FLAG_SORT_OUTPUT)
     std::sort(out, out + so.count, [](const kamsta_wedge& a, const kamsta_wedge& b) {
@@ -269,6 +277,7 @@ kamsta_status kamsta_ctx_create(int device, kamsta_ctx** out) {
       (e = cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming)) != cudaSuccess ||
       (e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&c->ev_early, cudaEventDisableTiming)) != cudaSuccess ||
       (e = cudaMalloc(&c->d_counters, sizeof(DevCounters) * kCSlots)) != cudaSuccess ||
       (e = cudaMalloc(&c->d_err, sizeof(uint32_t))) != cudaSuccess ||
       (e = cudaMalloc(&c->d_samples, sizeof(uint32_t) * kSampleCap)) != cudaSuccess ||
@@ -280,6 +289,9 @@ kamsta_status kamsta_ctx_create(int device, kamsta_ctx** out) {
   }
   for (int i = 0; s == KAMSTA_OK && i < kTimerEvents; ++i)
     if ((e = cudaEventCreate(&c->tev[i])) != cudaSuccess) s = cuda_status(e, "cudaEventCreate");
+  for (int i = 0; s == KAMSTA_OK && i < kInputPieces; ++i)
+    if ((e = cudaEventCreateWithFlags(&c->piece_ev[i], cudaEventDisableTiming)) != cudaSuccess)
+      s = cuda_status(e, "cudaEventCreate");
   if (s == KAMSTA_OK) {
     // a private stream-ordered pool for edge lists; it keeps its memory
     // between calls (release threshold = unlimited) until kamsta_ctx_trim
@@ -323,6 +335,9 @@ kamsta_status kamsta_ctx_destroy(kamsta_ctx* ctx) {
     if (ctx->tev[i]) cudaEventDestroy(ctx->tev[i]);
   ctx->io.release();
   if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_early) cudaEventDestroy(ctx->ev_early);
+  for (int i = 0; i < kInputPieces; ++i)
+    if (ctx->piece_ev[i]) cudaEventDestroy(ctx->piece_ev[i]);
   if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
   if (ctx->aux) cudaStreamDestroy(ctx->aux);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);

@@ -77,7 +77,11 @@ struct PassArgs {
   uint32_t n;         // ids must be < n (directed source)
   uint32_t validate;  // check id range and (src,dst) order (directed source)
   uint32_t aligned16; // directed source base is 16-byte aligned
+  uint32_t cta_base;  // segment / chunk index of block 0 (a pass launched in groups)
 };
+
+// The segment (and input chunk) this CTA owns.
+__device__ __forceinline__ uint32_t seg_id(const PassArgs& p) { return blockIdx.x + p.cta_base; }
 
 // Relabel a thread's ITEMS items with all label reads in flight together:
 // membership bits first (one load per endpoint), then the map for the
@@ -154,7 +158,7 @@ __device__ __forceinline__ void seg_tile_finish(const uint8_t (&cls)[ITEMS], uin
 #pragma unroll
   for (int c = 0; c < NOUT; ++c) {
     capc[c] = static_cast<uint32_t>(p.out[c].cap);
-    segc[c] = p.out[c].base + static_cast<uint64_t>(blockIdx.x) * p.out[c].cap;
+    segc[c] = p.out[c].base + static_cast<uint64_t>(seg_id(p)) * p.out[c].cap;
     runc[c] = static_cast<uint32_t>(run[c]);
   }
 #pragma unroll
@@ -179,7 +183,7 @@ __device__ __forceinline__ void seg_tile_finish(const uint8_t (&cls)[ITEMS], uin
     if (c == 0) min_mask |= 1u << j;
   }
   if (p.minval != nullptr && min_mask) {
-    const uint64_t seg0 = static_cast<uint64_t>(blockIdx.x) * p.out[0].cap + run[0];
+    const uint64_t seg0 = static_cast<uint64_t>(seg_id(p)) * p.out[0].cap + run[0];
     if (!p.min_checked) {
 #pragma unroll
       for (int j = 0; j < ITEMS; ++j) {
@@ -240,7 +244,7 @@ __device__ __forceinline__ void seg_pass_end(const uint64_t (&run)[NOUT], uint32
     if (s_red[1]) atomicAdd(&p.counts[1], static_cast<unsigned long long>(s_red[1]));
   }
   // unclamped: a count above cap tells the host the exact size to retry with
-  if (threadIdx.x < NOUT) p.out[threadIdx.x].count[blockIdx.x] = static_cast<uint32_t>(run[threadIdx.x]);
+  if (threadIdx.x < NOUT) p.out[threadIdx.x].count[seg_id(p)] = static_cast<uint32_t>(run[threadIdx.x]);
 }
 
 // Edge pass over the caller's directed input (12-byte records, (src,dst)
@@ -266,7 +270,7 @@ __global__ void __launch_bounds__(kBlock, ITEMS <= 8 ? 4 : 3)
   extern __shared__ __align__(128) uint32_t s_words[];  // two stages
   __shared__ __align__(8) uint64_t s_bar[2];
   __shared__ uint32_t s_ok;
-  const uint64_t lo = static_cast<uint64_t>(blockIdx.x) * p.chunk;
+  const uint64_t lo = static_cast<uint64_t>(seg_id(p)) * p.chunk;
   const uint64_t hi = lo + p.chunk < p.total ? lo + p.chunk : p.total;
   const uint32_t ntile = lo < hi ? static_cast<uint32_t>((hi - lo + kDirTile - 1) / kDirTile) : 0u;
   const bool tma = p.aligned16 != 0;
@@ -454,7 +458,7 @@ __global__ void __launch_bounds__(kBlock, ITEMS <= 2 ? 5 : ITEMS <= 4 ? 4 : 3)
   __shared__ __align__(8) uint64_t s_bar[2];
   __shared__ uint32_t s_ok, s_plain[2];
   seg_prefix(in, s_prefix);
-  const uint64_t lo = static_cast<uint64_t>(blockIdx.x) * p.chunk;
+  const uint64_t lo = static_cast<uint64_t>(seg_id(p)) * p.chunk;
   const uint64_t hi = lo + p.chunk < p.total ? lo + p.chunk : p.total;
   const uint32_t ntile = lo < hi ? static_cast<uint32_t>((hi - lo + kRecTile - 1) / kRecTile) : 0u;
   auto tile_items = [&](uint32_t k) -> uint32_t {

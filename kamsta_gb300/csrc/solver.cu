@@ -121,6 +121,8 @@ class Solve {
   kamsta_status run(Algo algo, kamsta_wedge* d_out, SolveOut* out);
   // forest as a bitmap over input positions instead of edges (batch split)
   uint32_t* forest_bits_ = nullptr;
+  // host input arriving in pieces / early forest copy (host entry point)
+  HostIo* io_ = nullptr;
 
  private:
   // ---- memory
@@ -241,6 +243,12 @@ class Solve {
   uint32_t* big_ = nullptr;         // membership bitmap of the largest component
   uint32_t nreps_ = 0;
   uint64_t msf_count_ = 0;
+  bool input_complete_ = true;  // every later input reader is ordered after the last piece
+  kamsta_status wait_input(int piece) {
+    if (io_ && io_->pieces > 0)
+      CU_TRY(cudaStreamWaitEvent(st_, io_->piece_ev[piece < io_->pieces ? piece : io_->pieces - 1], 0));
+    return KAMSTA_OK;
+  }
   // Direct emission: the first round over original ids (the first pass's
   // lightest class) writes its forest edges to the output itself, so the
   // final emit gathers only the later rounds' edges from the input.
@@ -476,7 +484,32 @@ kamsta_status Solve::pass(int phase, const SegList* src, const uint32_t* map, ui
     a.validate = validate ? 1 : 0;
     a.aligned16 = aligned16_ ? 1 : 0;
     const int t0 = tick();
-    if (dir && mapped && items == 8)
+    bool launched = false;
+    if (dir && !mapped && !input_complete_ && items == 8 && attempt == 0) {
+      // the input is still arriving: launch the CTAs whose chunks have landed
+      uint32_t b0 = 0;
+      for (int k = 0; k < io_->pieces && b0 < G; ++k) {
+        const uint32_t b1 =
+            k + 1 == io_->pieces
+                ? G
+                : static_cast<uint32_t>(std::min<uint64_t>(G, io_->piece_end[k] / chunk));
+        if (b1 <= b0) continue;
+        KS_TRY(wait_input(k));
+        a.cta_base = b0;
+        k_pass_dir<NOUT, 8, false><<<b1 - b0, kBlock, dyn, st_>>>(in_, a);
+        b0 = b1;
+      }
+      a.cta_base = 0;
+      KS_TRY(wait_input(io_->pieces - 1));
+      input_complete_ = true;
+      launched = true;
+    } else if (!input_complete_) {
+      KS_TRY(wait_input(io_->pieces - 1));
+      input_complete_ = true;
+    }
+    if (launched) {
+      // the first pass ran in groups above
+    } else if (dir && mapped && items == 8)
       k_pass_dir<NOUT, 8, true><<<G, kBlock, dyn, st_>>>(in_, a);
     else if (dir && mapped && items == 6)
       k_pass_dir<NOUT, 6, true><<<G, kBlock, dyn, st_>>>(in_, a);
@@ -675,7 +708,17 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
             uint64_t(nr) * ((8 + 16 + 8 + 8) + 16 + (4 + 8 + 4) + (8 + 4 + 4)) + n_next * 16 +
                 added * (direct ? 8 + 12 : 8) - (direct ? uint64_t(nr) * 20 : 0),
             6);
-    if (direct) direct_count_ = added;
+    if (direct) {
+      direct_count_ = added;
+      if (io_ && io_->host_out && added > 0) {
+        // final already: send them to the host while the solve goes on
+        CU_TRY(cudaEventRecord(io_->ev_early, st_));
+        CU_TRY(cudaStreamWaitEvent(io_->copy_stream, io_->ev_early, 0));
+        CU_TRY(cudaMemcpyAsync(io_->host_out, d_out_, added * sizeof(kamsta_wedge),
+                               cudaMemcpyDeviceToHost, io_->copy_stream));
+        io_->early = added;
+      }
+    }
     if (debug_) {
       fprintf(stderr, "[kamsta debug] round %u: m=%llu n=%u -> m'=%llu n'=%llu forest+=%llu\n", r,
               (unsigned long long)m, nr, (unsigned long long)nxt->total,
@@ -749,7 +792,11 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
 
 kamsta_status Solve::sample_weights(const SegList* L, uint32_t count, std::vector<uint32_t>* out) {
   out->clear();
-  const uint64_t m = L ? L->total : md_;
+  uint64_t m = L ? L->total : md_;
+  if (!L && !input_complete_) {  // only the first piece of the input is there yet
+    KS_TRY(wait_input(0));
+    m = io_->piece_end[0];
+  }
   if (m == 0) return KAMSTA_OK;
   count = std::min<uint32_t>(count, kSamples);
   const int g = grid_for(count);
@@ -1114,6 +1161,13 @@ kamsta_status Solve::run(Algo algo, kamsta_wedge* d_out, SolveOut* out) {
   // covers every edge, so the distributed recursion has nothing left.
   if (algo == Algo::kFilterBoruvka && cfg_.local_preprocessing != KAMSTA_NO_PREPROCESSING)
     algo = Algo::kBoruvka;
+  // host input still arriving: the boruvka plan samples the first piece and
+  // its first pass follows the pieces; everything else waits for all of it
+  input_complete_ = !(io_ && io_->pieces > 0);
+  if (!input_complete_ && algo != Algo::kBoruvka) {
+    KS_TRY(wait_input(io_->pieces - 1));
+    input_complete_ = true;
+  }
   if (algo == Algo::kBoruvka) {
     std::vector<uint32_t> thr_desc = plan_classes();
     bounds_.assign(thr_desc.rbegin(), thr_desc.rend());
@@ -1175,10 +1229,11 @@ kamsta_status Solve::run(Algo algo, kamsta_wedge* d_out, SolveOut* out) {
 kamsta_status solve_device(kamsta_ctx* ctx, Algo algo, const kamsta_wedge* d_in,
                            uint64_t m_directed, uint32_t n, const kamsta_cfg& cfg,
                            kamsta_wedge* d_out, SolveOut* out, kamsta_stats* st,
-                           cudaStream_t stream, uint32_t* d_forest_bits) {
+                           cudaStream_t stream, uint32_t* d_forest_bits, HostIo* io) {
   if (st) std::memset(st, 0, sizeof(*st));
   Solve s(ctx, stream ? stream : ctx->stream, d_in, m_directed, n, cfg, st);
   s.forest_bits_ = d_forest_bits;
+  s.io_ = io;
   return s.run(algo, d_out, out);
 }
 

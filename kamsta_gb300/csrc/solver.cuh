@@ -45,6 +45,7 @@ static_assert(sizeof(DevCounters) == 128, "counter block size");
 enum CounterSlot : int { kCVertex = 0, kCEdge = 1, kCRep = 2, kCMisc = 3, kCSlots = 4 };
 constexpr uint32_t kSampleCap = 4096;
 constexpr int kTimerEvents = 64;
+constexpr int kInputPieces = 16;  // host input copied in this many pieces
 
 }  // namespace kamsta
 
@@ -66,6 +67,8 @@ struct kamsta_ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t tev[kamsta::kTimerEvents] = {};  // per-phase timing events
   kamsta::Arena io;      // host-buffer entry points: device copies of in/out
+  cudaEvent_t piece_ev[kamsta::kInputPieces] = {};  // host input piece k is on the device
+  cudaEvent_t ev_early = nullptr;  // the first round's forest edges are written
   std::mutex mu;
 };
 
@@ -79,6 +82,24 @@ struct SolveOut {
 // Which reference entry point a call mirrors.
 enum class Algo { kBoruvka, kFilterBoruvka };
 
+// The host-buffer entry point overlaps its copies with the solve.  The input
+// arrives in pieces on copy_stream: entries [0, piece_end[k]) are on the
+// device once piece_ev[k] has completed (the events are recorded in order).
+// The first pass starts on each chunk as soon as it has landed, and the
+// weight sample of the class plan is drawn from the first piece.  When
+// host_out is set, the forest edges that the first round writes directly
+// are copied back to host_out[0, early) on copy_stream while the rest of the
+// solve runs.
+struct HostIo {
+  int pieces = 0;
+  uint64_t piece_end[kInputPieces] = {};
+  const cudaEvent_t* piece_ev = nullptr;
+  cudaStream_t copy_stream = nullptr;
+  kamsta_wedge* host_out = nullptr;
+  cudaEvent_t ev_early = nullptr;
+  uint64_t early = 0;  // out
+};
+
 // Solves one graph whose directed, (src,dst)-sorted input lies in device
 // memory.  Writes the forest to d_out (device, capacity >= n-1), or, when
 // d_forest_bits is given (zeroed, one bit per input entry), sets the bit of
@@ -86,7 +107,8 @@ enum class Algo { kBoruvka, kFilterBoruvka };
 kamsta_status solve_device(kamsta_ctx* ctx, Algo algo, const kamsta_wedge* d_in,
                            uint64_t m_directed, uint32_t n, const kamsta_cfg& cfg,
                            kamsta_wedge* d_out, SolveOut* out, kamsta_stats* st,
-                           cudaStream_t stream, uint32_t* d_forest_bits = nullptr);
+                           cudaStream_t stream, uint32_t* d_forest_bits = nullptr,
+                           HostIo* io = nullptr);
 
 void set_error(const std::string& msg);
 kamsta_status cuda_status(cudaError_t e, const char* what);
