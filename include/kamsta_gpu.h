@@ -384,6 +384,23 @@ kamsta_status kamsta_load_wedge9_dev(kamsta_ctx* ctx, const char* const* paths,
                                      uint64_t* m_directed_out, uint32_t* n_out,
                                      kamsta_stream stream);
 
+/* MatrixMarket coordinate files (the reference's INFILE_UNWEIGHTED input,
+ * read by graphs::read_unweighted_graph(file, GraphFormat::MatrixMarket) at
+ * benchmarks/mst_benchmarks.hpp:181-184): entry (i, j), 1-based, is the
+ * undirected edge {i-1, j-1}; values are ignored, self loops dropped,
+ * repeated pairs merged; n = max(rows, cols) (< 2^31).  Every edge gets the
+ * generators' weight in [1, max_weight] from `seed`.  The output is the
+ * solver's input (both directions, (src, dst)-sorted).  kamsta_mtx_header
+ * (host only) reads rows, cols and the stored entries; 2 * entries bounds
+ * the directed entries.  Counting / capacity convention as
+ * kamsta_gen_rgg2d_dev. */
+kamsta_status kamsta_mtx_header(const char* path, uint64_t* rows, uint64_t* cols,
+                                uint64_t* entries);
+kamsta_status kamsta_load_mtx_dev(kamsta_ctx* ctx, const char* path, uint64_t seed,
+                                  uint32_t max_weight, kamsta_wedge* d_out,
+                                  uint64_t capacity, uint64_t* m_directed_out,
+                                  uint32_t* n_out, kamsta_stream stream);
+
 /* ---- device graph generators (seeded; identical to the oracle's CPU
  * generators).  d_out must hold 2*m entries; *m_directed_out receives the
  * number written.  Stand-ins for KaGen's get_gnm / get_rgg2D / get_rhg

@@ -17,6 +17,7 @@ from __future__ import annotations
 
 import ctypes as C
 import enum
+import os
 from dataclasses import dataclass
 
 import numpy as np
@@ -157,6 +158,14 @@ def boruvka_wedge64(input_edges: np.ndarray, config: AlgorithmConfig | None = No
     if stats is not None:
         stats.update(st.as_dict())
     return out[: cnt.value].copy()
+
+
+def mtx_header(path) -> tuple[int, int, int]:
+    """(rows, cols, stored entries) of a MatrixMarket coordinate file (host
+    only, kamsta_mtx_header)."""
+    r, c, e = C.c_uint64(0), C.c_uint64(0), C.c_uint64(0)
+    check(lib().kamsta_mtx_header(os.fsencode(path), C.byref(r), C.byref(c), C.byref(e)))
+    return int(r.value), int(c.value), int(e.value)
 
 
 class Compressed:
@@ -425,6 +434,20 @@ class Context:
                                         C.c_void_p(d_out or 0), int(capacity), C.byref(cnt),
                                         C.c_void_p(stream or 0)))
         return int(cnt.value)
+
+    def load_mtx_dev(self, path, seed: int = 1, max_weight: int = 254, stream=0):
+        """A MatrixMarket coordinate file as solver input on the device (the
+        reference's unweighted input; hash weights in [1, max_weight]).
+        Returns (edges tensor (m, 3) int32 on cuda, m_directed, n)."""
+        import torch
+        _, _, entries = mtx_header(path)
+        cap = max(2 * entries, 1)
+        d = torch.empty((cap, 3), dtype=torch.int32, device="cuda")
+        m, n = C.c_uint64(0), C.c_uint32(0)
+        check(lib().kamsta_load_mtx_dev(self._h, os.fsencode(path), int(seed), int(max_weight),
+                                        C.c_void_p(d.data_ptr()), cap, C.byref(m), C.byref(n),
+                                        C.c_void_p(stream or 0)))
+        return d[: m.value], int(m.value), int(n.value)
 
     def load_wedge9_dev(self, paths, symmetrize: bool = True, stream=0):
         """Stream the reference's 9-byte binary edge files to the device.

@@ -155,6 +155,9 @@ SIGNATURES = {
     "kamsta_wedge9_capacity": (I32, [C.POINTER(C.c_char_p), U32, U32, C.POINTER(U64)]),
     "kamsta_load_wedge9_dev": (I32, [P, C.POINTER(C.c_char_p), U32, U32, P, U64,
                                      C.POINTER(U64), C.POINTER(U32), P]),
+    "kamsta_mtx_header": (I32, [C.c_char_p, C.POINTER(U64), C.POINTER(U64), C.POINTER(U64)]),
+    "kamsta_load_mtx_dev": (I32, [P, C.c_char_p, U64, U32, P, U64, C.POINTER(U64),
+                                  C.POINTER(U32), P]),
     "kamsta_gen_gnm_dev": (I32, [P, U32, U64, U64, U32, P, C.POINTER(U64), P]),
     "kamsta_gen_rgg2d_dev": (I32, [P, U32, C.c_double, U64, U32, P, U64, C.POINTER(U64), P]),
     "kamsta_gen_rhg_dev": (I32, [P, U32, C.c_double, C.c_double, U64, U32, P, U64,

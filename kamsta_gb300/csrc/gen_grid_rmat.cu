@@ -458,23 +458,39 @@ kamsta_status gen_rmat(kamsta_ctx* ctx, uint32_t log_n, uint64_t samples, double
   const uint64_t wseed = mix64(seed ^ kWeightSalt);
   const uint64_t K = samples;
   const uint32_t L = log_n;
+  GenBuf bk;
+  uint64_t* keys;
+  GEN_CHECK(bk.alloc(ctx, st, &keys, K));
+  k_rmat_keys<<<sm_count() * 8, 256, 0, st>>>(K, base, L, ta, tab, tabc, keys);
+  GEN_CHECK(cudaGetLastError());
+  return pairs_to_edges(ctx, st, bk, K, L, wseed, max_weight, "gen_rmat", d_out, capacity, m_out);
+}
+
+kamsta_status pairs_to_edges(kamsta_ctx* ctx, cudaStream_t st, GenBuf& bk, uint64_t K, uint32_t L,
+                             uint64_t wseed, uint32_t max_weight, const char* name,
+                             kamsta_wedge* d_out, uint64_t capacity, uint64_t* m_out) {
+  *m_out = 0;
+  if (K == 0) return KAMSTA_OK;
+  if (L == 0 || L > 31 || K >= (1ull << 32) - kRmatSortSlack) {
+    set_error(std::string(name) + ": needs 1 <= id bits <= 31 and fewer than 2^32 - 4096 pairs");
+    return KAMSTA_E_INPUT;
+  }
+  uint64_t* keys = static_cast<uint64_t*>(bk.p);
   const uint64_t invalid = (1ull << (2 * L)) - 1;
   const int sms = sm_count();
   const int grid = sms * 8;
-  GenBuf bk, bk2, bkeep, bpos, bcnt, bstat, bsmall;
-  uint64_t *keys, *keys2, *status;
+  GenBuf bk2, bkeep, bpos, bcnt, bstat, bsmall;
+  uint64_t *keys2, *status;
   uint32_t *keep, *pos, *counts;
   unsigned long long* small;
   GEN_CHECK(bsmall.alloc(ctx, st, &small, 4));
   uint32_t* ticket = reinterpret_cast<uint32_t*>(small + 2);
   uint32_t* err = reinterpret_cast<uint32_t*>(small + 3);
   GEN_CHECK(cudaMemsetAsync(small, 0, 4 * sizeof(unsigned long long), st));
-  GEN_CHECK(bk.alloc(ctx, st, &keys, K));
   GEN_CHECK(bk2.alloc(ctx, st, &keys2, K));
   const RadixScratch rs = radix_scratch_bytes(K);
   GEN_CHECK(bcnt.alloc(ctx, st, &counts, rs.counts));
   GEN_CHECK(bstat.alloc(ctx, st, &status, std::max<uint64_t>(rs.status, cdiv32(K, 2048) + 2)));
-  k_rmat_keys<<<grid, 256, 0, st>>>(K, base, L, ta, tab, tabc, keys);
   int alt = 0;
   GEN_CHECK(radix_sort_keys(st, keys, keys2, K, 2 * static_cast<int>(L), counts, status, ticket,
                             err, &alt, sms));
@@ -494,18 +510,18 @@ kamsta_status gen_rmat(kamsta_ctx* ctx, uint32_t log_n, uint64_t samples, double
   GEN_CHECK(cudaMemcpyAsync(&herr, err, sizeof(herr), cudaMemcpyDeviceToHost, st));
   GEN_CHECK(cudaStreamSynchronize(st));
   if (herr) {
-    set_error("gen_rmat: device scan wait cap reached");
+    set_error(std::string(name) + ": device scan wait cap reached");
     return KAMSTA_E_NOCONVERGE;
   }
   const uint64_t md = 2 * pairs;
   if (md >= (1ull << 32) - kRmatSortSlack) {
-    set_error("gen_rmat: more than 2^32 - 4096 directed entries");
+    set_error(std::string(name) + ": more than 2^32 - 4096 directed entries");
     return KAMSTA_E_INPUT;
   }
   *m_out = md;
   if (!d_out) return KAMSTA_OK;
   if (md > capacity) {
-    set_error("gen_rmat: output capacity too small (required count in m_directed_out)");
+    set_error(std::string(name) + ": output capacity too small (required count in m_directed_out)");
     return KAMSTA_E_INPUT;
   }
   GenBuf bd, bd2, bcnt2, bstat2;
@@ -526,7 +542,7 @@ kamsta_status gen_rmat(kamsta_ctx* ctx, uint32_t log_n, uint64_t samples, double
   GEN_CHECK(cudaStreamSynchronize(st));
   GEN_CHECK(cudaGetLastError());
   if (herr) {
-    set_error("gen_rmat: device scan wait cap reached");
+    set_error(std::string(name) + ": device scan wait cap reached");
     return KAMSTA_E_NOCONVERGE;
   }
   return KAMSTA_OK;

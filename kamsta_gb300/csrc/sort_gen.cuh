@@ -48,4 +48,15 @@ kamsta_status gen_rhg(kamsta_ctx* ctx, uint32_t n, double gamma, double avg_degr
                       uint32_t max_weight, kamsta_wedge* d_out, uint64_t capacity,
                       uint64_t* m_out, cudaStream_t st);
 
+struct GenBuf;
+// Distinct undirected pairs -> the solver's input: bk holds K keys (min id
+// << L | max id, or (1 << 2L) - 1 for "no pair") in device memory, in any
+// order.  Writes both directions of every distinct pair, (src, dst)-sorted,
+// with the generators' weight 1 + hi64(mix64(wseed ^ (min << 32 | max)) *
+// max_weight).  Counting / capacity convention of the generators; `name`
+// prefixes error messages.  bk may be swapped with scratch (it stays owned).
+kamsta_status pairs_to_edges(kamsta_ctx* ctx, cudaStream_t st, GenBuf& bk, uint64_t K, uint32_t L,
+                             uint64_t wseed, uint32_t max_weight, const char* name,
+                             kamsta_wedge* d_out, uint64_t capacity, uint64_t* m_out);
+
 }  // namespace kamsta
