@@ -500,7 +500,7 @@ def main():
     # autotune the first-pass tile (entries per thread) on this workload:
     # one untimed solve per candidate, the fastest is used for every step
     tiles = {}
-    cands = ((8, 4), (6, 4), (12, 4), (8, 2), (6, 2), (8, 8))
+    cands = ((8, 2), (6, 2), (12, 2), (8, 4), (12, 4), (6, 4))
     if args.tiles != "auto":
         cands = (tuple(int(x) for x in args.tiles.split("x")),)
     for items, seg in cands:

@@ -99,7 +99,7 @@ typedef struct kamsta_cfg {
   uint32_t seg_items_per_thread; /* list-pass tile: 2, 4 or 8 records per   */
                                /* thread (0 = 2)                             */
   uint32_t items_per_thread;   /* first-pass tile: 6, 8 or 12 directed       */
-                               /* entries per thread (0 = 8)                 */
+                               /* entries per thread (0 = 6)                 */
 } kamsta_cfg;
 
 #define KAMSTA_TRACE_MAX 128

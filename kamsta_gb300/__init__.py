@@ -57,7 +57,7 @@ class AlgorithmConfig:
     trace: bool = False
     seed: int | None = None
     filter: bool = False        # batch / serving: filter_boruvka instead of boruvka
-    items_per_thread: int = 0   # first-pass tile: 6, 8 or 12 entries per thread (0 = 8)
+    items_per_thread: int = 0   # first-pass tile: 6, 8 or 12 entries per thread (0 = 6)
     seg_items_per_thread: int = 0  # list-pass tile: 2, 4 or 8 records per thread (0 = 2)
 
     def to_c(self) -> _native.Cfg:

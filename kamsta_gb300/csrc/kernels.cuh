@@ -17,7 +17,7 @@
 namespace kamsta {
 
 constexpr int kBlock = 256;
-constexpr int kItemsDir = 8;    // directed 12-byte records per thread (default tile)
+constexpr int kItemsDir = 6;    // directed 12-byte records per thread (default tile)
 constexpr int kItemsRec = 2;    // 16-byte records per thread (default tile)
 constexpr int kMaxOut = 3;      // weight classes materialised by one pass
 
@@ -136,95 +136,73 @@ __device__ __forceinline__ uint32_t next_tile(uint32_t* ticket) {
 
 // Rank the tile's kept items (stable), append them to this CTA's output
 // segments and feed the fused minimum.  rec(t) returns tile item t from
-// shared memory.  run[] holds the CTA's running segment sizes (the same in
-// every thread).  Class loops are unrolled so no array is indexed at run
-// time.  Minimum updates of a checked pass first read all their current
-// values, then issue the reductions, so a thread waits for at most one
-// memory round trip per tile.
+// shared memory; run[] holds the CTA's running segment sizes (the same in
+// every thread).  Two steps: the ranks place every kept item's tile index in
+// a shared list (class by class, tile order), then the whole CTA writes the
+// records and feeds the minimum from that list -- one kept item per thread
+// and step instead of one predicated slot per item.  Few items of a pass
+// over the directed input are kept (an eighth in the GNM first pass), so
+// this halved its instructions per entry (first pass 8.15 -> 7.27 ms at
+// 2^26/2^30; the list passes gained 0.3 ms).  Minimum updates of a checked
+// pass read the current value first and reduce only when smaller.
 template <int NOUT, int ITEMS, typename RecAt>
-__device__ __forceinline__ void seg_tile_finish(const uint8_t (&cls)[ITEMS], uint64_t (&run)[NOUT],
-                                                const PassArgs& p, RecAt rec) {
+__device__ __forceinline__ void seg_tile_finish(const uint8_t (&cls)[ITEMS],
+                                                      uint64_t (&run)[NOUT], const PassArgs& p,
+                                                      RecAt rec) {
   __shared__ uint32_t s_rank[NOUT * ITEMS * (kBlock / 32)];
   __shared__ uint32_t s_tot[NOUT];
+  __shared__ uint16_t s_dense[ITEMS * kBlock];
   uint32_t offs[ITEMS];
 #pragma unroll
   for (int j = 0; j < ITEMS; ++j) offs[j] = 0;
   tile_rank<NOUT, ITEMS, kBlock>(cls, offs, s_rank, s_tot);
-  uint32_t min_mask = 0;  // class-0 items whose minimum must be fed
-  // one pass over the items; the class picks segment, size and capacity
-  // (all below 2^32: a segment holds at most one CTA's chunk)
-  Rec* segc[NOUT];
-  uint32_t runc[NOUT], capc[NOUT];
+  uint32_t cbase[NOUT], tot[NOUT];
 #pragma unroll
   for (int c = 0; c < NOUT; ++c) {
-    capc[c] = static_cast<uint32_t>(p.out[c].cap);
-    segc[c] = p.out[c].base + static_cast<uint64_t>(seg_id(p)) * p.out[c].cap;
-    runc[c] = static_cast<uint32_t>(run[c]);
+    tot[c] = s_tot[c];
+    cbase[c] = c == 0 ? 0u : cbase[c - 1] + tot[c - 1];
   }
 #pragma unroll
   for (int j = 0; j < ITEMS; ++j) {
     const uint8_t c = cls[j];
     if (c == 0xff) continue;
-    Rec* sg = segc[0];
-    uint32_t rb = runc[0], cp = capc[0];
+    uint32_t b = cbase[0];
 #pragma unroll
     for (int k = 1; k < NOUT; ++k)
-      if (c == k) {
-        sg = segc[k];
-        rb = runc[k];
-        cp = capc[k];
-      }
-    const uint32_t local = rb + offs[j];
-    if (local >= cp) {
-      atomicOr(p.err, kErrOverflow);
-      continue;
-    }
-    sg[local] = rec(j * kBlock + threadIdx.x);
-    if (c == 0) min_mask |= 1u << j;
+      if (c == k) b = cbase[k];
+    s_dense[b + offs[j]] = static_cast<uint16_t>(j * kBlock + threadIdx.x);
   }
-  if (p.minval != nullptr && min_mask) {
-    const uint64_t seg0 = static_cast<uint64_t>(seg_id(p)) * p.out[0].cap + run[0];
-    if (!p.min_checked) {
+  __syncthreads();
 #pragma unroll
-      for (int j = 0; j < ITEMS; ++j) {
-        if (!((min_mask >> j) & 1u)) continue;
-        const Rec r = rec(j * kBlock + threadIdx.x);
-        const uint64_t wk = static_cast<uint64_t>(r.w) << 32;
-        if (p.min_partner) {
-          red_min(&p.minval[r.a], wk | r.b);
-          red_min(&p.minval[r.b], wk | r.a);
-        } else {
-          red_min(&p.minval[r.a], wk | (seg0 + offs[j]));
-          red_min(&p.minval[r.b], wk | (seg0 + offs[j]));
-        }
+  for (int c = 0; c < NOUT; ++c) {
+    Rec* sg = p.out[c].base + static_cast<uint64_t>(seg_id(p)) * p.out[c].cap;
+    const uint32_t cap = static_cast<uint32_t>(p.out[c].cap);
+    const uint32_t run0 = static_cast<uint32_t>(run[c]);
+    const uint64_t seg0 = static_cast<uint64_t>(seg_id(p)) * p.out[c].cap + run0;
+    for (uint32_t i = threadIdx.x; i < tot[c]; i += kBlock) {
+      const uint32_t local = run0 + i;
+      if (local >= cap) {
+        atomicOr(p.err, kErrOverflow);
+        continue;
       }
-    } else {
-      constexpr int G = 4;  // items per batch of filter reads
-#pragma unroll
-      for (int g = 0; g < ITEMS; g += G) {
-        uint64_t cur[2 * G];
-#pragma unroll
-        for (int q = 0; q < G && g + q < ITEMS; ++q) {
-          if (!((min_mask >> (g + q)) & 1u)) continue;
-          const Rec r = rec((g + q) * kBlock + threadIdx.x);
-          cur[2 * q] = ld_weak(&p.minval[r.a]);
-          cur[2 * q + 1] = ld_weak(&p.minval[r.b]);
-        }
-#pragma unroll
-        for (int q = 0; q < G && g + q < ITEMS; ++q) {
-          if (!((min_mask >> (g + q)) & 1u)) continue;
-          const Rec r = rec((g + q) * kBlock + threadIdx.x);
-          const uint64_t wk = static_cast<uint64_t>(r.w) << 32;
-          const uint64_t va = p.min_partner ? (wk | r.b) : (wk | (seg0 + offs[g + q]));
-          const uint64_t vb = p.min_partner ? (wk | r.a) : (wk | (seg0 + offs[g + q]));
-          if (va < cur[2 * q]) red_min(&p.minval[r.a], va);
-          if (vb < cur[2 * q + 1]) red_min(&p.minval[r.b], vb);
-        }
+      const Rec r = rec(s_dense[cbase[c] + i]);
+      sg[local] = r;
+      if (c != 0 || p.minval == nullptr) continue;
+      const uint64_t wk = static_cast<uint64_t>(r.w) << 32;
+      const uint64_t va = p.min_partner ? (wk | r.b) : (wk | (seg0 + i));
+      const uint64_t vb = p.min_partner ? (wk | r.a) : (wk | (seg0 + i));
+      if (p.min_checked) {
+        const uint64_t ca = ld_weak(&p.minval[r.a]), cb = ld_weak(&p.minval[r.b]);
+        if (va < ca) red_min(&p.minval[r.a], va);
+        if (vb < cb) red_min(&p.minval[r.b], vb);
+      } else {
+        red_min(&p.minval[r.a], va);
+        red_min(&p.minval[r.b], vb);
       }
     }
   }
 #pragma unroll
-  for (int c = 0; c < NOUT; ++c) run[c] += s_tot[c];
+  for (int c = 0; c < NOUT; ++c) run[c] += tot[c];
 }
 
 template <int NOUT>
@@ -255,7 +233,7 @@ __device__ __forceinline__ void seg_pass_end(const uint64_t (&run)[NOUT], uint32
 // item j of thread t is tile item j*kBlock + t, so consecutive lanes read
 // consecutive records (conflict-free) and write consecutive output slots.
 // Items per thread is a tile-size knob (kamsta_cfg.items_per_thread: 6, 8
-// or 12; 8 by default, the fastest on GB300 at 2^26/2^30).
+// or 12; 6 by default, the fastest on GB300 at 2^26/2^30).
 constexpr uint32_t dir_tile(int items) { return static_cast<uint32_t>(items) * kBlock; }
 constexpr size_t dir_dyn_smem(int items) { return 2ull * dir_tile(items) * 3 * sizeof(uint32_t); }
 constexpr uint32_t kDirTile = dir_tile(kItemsDir);
@@ -383,14 +361,15 @@ __global__ void __launch_bounds__(kBlock, ITEMS <= 8 ? 4 : 3)
         cls[j] = weight_class<NOUT>(ww[j], p);
       }
     }
-    seg_tile_finish<NOUT, kItemsDir>(cls, run, p, [&](uint32_t t) {
+    auto rec_at = [&](uint32_t t) {
       Rec r;
       r.a = words[3 * t];
       r.b = words[3 * t + 1];
       r.w = words[3 * t + 2];
       r.oid = static_cast<uint32_t>(base + t);
       return r;
-    });
+    };
+    seg_tile_finish<NOUT, kItemsDir>(cls, run, p, rec_at);
   }
   seg_pass_end<NOUT>(run, dropped_w, cand, p);
 }

@@ -76,9 +76,9 @@ void Arena::release() {
 
 static inline size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 // Entries per thread of the mapped (relabelling) passes over the directed
-// input when the first pass uses 8: the mapped 8-entry kernel spills (its
-// label gathers need registers); 6 entries do not (R-MAT 2^24 class pass
-// 1.98 -> 1.36 ms, RHG 1.55 -> 1.35 ms).
+// input when the first pass uses 8: 6 (R-MAT 2^24 class pass 1.98 -> 1.36
+// ms, RHG 1.55 -> 1.35 ms, when the 8-entry kernel still spilled; 8 gains
+// nothing since).
 constexpr int kMappedDirItems = 6;
 static inline uint32_t ceil_div(uint64_t a, uint64_t b) {
   return static_cast<uint32_t>((a + b - 1) / b);
@@ -485,7 +485,7 @@ kamsta_status Solve::pass(int phase, const SegList* src, const uint32_t* map, ui
     a.aligned16 = aligned16_ ? 1 : 0;
     const int t0 = tick();
     bool launched = false;
-    if (dir && !mapped && !input_complete_ && items == 8 && attempt == 0) {
+    if (dir && !mapped && !input_complete_ && attempt == 0) {
       // the input is still arriving: launch the CTAs whose chunks have landed
       uint32_t b0 = 0;
       for (int k = 0; k < io_->pieces && b0 < G; ++k) {
@@ -496,7 +496,9 @@ kamsta_status Solve::pass(int phase, const SegList* src, const uint32_t* map, ui
         if (b1 <= b0) continue;
         KS_TRY(wait_input(k));
         a.cta_base = b0;
-        k_pass_dir<NOUT, 8, false><<<b1 - b0, kBlock, dyn, st_>>>(in_, a);
+        if (items == 8) k_pass_dir<NOUT, 8, false><<<b1 - b0, kBlock, dyn, st_>>>(in_, a);
+        else if (items == 6) k_pass_dir<NOUT, 6, false><<<b1 - b0, kBlock, dyn, st_>>>(in_, a);
+        else k_pass_dir<NOUT, 12, false><<<b1 - b0, kBlock, dyn, st_>>>(in_, a);
         b0 = b1;
       }
       a.cta_base = 0;
