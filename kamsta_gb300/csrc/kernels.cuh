@@ -1259,12 +1259,6 @@ __global__ void k_row_scan(const uint32_t* __restrict__ in, uint64_t md, uint32_
 
 __global__ void k_set_u32(uint32_t* p, uint32_t v) { *p = v; }
 
-__global__ void k_iota_u32(uint64_t k, uint32_t* __restrict__ idx) {
-  for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < k;
-       i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
-    idx[i] = static_cast<uint32_t>(i);
-}
-
 // out[p] = in[idx[p]] and the round-0 minimum with position p.  Nearly every
 // record has the largest component (`hub`) as one endpoint: its minimum is
 // reduced in registers and per warp, one atomic per warp; the other
@@ -1323,9 +1317,9 @@ __global__ void k_relabel_all(uint32_t n, uint32_t* __restrict__ P,
 }
 
 __global__ void k_iota(uint32_t n, uint32_t* __restrict__ a) {
-  for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n;
-       x += gridDim.x * blockDim.x)
-    a[x] = x;
+  for (uint64_t x = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; x < n;
+       x += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+    a[x] = static_cast<uint32_t>(x);
 }
 
 __global__ void k_fill64(uint64_t n, uint64_t* __restrict__ a, uint64_t v) {

@@ -944,7 +944,7 @@ kamsta_status Solve::contract_rows(uint32_t wmin, uint32_t wmax, SegList* E, boo
                                                D_, big_, big_label_, wmin, wmax, canon, key_bits,
                                                tmp, keys, k, &ctx_->d_counters[kCMisc].cnt[2],
                                                ctx_->d_err);
-    k_iota_u32<<<grid_for(k), kBlock, 0, st_>>>(k, idx);
+    k_iota<<<grid_for(k), kBlock, 0, st_>>>(static_cast<uint32_t>(k), idx);
     int alt = 0;
     cudaError_t e = radix_sort_pairs_u32(st_, keys, keys2, idx, idx2, k,
                                          static_cast<int>(2 * key_bits), counts, status,
