@@ -376,6 +376,14 @@ kamsta_status kamsta_mst_boruvka_7bit(const kamsta_cgraph* g, const kamsta_cfg* 
  * largest id + 1 (ids < 2^28).  kamsta_wedge9_capacity gives an upper bound
  * of the entries written (records, doubled when symmetrising). */
 #define KAMSTA_LOAD_SYMMETRIZE 0x1u
+
+/* Edge weights of the geometric generators (the reference's distance types,
+ * benchmarks/mst_benchmarks.hpp:59-64): a seeded hash, or from the
+ * distance d <= R of the endpoints: 1 + floor((max_weight - 1) d / R), or
+ * 1 + floor((max_weight - 1) d^2 / R^2). */
+#define KAMSTA_DISTANCE_RANDOM 0u
+#define KAMSTA_DISTANCE_EUCLIDEAN 1u
+#define KAMSTA_DISTANCE_SQUARED_EUCLIDEAN 2u
 kamsta_status kamsta_wedge9_capacity(const char* const* paths, uint32_t num_paths,
                                      uint32_t flags, uint64_t* capacity);
 kamsta_status kamsta_load_wedge9_dev(kamsta_ctx* ctx, const char* const* paths,
@@ -413,12 +421,14 @@ kamsta_status kamsta_gen_gnm_dev(kamsta_ctx* ctx, uint32_t n, uint64_t m,
  * expected degree d away from the border, radius = sqrt(d / (pi n))).  The
  * edge count is data dependent: with d_out == NULL the call only counts
  * (*m_directed_out = entries needed); with capacity < that count it returns
- * KAMSTA_E_INPUT and the count.  Stand-in for get_rgg2D
+ * KAMSTA_E_INPUT and the count.  `distance` is a KAMSTA_DISTANCE_* weight
+ * rule (KAMSTA_DISTANCE_RANDOM: the hash weight).  Stand-in for get_rgg2D
  * (benchmarks/mst_benchmarks.hpp:133-139). */
 kamsta_status kamsta_gen_rgg2d_dev(kamsta_ctx* ctx, uint32_t n, double radius,
                                    uint64_t seed, uint32_t max_weight,
-                                   kamsta_wedge* d_out, uint64_t capacity,
-                                   uint64_t* m_directed_out, kamsta_stream stream);
+                                   uint32_t distance, kamsta_wedge* d_out,
+                                   uint64_t capacity, uint64_t* m_directed_out,
+                                   kamsta_stream stream);
 /* Threshold random hyperbolic graph: power-law exponent gamma > 2 (the
  * reference's --gamma), target average degree avg_degree; hubs of very high
  * degree.  Counting / capacity convention as kamsta_gen_rgg2d_dev.  The
@@ -442,12 +452,13 @@ kamsta_status kamsta_gen_grid_dev(kamsta_ctx* ctx, uint32_t x, uint32_t y, uint3
                                   kamsta_stream stream);
 /* 3-D random geometric graph in the unit cube (radius in [0, 1]; for an
  * expected degree d away from the border, radius = cbrt(3 d / (4 pi n))).
- * Counting / capacity convention as kamsta_gen_rgg2d_dev.  Stand-in for
- * get_rgg3D (benchmarks/mst_benchmarks.hpp:140-146). */
+ * Counting / capacity convention and `distance` as kamsta_gen_rgg2d_dev.
+ * Stand-in for get_rgg3D (benchmarks/mst_benchmarks.hpp:140-146). */
 kamsta_status kamsta_gen_rgg3d_dev(kamsta_ctx* ctx, uint32_t n, double radius,
                                    uint64_t seed, uint32_t max_weight,
-                                   kamsta_wedge* d_out, uint64_t capacity,
-                                   uint64_t* m_directed_out, kamsta_stream stream);
+                                   uint32_t distance, kamsta_wedge* d_out,
+                                   uint64_t capacity, uint64_t* m_directed_out,
+                                   kamsta_stream stream);
 /* R-MAT graph on 2^log_n vertices (log_n <= 31): `samples` (< 2^32 - 4096)
  * recursive quadrant descents with probabilities a, b, c and d = 1 - a - b -
  * c (Graph 500: 0.57, 0.19, 0.19); the graph = the distinct pairs u != v,

@@ -382,13 +382,14 @@ class Context:
         return int(cnt.value)
 
     def gen_rgg2d_dev(self, n: int, radius: float, seed: int, max_weight: int, d_out: int = 0,
-                      capacity: int = 0, stream=0) -> int:
+                      capacity: int = 0, stream=0, distance: int = 0) -> int:
         """Device 2-D random geometric graph.  With d_out == 0 it only counts;
-        returns the number of directed entries."""
+        returns the number of directed entries.  distance: 0 random weights,
+        1 Euclidean, 2 squared Euclidean (KAMSTA_DISTANCE_*)."""
         cnt = C.c_uint64(0)
         check(lib().kamsta_gen_rgg2d_dev(self._h, int(n), float(radius), int(seed),
-                                         int(max_weight), C.c_void_p(d_out or 0), int(capacity),
-                                         C.byref(cnt), C.c_void_p(stream or 0)))
+                                         int(max_weight), int(distance), C.c_void_p(d_out or 0),
+                                         int(capacity), C.byref(cnt), C.c_void_p(stream or 0)))
         return int(cnt.value)
 
     def gen_rhg_dev(self, n: int, gamma: float, avg_degree: float, seed: int, max_weight: int,
@@ -414,13 +415,14 @@ class Context:
         return int(cnt.value)
 
     def gen_rgg3d_dev(self, n: int, radius: float, seed: int, max_weight: int = 254,
-                      d_out: int = 0, capacity: int = 0, stream=0) -> int:
+                      d_out: int = 0, capacity: int = 0, stream=0, distance: int = 0) -> int:
         """Device 3-D random geometric graph in the unit cube.  With
-        d_out == 0 it only counts; returns the directed entries."""
+        d_out == 0 it only counts; returns the directed entries.  distance
+        as in gen_rgg2d_dev."""
         cnt = C.c_uint64(0)
         check(lib().kamsta_gen_rgg3d_dev(self._h, int(n), float(radius), int(seed),
-                                         int(max_weight), C.c_void_p(d_out or 0), int(capacity),
-                                         C.byref(cnt), C.c_void_p(stream or 0)))
+                                         int(max_weight), int(distance), C.c_void_p(d_out or 0),
+                                         int(capacity), C.byref(cnt), C.c_void_p(stream or 0)))
         return int(cnt.value)
 
     def gen_rmat_dev(self, log_n: int, samples: int, seed: int, a: float = 0.57,

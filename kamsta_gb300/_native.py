@@ -24,6 +24,7 @@ FLAG_DEDUPE_NEVER = 0x4
 FLAG_DEDUPE_ALWAYS = 0x8
 FLAG_TRACE = 0x10
 FLAG_FILTER = 0x20
+DISTANCE_RANDOM, DISTANCE_EUCLIDEAN, DISTANCE_SQUARED_EUCLIDEAN = 0, 1, 2
 LOAD_SYMMETRIZE = 0x1
 TRACE_MAX = 128
 PHASES = ["plan", "first_pass", "round_edges", "round_verts", "class_pass", "finalize", "emit",
@@ -159,12 +160,14 @@ SIGNATURES = {
     "kamsta_load_mtx_dev": (I32, [P, C.c_char_p, U64, U32, P, U64, C.POINTER(U64),
                                   C.POINTER(U32), P]),
     "kamsta_gen_gnm_dev": (I32, [P, U32, U64, U64, U32, P, C.POINTER(U64), P]),
-    "kamsta_gen_rgg2d_dev": (I32, [P, U32, C.c_double, U64, U32, P, U64, C.POINTER(U64), P]),
+    "kamsta_gen_rgg2d_dev": (I32, [P, U32, C.c_double, U64, U32, U32, P, U64, C.POINTER(U64),
+                                   P]),
     "kamsta_gen_rhg_dev": (I32, [P, U32, C.c_double, C.c_double, U64, U32, P, U64,
                                  C.POINTER(U64), P]),
     "kamsta_gen_grid_dev": (I32, [P, U32, U32, U32, C.c_double, C.c_int, U64, U32, P, U64,
                                   C.POINTER(U64), P]),
-    "kamsta_gen_rgg3d_dev": (I32, [P, U32, C.c_double, U64, U32, P, U64, C.POINTER(U64), P]),
+    "kamsta_gen_rgg3d_dev": (I32, [P, U32, C.c_double, U64, U32, U32, P, U64, C.POINTER(U64),
+                                   P]),
     "kamsta_gen_rmat_dev": (I32, [P, U32, U64, C.c_double, C.c_double, C.c_double, U64, U32, P,
                                   U64, C.POINTER(U64), P]),
     "kamsta_mst_boruvka_noalloc": (I32, [P, U64, U32, P, C.POINTER(U64), C.POINTER(U64), P]),

@@ -7,6 +7,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
+
+#include "../../include/kamsta_gpu.h"
+
 namespace kamsta {
 
 constexpr uint64_t kInf64 = ~0ull;
@@ -91,6 +95,38 @@ __host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
   z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
   z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
   return z ^ (z >> 31);
+}
+
+// floor(sqrt(x)) for any 64-bit x (a double estimate, corrected exactly).
+__host__ __device__ __forceinline__ uint64_t isqrt_u64(uint64_t x) {
+  uint64_t s = static_cast<uint64_t>(sqrt(static_cast<double>(x)));
+  if (s > 0xffffffffull) s = 0xffffffffull;
+  while (s > 0 && s * s > x) --s;
+  while (s < 0xffffffffull && (s + 1) * (s + 1) <= x) ++s;
+  return s;
+}
+
+// Weight of a geometric generator's edge from its squared integer distance
+// d2 <= R2 (the reference's distance types, benchmarks/mst_benchmarks.hpp:
+// 59-64): random = the hash weight 1 + hi64(mix64(wseed ^ canon) *
+// max_weight); squared Euclidean = 1 + floor((max_weight - 1) d2 / R2);
+// Euclidean = 1 + floor(sqrt(floor((max_weight - 1)^2 d2 / R2))), i.e.
+// 1 + floor((max_weight - 1) d / R).  Exact integer arithmetic, the same on
+// host and device.
+__host__ __device__ __forceinline__ uint32_t geo_weight(uint32_t mode, uint64_t d2, uint64_t R2,
+                                                        uint64_t wseed, uint64_t canon,
+                                                        uint32_t max_weight) {
+  if (mode == KAMSTA_DISTANCE_RANDOM) {
+    const unsigned __int128 p =
+        static_cast<unsigned __int128>(mix64(wseed ^ canon)) * max_weight;
+    return 1u + static_cast<uint32_t>(p >> 64);
+  }
+  if (R2 == 0) return 1u;
+  const uint64_t k = max_weight - 1ull;
+  if (mode == KAMSTA_DISTANCE_SQUARED_EUCLIDEAN)
+    return 1u + static_cast<uint32_t>(static_cast<unsigned __int128>(d2) * k / R2);
+  const unsigned __int128 q = static_cast<unsigned __int128>(d2) * k * k / R2;  // <= k^2
+  return 1u + static_cast<uint32_t>(isqrt_u64(static_cast<uint64_t>(q)));
 }
 
 template <typename T>

@@ -176,7 +176,8 @@ __global__ void k_rgg3_edges(uint32_t n, const uint32_t* __restrict__ px,
                              const uint32_t* __restrict__ py, const uint32_t* __restrict__ pz,
                              const uint32_t* __restrict__ cbeg, uint64_t G, uint64_t R2,
                              uint32_t* __restrict__ deg, const uint32_t* __restrict__ off,
-                             uint64_t wseed, uint32_t max_weight, uint32_t* __restrict__ out) {
+                             uint64_t wseed, uint32_t max_weight, uint32_t mode,
+                             uint32_t* __restrict__ out) {
   GRID_STRIDE_LOOP(j, n) {
     const uint64_t xj = px[j], yj = py[j], zj = pz[j];
     const uint64_t cx = (xj * G) >> 31, cy = (yj * G) >> 31, cz = (zj * G) >> 31;
@@ -193,11 +194,13 @@ __global__ void k_rgg3_edges(uint32_t n, const uint32_t* __restrict__ px,
           if (k == j) continue;
           const uint64_t dx = absdiff(xj, px[k]), dy = absdiff(yj, py[k]),
                          dz = absdiff(zj, pz[k]);
-          if (dx * dx + dy * dy + dz * dz <= R2) {
+          const uint64_t d2 = dx * dx + dy * dy + dz * dz;
+          if (d2 <= R2) {
             if (WRITE) {
+              const uint64_t lo = j < k ? j : k, hi = j < k ? k : j;
               out[3 * o] = static_cast<uint32_t>(j);
               out[3 * o + 1] = k;
-              out[3 * o + 2] = gen_weight(wseed, j < k ? j : k, j < k ? k : j, max_weight);
+              out[3 * o + 2] = geo_weight(mode, d2, R2, wseed, (lo << 32) | hi, max_weight);
               ++o;
             }
             ++d;
@@ -367,11 +370,11 @@ static uint64_t icbrt64(uint64_t n) {
 }
 
 kamsta_status gen_rgg3d(kamsta_ctx* ctx, uint32_t n, double radius, uint64_t seed,
-                        uint32_t max_weight, kamsta_wedge* d_out, uint64_t capacity,
-                        uint64_t* m_out, cudaStream_t st) {
+                        uint32_t max_weight, uint32_t distance, kamsta_wedge* d_out,
+                        uint64_t capacity, uint64_t* m_out, cudaStream_t st) {
   *m_out = 0;
-  if (max_weight == 0) {
-    set_error("gen_rgg3d: max_weight must be >= 1");
+  if (max_weight == 0 || distance > KAMSTA_DISTANCE_SQUARED_EUCLIDEAN) {
+    set_error("gen_rgg3d: max_weight must be >= 1 and distance a KAMSTA_DISTANCE_* value");
     return KAMSTA_E_INPUT;
   }
   if (n == 0) return KAMSTA_OK;
@@ -428,11 +431,11 @@ kamsta_status gen_rgg3d(kamsta_ctx* ctx, uint32_t n, double radius, uint64_t see
       ctx, st, n, "gen_rgg3d", d_out, capacity, m_out,
       [&](uint32_t* deg) {
         k_rgg3_edges<false><<<grid, 256, 0, st>>>(n, px, py, pz, cbeg, G, R2, deg, nullptr, wseed,
-                                                  max_weight, nullptr);
+                                                  max_weight, distance, nullptr);
       },
       [&](uint32_t* deg, uint32_t* off, uint32_t* out) {
         k_rgg3_edges<true><<<grid, 256, 0, st>>>(n, px, py, pz, cbeg, G, R2, deg, off, wseed,
-                                                 max_weight, out);
+                                                 max_weight, distance, out);
       });
 }
 
@@ -571,14 +574,15 @@ extern "C" kamsta_status kamsta_gen_grid_dev(kamsta_ctx* ctx, uint32_t x, uint32
 
 extern "C" kamsta_status kamsta_gen_rgg3d_dev(kamsta_ctx* ctx, uint32_t n, double radius,
                                               uint64_t seed, uint32_t max_weight,
-                                              kamsta_wedge* d_out, uint64_t capacity,
-                                              uint64_t* m_directed_out, kamsta_stream stream) {
+                                              uint32_t distance, kamsta_wedge* d_out,
+                                              uint64_t capacity, uint64_t* m_directed_out,
+                                              kamsta_stream stream) {
   if (!m_directed_out) {
     kamsta::set_error("null pointer argument");
     return KAMSTA_E_INPUT;
   }
-  return kamsta::gen_rgg3d(ctx, n, radius, seed, max_weight, d_out, capacity, m_directed_out,
-                           gen_stream(ctx, stream));
+  return kamsta::gen_rgg3d(ctx, n, radius, seed, max_weight, distance, d_out, capacity,
+                           m_directed_out, gen_stream(ctx, stream));
 }
 
 extern "C" kamsta_status kamsta_gen_rmat_dev(kamsta_ctx* ctx, uint32_t log_n, uint64_t samples,

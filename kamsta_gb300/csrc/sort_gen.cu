@@ -388,7 +388,7 @@ __global__ void k_rgg_edges(uint32_t n, const uint32_t* __restrict__ px,
                             const uint32_t* __restrict__ py, const uint32_t* __restrict__ cbeg,
                             uint64_t G, uint64_t R2, uint32_t* __restrict__ deg,
                             const uint32_t* __restrict__ off, uint64_t wseed, uint32_t max_weight,
-                            uint32_t* __restrict__ out) {
+                            uint32_t mode, uint32_t* __restrict__ out) {
   for (uint64_t j = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; j < n;
        j += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
     const uint64_t xj = px[j], yj = py[j];
@@ -405,14 +405,13 @@ __global__ void k_rgg_edges(uint32_t n, const uint32_t* __restrict__ px,
         const uint64_t xk = px[k], yk = py[k];
         const uint64_t dx = xj > xk ? xj - xk : xk - xj;
         const uint64_t dy = yj > yk ? yj - yk : yk - yj;
-        if (dx * dx + dy * dy <= R2) {
+        const uint64_t d2 = dx * dx + dy * dy;
+        if (d2 <= R2) {
           if (WRITE) {
             const uint64_t lo = j < k ? j : k, hi = j < k ? k : j;
-            const uint64_t canon = (lo << 32) | hi;
             out[3 * o] = static_cast<uint32_t>(j);
             out[3 * o + 1] = k;
-            out[3 * o + 2] = 1u + static_cast<uint32_t>(__umul64hi(mix64(wseed ^ canon),
-                                                                   max_weight));
+            out[3 * o + 2] = geo_weight(mode, d2, R2, wseed, (lo << 32) | hi, max_weight);
             ++o;
           }
           ++d;
@@ -459,11 +458,11 @@ static uint64_t isqrt64(uint64_t n) {
 }
 
 kamsta_status gen_rgg2d(kamsta_ctx* ctx, uint32_t n, double radius, uint64_t seed,
-                        uint32_t max_weight, kamsta_wedge* d_out, uint64_t capacity,
-                        uint64_t* m_out, cudaStream_t st) {
+                        uint32_t max_weight, uint32_t distance, kamsta_wedge* d_out,
+                        uint64_t capacity, uint64_t* m_out, cudaStream_t st) {
   *m_out = 0;
-  if (max_weight == 0) {
-    set_error("gen_rgg2d: max_weight must be >= 1");
+  if (max_weight == 0 || distance > KAMSTA_DISTANCE_SQUARED_EUCLIDEAN) {
+    set_error("gen_rgg2d: max_weight must be >= 1 and distance a KAMSTA_DISTANCE_* value");
     return KAMSTA_E_INPUT;
   }
   if (n == 0) return KAMSTA_OK;
@@ -511,7 +510,7 @@ kamsta_status gen_rgg2d(kamsta_ctx* ctx, uint32_t n, double radius, uint64_t see
   GEN_TRY(tdeg.alloc(&deg, n));
   GEN_TRY(toff.alloc(&off, n));
   k_rgg_edges<false><<<grid, 256, 0, st>>>(n, px, py, cbeg, G, R * R, deg, nullptr, wseed,
-                                           max_weight, nullptr);
+                                           max_weight, distance, nullptr);
   const uint32_t nst = cdiv(n, kScanTile);
   GEN_TRY(cudaMemsetAsync(status, 0, sizeof(uint64_t) * nst, st));
   GEN_TRY(cudaMemsetAsync(d_ticket, 0, sizeof(uint32_t), st));
@@ -542,7 +541,7 @@ kamsta_status gen_rgg2d(kamsta_ctx* ctx, uint32_t n, double radius, uint64_t see
     return KAMSTA_OK;
   }
   k_rgg_edges<true><<<grid, 256, 0, st>>>(n, px, py, cbeg, G, R * R, deg, off, wseed,
-                                          max_weight, reinterpret_cast<uint32_t*>(d_out));
+                                          max_weight, distance, reinterpret_cast<uint32_t*>(d_out));
   GEN_TRY(cudaGetLastError());
   GEN_TRY(cudaStreamSynchronize(st));
   return KAMSTA_OK;
@@ -552,14 +551,16 @@ kamsta_status gen_rgg2d(kamsta_ctx* ctx, uint32_t n, double radius, uint64_t see
 
 extern "C" kamsta_status kamsta_gen_rgg2d_dev(kamsta_ctx* ctx, uint32_t n, double radius,
                                               uint64_t seed, uint32_t max_weight,
-                                              kamsta_wedge* d_out, uint64_t capacity,
-                                              uint64_t* m_directed_out, kamsta_stream stream) {
+                                              uint32_t distance, kamsta_wedge* d_out,
+                                              uint64_t capacity, uint64_t* m_directed_out,
+                                              kamsta_stream stream) {
   if (!m_directed_out) {
     kamsta::set_error("null pointer argument");
     return KAMSTA_E_INPUT;
   }
   cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : (ctx ? ctx->stream : nullptr);
-  return kamsta::gen_rgg2d(ctx, n, radius, seed, max_weight, d_out, capacity, m_directed_out, st);
+  return kamsta::gen_rgg2d(ctx, n, radius, seed, max_weight, distance, d_out, capacity,
+                           m_directed_out, st);
 }
 
 extern "C" kamsta_status kamsta_gen_gnm_dev(kamsta_ctx* ctx, uint32_t n, uint64_t m, uint64_t seed,

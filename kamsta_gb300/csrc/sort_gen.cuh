@@ -42,8 +42,8 @@ kamsta_status gen_gnm(kamsta_ctx* ctx, uint32_t n, uint64_t m, uint64_t seed,
                       cudaStream_t st);
 
 kamsta_status gen_rgg2d(kamsta_ctx* ctx, uint32_t n, double radius, uint64_t seed,
-                        uint32_t max_weight, kamsta_wedge* d_out, uint64_t capacity,
-                        uint64_t* m_out, cudaStream_t st);
+                        uint32_t max_weight, uint32_t distance, kamsta_wedge* d_out,
+                        uint64_t capacity, uint64_t* m_out, cudaStream_t st);
 kamsta_status gen_rhg(kamsta_ctx* ctx, uint32_t n, double gamma, double avg_degree, uint64_t seed,
                       uint32_t max_weight, kamsta_wedge* d_out, uint64_t capacity,
                       uint64_t* m_out, cudaStream_t st);

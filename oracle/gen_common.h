@@ -27,5 +27,28 @@ inline uint32_t weight(uint64_t wseed, uint64_t lo, uint64_t hi, uint32_t max_we
 
 constexpr uint64_t kWeightSalt = 0x6a09e667f3bcc909ull;
 
+/* floor(sqrt(x)), by bisection on 64-bit integers. */
+inline uint64_t isqrt(uint64_t x) {
+  uint64_t lo = 0, hi = 0xffffffffull;
+  while (lo < hi) {
+    const uint64_t mid = lo + (hi - lo + 1) / 2;
+    if (mid * mid <= x) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+/* Weight of a geometric edge with squared distance d2 <= R2 under distance
+ * rule `mode` (0 random: weight(); 1 Euclidean: 1 + floor((max_weight-1)
+ * sqrt(d2 / R2)) computed as 1 + isqrt(floor((max_weight-1)^2 d2 / R2));
+ * 2 squared Euclidean: 1 + floor((max_weight-1) d2 / R2)). */
+inline uint32_t geo_weight(uint32_t mode, uint64_t d2, uint64_t R2, uint64_t wseed, uint64_t lo,
+                           uint64_t hi, uint32_t max_weight) {
+  if (mode == 0) return weight(wseed, lo, hi, max_weight);
+  if (R2 == 0) return 1u;
+  const unsigned __int128 k = max_weight - 1ull;
+  if (mode == 2) return 1u + static_cast<uint32_t>(d2 * k / R2);
+  return 1u + static_cast<uint32_t>(isqrt(static_cast<uint64_t>(d2 * k * k / R2)));
+}
+
 }  // namespace gen
 #endif

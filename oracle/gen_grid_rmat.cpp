@@ -105,9 +105,10 @@ extern "C" int oracle_gen_grid(uint32_t X, uint32_t Y, uint32_t Z, double p, int
 }
 
 extern "C" int oracle_gen_rgg3d(uint32_t n, double radius, uint64_t seed, uint32_t max_weight,
-                                kamsta_wedge* out, uint64_t capacity, uint64_t* m_directed_out) {
+                                uint32_t distance, kamsta_wedge* out, uint64_t capacity,
+                                uint64_t* m_directed_out) {
   *m_directed_out = 0;
-  if (max_weight == 0) return 1;
+  if (max_weight == 0 || distance > 2) return 1;
   if (n == 0) return 0;
   uint64_t R = 0;
   if (!(radius > 0)) R = 0;
@@ -159,8 +160,22 @@ extern "C" int oracle_gen_rgg3d(uint32_t n, double radius, uint64_t seed, uint32
   std::vector<uint64_t> dk;
   for (auto& v : per) dk.insert(dk.end(), v.begin(), v.end());
   __gnu_parallel::sort(dk.begin(), dk.end());
-  return emit_sorted(dk, mix64(seed ^ gen::kWeightSalt), max_weight, out, capacity,
-                     m_directed_out);
+  if (distance == 0)
+    return emit_sorted(dk, mix64(seed ^ gen::kWeightSalt), max_weight, out, capacity,
+                       m_directed_out);
+  *m_directed_out = dk.size();
+  if (dk.size() > capacity) return 2;
+  const uint64_t wseed = mix64(seed ^ gen::kWeightSalt);
+#pragma omp parallel for schedule(static)
+  for (uint64_t i = 0; i < dk.size(); ++i) {
+    const uint64_t j = dk[i] >> 32, k = dk[i] & 0xffffffffull;
+    const uint64_t d2 = ad(px[j], px[k]) * ad(px[j], px[k]) + ad(py[j], py[k]) * ad(py[j], py[k]) +
+                        ad(pz[j], pz[k]) * ad(pz[j], pz[k]);
+    out[i] = kamsta_wedge{static_cast<uint32_t>(j), static_cast<uint32_t>(k),
+                          gen::geo_weight(distance, d2, R2, wseed, std::min(j, k),
+                                          std::max(j, k), max_weight)};
+  }
+  return 0;
 }
 
 extern "C" int oracle_gen_rmat(uint32_t log_n, uint64_t samples, double a, double b, double c,

@@ -496,11 +496,11 @@ inline RggParams rgg_params(uint32_t n, double radius) {
 }  // namespace gen
 
 extern "C" int oracle_gen_rgg2d(uint32_t n, double radius, uint64_t seed, uint32_t max_weight,
-                                kamsta_wedge* out, uint64_t capacity,
+                                uint32_t distance, kamsta_wedge* out, uint64_t capacity,
                                 uint64_t* m_directed_out) {
   using namespace gen;
   *m_directed_out = 0;
-  if (max_weight == 0) return 1;
+  if (max_weight == 0 || distance > 2) return 1;
   if (n == 0) return 0;
   const RggParams P = rgg_params(n, radius);
   const uint64_t base = mix64(seed ^ 0x5247473244ull);
@@ -533,7 +533,7 @@ extern "C" int oracle_gen_rgg2d(uint32_t n, double radius, uint64_t seed, uint32
           if (k == j) continue;
           const uint64_t dx = px[j] > px[k] ? px[j] - px[k] : px[k] - px[j];
           const uint64_t dy = py[j] > py[k] ? py[j] - py[k] : py[k] - py[j];
-          if (dx * dx + dy * dy <= R2) emit(k);
+          if (dx * dx + dy * dy <= R2) emit(k, dx * dx + dy * dy);
         }
       }
   };
@@ -541,7 +541,7 @@ extern "C" int oracle_gen_rgg2d(uint32_t n, double radius, uint64_t seed, uint32
 #pragma omp parallel for schedule(dynamic, 1024)
   for (uint64_t j = 0; j < n; ++j) {
     uint64_t d = 0;
-    visit(j, [&](uint64_t) { ++d; });
+    visit(j, [&](uint64_t, uint64_t) { ++d; });
     off[j + 1] = d;
   }
   for (uint64_t j = 0; j < n; ++j) off[j + 1] += off[j];
@@ -550,9 +550,9 @@ extern "C" int oracle_gen_rgg2d(uint32_t n, double radius, uint64_t seed, uint32
 #pragma omp parallel for schedule(dynamic, 1024)
   for (uint64_t j = 0; j < n; ++j) {
     uint64_t o = off[j];
-    visit(j, [&](uint64_t k) {
-      const uint64_t canon = (std::min(j, k) << 32) | std::max(j, k);
-      const uint32_t w = 1 + static_cast<uint32_t>(hi64(mix64(wseed ^ canon), max_weight));
+    visit(j, [&](uint64_t k, uint64_t d2) {
+      const uint32_t w = geo_weight(distance, d2, R2, wseed, std::min(j, k), std::max(j, k),
+                                    max_weight);
       out[o++] = kamsta_wedge{static_cast<uint32_t>(j), static_cast<uint32_t>(k), w};
     });
   }

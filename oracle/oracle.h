@@ -64,12 +64,14 @@ int oracle_gen_gnm(uint32_t n, uint64_t m, uint64_t seed, uint32_t max_weight,
                    kamsta_wedge* out, uint64_t* m_directed_out);
 
 /* Seeded 2-D random geometric graph (unit square, integer coordinates,
- * radius in [0, 1]); definition in oracle.cpp, bit-identical to the device
- * generator kamsta_gen_rgg2d_dev.  *m_directed_out receives the number of
+ * radius in [0, 1]; `distance` a weight rule as in kamsta_gen_rgg2d_dev);
+ * definition in oracle.cpp, bit-identical to the device generator
+ * kamsta_gen_rgg2d_dev.  *m_directed_out receives the number of
  * directed entries; returns 0, 2 if it exceeds `capacity` (nothing written),
  * 1 on bad arguments. */
 int oracle_gen_rgg2d(uint32_t n, double radius, uint64_t seed, uint32_t max_weight,
-                     kamsta_wedge* out, uint64_t capacity, uint64_t* m_directed_out);
+                     uint32_t distance, kamsta_wedge* out, uint64_t capacity,
+                     uint64_t* m_directed_out);
 
 /* Seeded threshold random hyperbolic graph (power-law exponent gamma > 2,
  * target average degree); definition in oracle.cpp, bit-identical to the
@@ -89,7 +91,8 @@ int oracle_gen_grid(uint32_t x, uint32_t y, uint32_t z, double p, int periodic, 
 /* Seeded 3-D random geometric graph in the unit cube.  Return convention as
  * oracle_gen_rgg2d. */
 int oracle_gen_rgg3d(uint32_t n, double radius, uint64_t seed, uint32_t max_weight,
-                     kamsta_wedge* out, uint64_t capacity, uint64_t* m_directed_out);
+                     uint32_t distance, kamsta_wedge* out, uint64_t capacity,
+                     uint64_t* m_directed_out);
 
 /* Seeded R-MAT graph on 2^log_n vertices from `samples` samples with
  * quadrant probabilities a, b, c (d = 1 - a - b - c).  Return convention as

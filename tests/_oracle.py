@@ -26,12 +26,12 @@ def lib():
         L.oracle_boruvka_filter.argtypes = [P, U64, U32, C.c_int, P, C.POINTER(U64),
                                             C.POINTER(U64), C.POINTER(U32)]
         L.oracle_gen_gnm.argtypes = [U32, U64, U64, U32, P, C.POINTER(U64)]
-        L.oracle_gen_rgg2d.argtypes = [U32, C.c_double, U64, U32, P, U64, C.POINTER(U64)]
+        L.oracle_gen_rgg2d.argtypes = [U32, C.c_double, U64, U32, U32, P, U64, C.POINTER(U64)]
         L.oracle_gen_rhg.argtypes = [U32, C.c_double, C.c_double, U64, U32, P, U64,
                                      C.POINTER(U64)]
         L.oracle_gen_grid.argtypes = [U32, U32, U32, C.c_double, C.c_int, U64, U32, P, U64,
                                       C.POINTER(U64)]
-        L.oracle_gen_rgg3d.argtypes = [U32, C.c_double, U64, U32, P, U64, C.POINTER(U64)]
+        L.oracle_gen_rgg3d.argtypes = [U32, C.c_double, U64, U32, U32, P, U64, C.POINTER(U64)]
         L.oracle_gen_rmat.argtypes = [U32, U64, C.c_double, C.c_double, C.c_double, U64, U32, P,
                                       U64, C.POINTER(U64)]
         L.oracle_max_threads.restype = C.c_int
@@ -48,14 +48,15 @@ def gen_gnm(n: int, m: int, seed: int, max_weight: int = 254) -> np.ndarray:
     return out[: cnt.value]
 
 
-def gen_rgg2d(n: int, radius: float, seed: int, max_weight: int = 254) -> np.ndarray:
+def gen_rgg2d(n: int, radius: float, seed: int, max_weight: int = 254,
+              distance: int = 0) -> np.ndarray:
     cnt = C.c_uint64()
-    rc = lib().oracle_gen_rgg2d(n, radius, seed, max_weight, None, 0, C.byref(cnt))
+    rc = lib().oracle_gen_rgg2d(n, radius, seed, max_weight, distance, None, 0, C.byref(cnt))
     if rc not in (0, 2):
         raise ValueError("oracle_gen_rgg2d: bad arguments")
     out = np.empty(max(cnt.value, 1), WEDGE)
-    rc = lib().oracle_gen_rgg2d(n, radius, seed, max_weight, out.ctypes.data, cnt.value,
-                                C.byref(cnt))
+    rc = lib().oracle_gen_rgg2d(n, radius, seed, max_weight, distance, out.ctypes.data,
+                                cnt.value, C.byref(cnt))
     assert rc == 0
     return out[: cnt.value]
 
@@ -91,8 +92,9 @@ def gen_grid(x: int, y: int, z: int = 1, p: float = 1.0, periodic: bool = True, 
     return _counted(lib().oracle_gen_grid, x, y, z, p, int(periodic), seed, max_weight)
 
 
-def gen_rgg3d(n: int, radius: float, seed: int, max_weight: int = 254) -> np.ndarray:
-    return _counted(lib().oracle_gen_rgg3d, n, radius, seed, max_weight)
+def gen_rgg3d(n: int, radius: float, seed: int, max_weight: int = 254,
+              distance: int = 0) -> np.ndarray:
+    return _counted(lib().oracle_gen_rgg3d, n, radius, seed, max_weight, distance)
 
 
 def gen_rmat(log_n: int, samples: int, seed: int, a: float = 0.57, b: float = 0.19,

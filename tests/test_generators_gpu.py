@@ -174,3 +174,33 @@ def test_mst_on_more_families(kamsta, oracle, algo, family):
     else:
         n, e = 1 << 18, oracle.gen_rmat(18, 1 << 22, 6)
     _check(oracle, fn(e, cfg, n=n), e, n)
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_distance_weights_match_oracle(kamsta, oracle, mode, dim):
+    """Euclidean / squared-Euclidean weights of the geometric generators are
+    bit-identical to the oracle's (exact integer rules)."""
+    ctx = kamsta.Context(0)
+    n = 1 << 16
+    if dim == 2:
+        r = oracle.rgg_radius(n, 12)
+        got = _dev_counted(kamsta, lambda **kw: ctx.gen_rgg2d_dev(n, r, 11, 254, distance=mode,
+                                                                 **kw))
+        ref = oracle.gen_rgg2d(n, r, 11, 254, distance=mode)
+    else:
+        r = oracle.rgg3d_radius(n, 12)
+        got = _dev_counted(kamsta, lambda **kw: ctx.gen_rgg3d_dev(n, r, 11, 254, distance=mode,
+                                                                 **kw))
+        ref = oracle.gen_rgg3d(n, r, 11, 254, distance=mode)
+    assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("algo", ["boruvka_plain", "boruvka_local", "filter_boruvka"])
+def test_mst_on_euclidean_rgg(kamsta, oracle, algo):
+    """Distance weights make the MSF geometric (and tie often: 254 levels)."""
+    from tests.test_parity_gpu import _check, _configs
+    fn, cfg = _configs(kamsta)[algo]
+    n = 1 << 17
+    e = oracle.gen_rgg2d(n, oracle.rgg_radius(n, 10), 12, 254, distance=1)
+    _check(oracle, fn(e, cfg, n=n), e, n)

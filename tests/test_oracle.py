@@ -103,7 +103,20 @@ def _mix64(z):
     return z ^ (z >> 31)
 
 
-def _py_rgg2d(n, radius, seed, wmax=254):
+def _geo_w(mode, d2, R2, wseed, j, k, wmax):
+    """The generators' weight rules: hash, Euclidean, squared Euclidean."""
+    import math
+    if mode == 0:
+        canon = (min(j, k) << 32) | max(j, k)
+        return 1 + ((_mix64(wseed ^ canon) * wmax) >> 64)
+    if R2 == 0:
+        return 1
+    if mode == 2:
+        return 1 + (d2 * (wmax - 1)) // R2
+    return 1 + math.isqrt((d2 * (wmax - 1) ** 2) // R2)
+
+
+def _py_rgg2d(n, radius, seed, wmax=254, mode=0):
     """All-pairs restatement of the RGG-2D definition (small n only)."""
     base = _mix64(seed ^ 0x5247473244)
     wseed = _mix64(seed ^ 0x6A09E667F3BCC909)
@@ -122,10 +135,9 @@ def _py_rgg2d(n, radius, seed, wmax=254):
     out = []
     for j, (_, _, xj, yj) in enumerate(pts):
         for k, (_, _, xk, yk) in enumerate(pts):
-            if k != j and (xj - xk) ** 2 + (yj - yk) ** 2 <= R * R:
-                canon = (min(j, k) << 32) | max(j, k)
-                w = 1 + ((_mix64(wseed ^ canon) * wmax) >> 64)
-                out.append((j, k, w))
+            d2 = (xj - xk) ** 2 + (yj - yk) ** 2
+            if k != j and d2 <= R * R:
+                out.append((j, k, _geo_w(mode, d2, R * R, wseed, j, k, wmax)))
     return out
 
 
@@ -350,3 +362,26 @@ def test_rmat_properties(oracle):
     assert np.array_equal(np.sort((d << np.uint64(32)) | s), k)
     deg = np.bincount(e["src"], minlength=1 << 16)
     assert deg[0] == deg.max() and deg[0] > 100 * len(e) / (1 << 16)  # hub at id 0
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("n,radius,seed,wmax", [(40, 0.3, 2, 254), (200, 0.1, 3, 7),
+                                                (90, 1.0, 4, 1 << 20), (50, 0.0, 5, 254)])
+def test_rgg2d_distance_weights_match_definition(oracle, mode, n, radius, seed, wmax):
+    e = oracle.gen_rgg2d(n, radius, seed, wmax, distance=mode)
+    got = [(int(a), int(b), int(w)) for a, b, w in zip(e["src"], e["dst"], e["w"])]
+    assert got == _py_rgg2d(n, radius, seed, wmax, mode)
+
+
+def test_distance_weights_follow_distance(oracle):
+    """Euclidean and squared weights grow with the distance, stay in
+    [1, max_weight], and agree on the edge set with the hash weights."""
+    n = 1 << 12
+    r = oracle.rgg_radius(n, 12)
+    base = oracle.gen_rgg2d(n, r, 8)
+    for mode in (1, 2):
+        e = oracle.gen_rgg2d(n, r, 8, 254, distance=mode)
+        assert np.array_equal(e["src"], base["src"]) and np.array_equal(e["dst"], base["dst"])
+        assert e["w"].min() >= 1 and e["w"].max() <= 254
+    e3 = oracle.gen_rgg3d(1 << 12, oracle.rgg3d_radius(1 << 12, 12), 8, 254, distance=1)
+    assert e3["w"].min() >= 1 and e3["w"].max() <= 254
