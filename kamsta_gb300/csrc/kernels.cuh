@@ -1123,18 +1123,33 @@ __global__ void k_big_bitmap(uint32_t n, const uint32_t* __restrict__ D, uint32_
 // copies.  With `canon` set (the batch's forest bitmap, which needs the
 // src < dst copy's position) the position of that copy is searched for.
 
-// Vertices outside the largest component (bit 0 in `big`), any order.
+// Vertices outside the largest component (bit 0 in `big`), any order; one
+// counter atomic per warp and step.
 __global__ void k_outside_big(uint32_t n, const uint32_t* __restrict__ big, uint32_t* __restrict__ out,
                              uint32_t cap, unsigned long long* count) {
   const uint32_t words = (n + 31) / 32;
-  for (uint32_t wi = blockIdx.x * blockDim.x + threadIdx.x; wi < words;
-       wi += gridDim.x * blockDim.x) {
-    uint32_t f = ~big[wi];
+  const uint32_t lane = lane_id();
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t start = blockIdx.x * blockDim.x + threadIdx.x;
+  for (uint32_t w0 = start - lane; w0 < words; w0 += stride) {  // warp-uniform loop
+    const uint32_t wi = w0 + lane;
+    uint32_t f = 0;
     const uint32_t base = wi * 32;
-    if (base + 32 > n) f &= (n - base >= 32) ? ~0u : ((1u << (n - base)) - 1);
-    if (!f) continue;
-    const uint64_t o = atomicAdd(count, static_cast<unsigned long long>(__popc(f)));
-    uint64_t k = o;
+    if (wi < words) {
+      f = ~big[wi];
+      if (base + 32 > n) f &= (n - base >= 32) ? ~0u : ((1u << (n - base)) - 1);
+    }
+    const uint32_t c = __popc(f);
+    uint32_t incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, incl, o);
+      if (lane >= static_cast<uint32_t>(o)) incl += y;
+    }
+    unsigned long long wbase = 0;
+    if (lane == 31 && incl) wbase = atomicAdd(count, static_cast<unsigned long long>(incl));
+    wbase = __shfl_sync(kFull, wbase, 31);
+    uint64_t k = wbase + incl - c;
     while (f) {
       const uint32_t b = __ffs(f) - 1;
       f &= f - 1;
@@ -1142,6 +1157,17 @@ __global__ void k_outside_big(uint32_t n, const uint32_t* __restrict__ big, uint
       ++k;
     }
   }
+}
+
+// Fence index of the (src, dst)-sorted input: fence[i] = src of entry
+// i * kFenceStep (i < ceil(md / kFenceStep)).  A row search then runs on the
+// fences (a few MB, L2-resident) and then inside one kFenceStep window.
+constexpr uint32_t kFenceStep = 1024;
+__global__ void k_fences(const uint32_t* __restrict__ in, uint64_t md, uint32_t* __restrict__ fence) {
+  const uint64_t nf = (md + kFenceStep - 1) / kFenceStep;
+  for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < nf;
+       i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+    fence[i] = in[3 * i * kFenceStep];
 }
 
 // first directed entry with src >= v (entries [0, md) sorted by src); one
@@ -1156,13 +1182,37 @@ __device__ __forceinline__ uint64_t row_begin(const uint32_t* __restrict__ in, u
   return lo;
 }
 
-// The same with the whole warp: 32 probes per step shrink the range 33-fold,
-// so a row of 2^31 entries is found in 7 dependent steps instead of 31.
-// Called by all 32 lanes with the same v; every lane returns the answer.
+// The same with the whole warp: 32 probes per step shrink the range 33-fold.
+// The fences narrow the range to one kFenceStep window first (their steps
+// hit L2), so only two steps read the input.  Called by all 32 lanes with
+// the same v; every lane returns the answer.
 __device__ __forceinline__ uint64_t row_begin_warp(const uint32_t* __restrict__ in, uint64_t md,
+                                                   const uint32_t* __restrict__ fence,
                                                    uint32_t v) {
   const uint32_t lane = lane_id();
   uint64_t lo = 0, hi = md;  // the answer lies in [lo, hi]
+  {
+    // first fence with src >= v: the answer lies in ((f - 1) step, f step]
+    const uint64_t nf = (md + kFenceStep - 1) / kFenceStep;
+    uint64_t flo = 0, fhi = nf;
+    while (fhi - flo > 32) {
+      const uint64_t span = fhi - flo;
+      const uint64_t p = flo + span * (lane + 1) / 33;
+      const uint32_t c = __popc(__ballot_sync(kFull, fence[p] < v));
+      const uint64_t below = __shfl_sync(kFull, p, c == 0 ? 0 : c - 1);
+      const uint64_t above = __shfl_sync(kFull, p, c == 32 ? 31 : c);
+      if (c == 0) fhi = above;
+      else if (c == 32) flo = below + 1;
+      else {
+        flo = below + 1;
+        fhi = above;
+      }
+    }
+    const uint64_t q = flo + lane;
+    const uint64_t f = flo + __popc(__ballot_sync(kFull, q < fhi && fence[q] < v));
+    lo = f == 0 ? 0 : (f - 1) * kFenceStep;
+    hi = f * kFenceStep < md ? f * kFenceStep : md;
+  }
   while (hi - lo > 32) {
     const uint64_t span = hi - lo;
     const uint64_t p = lo + span * (lane + 1) / 33;  // in [lo, hi), increasing in lane
@@ -1188,6 +1238,7 @@ __device__ __forceinline__ uint64_t row_begin_warp(const uint32_t* __restrict__ 
 template <bool WRITE>
 __global__ void k_row_scan(const uint32_t* __restrict__ in, uint64_t md, uint32_t n,
                            const uint32_t* __restrict__ S, uint32_t ns, uint32_t* __restrict__ row_lo,
+                           const uint32_t* __restrict__ fence,
                            const uint32_t* __restrict__ D, const uint32_t* __restrict__ big,
                            uint32_t big_label, uint32_t wmin, uint32_t wmax, uint32_t canon,
                            uint32_t key_bits, Rec* __restrict__ out, uint64_t* __restrict__ keys,
@@ -1200,7 +1251,7 @@ __global__ void k_row_scan(const uint32_t* __restrict__ in, uint64_t md, uint32_
     if (WRITE) {
       lo = row_lo[k];
     } else {
-      lo = row_begin_warp(in, md, v);
+      lo = row_begin_warp(in, md, fence, v);
       if (lane == 0) row_lo[k] = static_cast<uint32_t>(lo);
     }
     const uint32_t la = D[v];

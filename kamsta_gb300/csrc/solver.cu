@@ -892,8 +892,11 @@ kamsta_status Solve::contract_rows(uint32_t wmin, uint32_t wmax, SegList* E, boo
   *done = false;
   // the vertices outside the largest component
   const uint32_t cap_s = std::max<uint32_t>(1u << 16, n_ / 32);
-  void* smem = nullptr;  // outside vertices, then their row starts
-  CU_TRY(cudaMallocFromPoolAsync(&smem, sizeof(uint32_t) * 2 * uint64_t(cap_s), ctx_->pool, st_));
+  // outside vertices, their row starts, then the input's fence index
+  const uint64_t nfence = (md_ + kFenceStep - 1) / kFenceStep;
+  void* smem = nullptr;
+  CU_TRY(cudaMallocFromPoolAsync(&smem, sizeof(uint32_t) * (2 * uint64_t(cap_s) + nfence + 1),
+                                 ctx_->pool, st_));
   struct Free {
     void* p;
     cudaStream_t s;
@@ -903,6 +906,7 @@ kamsta_status Solve::contract_rows(uint32_t wmin, uint32_t wmax, SegList* E, boo
   } fs{smem, st_};
   uint32_t* S = static_cast<uint32_t*>(smem);
   uint32_t* row_lo = S + cap_s;
+  uint32_t* fence = row_lo + cap_s;
   const int t0 = tick();
   CU_TRY(cudaMemsetAsync(ctx_->d_counters + kCMisc, 0, sizeof(DevCounters), st_));
   unsigned long long* cnt = &ctx_->d_counters[kCMisc].cnt[0];
@@ -917,8 +921,10 @@ kamsta_status Solve::contract_rows(uint32_t wmin, uint32_t wmax, SegList* E, boo
   while (key_bits < 32 && (1ull << key_bits) < n_) ++key_bits;
   const uint32_t canon = forest_bits_ != nullptr ? 1u : 0u;
   // count (and find the rows), then write the surviving edges
+  k_fences<<<grid_for(nfence), kBlock, 0, st_>>>(in_, md_, fence);
   k_row_scan<false><<<grid, kBlock, 0, st_>>>(in_, md_, n_, S, static_cast<uint32_t>(ns), row_lo,
-                                              D_, big_, big_label_, wmin, wmax, canon, key_bits,
+                                              fence, D_, big_, big_label_, wmin, wmax, canon,
+                                              key_bits,
                                               nullptr, nullptr, 0,
                                               &ctx_->d_counters[kCMisc].cnt[1], ctx_->d_err);
   KS_TRY(fetch_counters());
@@ -941,7 +947,8 @@ kamsta_status Solve::contract_rows(uint32_t wmin, uint32_t wmax, SegList* E, boo
     uint32_t* counts = reinterpret_cast<uint32_t*>(m + rb + 2 * kb + 2 * ib);
     uint64_t* status = reinterpret_cast<uint64_t*>(m + rb + 2 * kb + 2 * ib + cb);
     k_row_scan<true><<<grid, kBlock, 0, st_>>>(in_, md_, n_, S, static_cast<uint32_t>(ns), row_lo,
-                                               D_, big_, big_label_, wmin, wmax, canon, key_bits,
+                                               fence, D_, big_, big_label_, wmin, wmax, canon,
+                                               key_bits,
                                                tmp, keys, k, &ctx_->d_counters[kCMisc].cnt[2],
                                                ctx_->d_err);
     k_iota<<<grid_for(k), kBlock, 0, st_>>>(static_cast<uint32_t>(k), idx);
