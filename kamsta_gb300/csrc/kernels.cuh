@@ -68,7 +68,10 @@ struct PassArgs {
   uint32_t min_checked;  // filter minimum updates by a cached read (hub-heavy passes)
   // Minimum keys (w << 32 | partner) instead of (w << 32 | list position):
   // the first pass over original ids, without parallel edges, where a
-  // vertex's canonical (w, min, max) order is its (w, partner) order.
+  // vertex's canonical (w, min, max) order is its (w, partner) order.  Both
+  // directions are stored, so every copy (v, u, w) feeds v's minimum from
+  // v's own row: the updates follow the (src, dst) order of the stream
+  // instead of scattering to both endpoints of the kept record.
   uint32_t min_partner;
   uint64_t total;  // logical input items
   uint64_t chunk;  // logical items per CTA (a multiple of the tile size)
@@ -187,17 +190,15 @@ __device__ __forceinline__ void seg_tile_finish(const uint8_t (&cls)[ITEMS],
       }
       const Rec r = rec(s_dense[cbase[c] + i]);
       sg[local] = r;
-      if (c != 0 || p.minval == nullptr) continue;
-      const uint64_t wk = static_cast<uint64_t>(r.w) << 32;
-      const uint64_t va = p.min_partner ? (wk | r.b) : (wk | (seg0 + i));
-      const uint64_t vb = p.min_partner ? (wk | r.a) : (wk | (seg0 + i));
+      if (c != 0 || p.minval == nullptr || p.min_partner) continue;
+      const uint64_t v = (static_cast<uint64_t>(r.w) << 32) | (seg0 + i);
       if (p.min_checked) {
         const uint64_t ca = ld_weak(&p.minval[r.a]), cb = ld_weak(&p.minval[r.b]);
-        if (va < ca) red_min(&p.minval[r.a], va);
-        if (vb < cb) red_min(&p.minval[r.b], vb);
+        if (v < ca) red_min(&p.minval[r.a], v);
+        if (v < cb) red_min(&p.minval[r.b], v);
       } else {
-        red_min(&p.minval[r.a], va);
-        red_min(&p.minval[r.b], vb);
+        red_min(&p.minval[r.a], v);
+        red_min(&p.minval[r.b], v);
       }
     }
   }
@@ -323,8 +324,14 @@ __global__ void __launch_bounds__(kBlock, ITEMS <= 8 ? 4 : 3)
         const uint32_t t = j * kBlock + threadIdx.x;
         const uint32_t s = words[3 * t], d = words[3 * t + 1], wt = words[3 * t + 2];
         cls[j] = 0xff;
-        if (t >= cnt || !(s < d) || d >= p.n) continue;
-        if (wt < p.wmin || wt > p.wmax) {
+        if (t >= cnt || s == d || s >= p.n || d >= p.n) continue;
+        const bool in_w = wt >= p.wmin && wt <= p.wmax;
+        // partner keys: every copy feeds its own row's minimum, so a
+        // tile's updates go to a few consecutive addresses
+        if (p.min_partner && in_w && weight_class<NOUT>(wt, p) == 0)
+          red_min(&p.minval[s], (static_cast<uint64_t>(wt) << 32) | d);
+        if (!(s < d)) continue;
+        if (!in_w) {
           dropped_w += (wt > p.wmax) ? 1u : 0u;
           continue;
         }

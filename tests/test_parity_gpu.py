@@ -138,6 +138,23 @@ def test_validation_rejects_unsorted_and_out_of_range(kamsta, oracle):
     _check(oracle, kamsta.boruvka(e, cfg, n=100), e, 100)
 
 
+def test_validation_across_input_pieces(kamsta, oracle):
+    """The host entry point copies the input in 16 pieces and starts the
+    first pass on each as it lands; validation must still compare every
+    entry with its predecessor, including across pieces and CTA chunks."""
+    n = 1 << 18
+    e = oracle.gen_gnm(n, 1 << 22, 33)
+    cfg = kamsta.AlgorithmConfig(validate=True)
+    _check(oracle, kamsta.boruvka(e, cfg, n=n), e, n)
+    per = (len(e) + 15) // 16
+    for at in (per, 7 * per, len(e) // 2):  # piece boundaries and a mid point
+        bad = e.copy()
+        bad[[at - 1, at]] = bad[[at, at - 1]]
+        with pytest.raises(kamsta.KamstaError) as ei:
+            kamsta.boruvka(bad, cfg, n=n)
+        assert ei.value.status == 1
+
+
 def test_wedge64_entry_point(kamsta, oracle):
     e = oracle.gen_gnm(2000, 10000, 31)
     e64 = np.zeros(len(e), kamsta.WEDGE64)
