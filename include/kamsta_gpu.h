@@ -52,6 +52,7 @@ typedef int kamsta_status;
 #define KAMSTA_E_UNSUPPORTED 5 /* option not implemented on this build        */
 #define KAMSTA_E_BUDGET 6      /* request larger than the serving budget      */
 #define KAMSTA_E_NOTREADY 7    /* serving: result not finished yet            */
+#define KAMSTA_E_CANCELLED 8   /* serving: job withdrawn before it ran        */
 
 /* ---- edge layouts -------------------------------------------------------- */
 /* Packed 12-byte weighted edge; same field order and width as WEdge_4_4
@@ -148,6 +149,11 @@ kamsta_status kamsta_ctx_destroy(kamsta_ctx* ctx);
 kamsta_status kamsta_ctx_trim(kamsta_ctx* ctx);
 /* Device bytes currently held by the context's scratch pool. */
 uint64_t kamsta_ctx_pool_bytes(const kamsta_ctx* ctx);
+/* Caps the device bytes the context may have in use (live allocations of
+ * its scratch pool plus its arenas); 0 = no cap (the default).  A call that
+ * would go over it fails with KAMSTA_E_OOM and leaves the context usable,
+ * like a failed device allocation. */
+kamsta_status kamsta_ctx_set_memory_limit(kamsta_ctx* ctx, uint64_t bytes);
 
 /* ---- single-graph solve, host buffers ----------------------------------
  * edges: m_directed entries (host memory); out: capacity >= n-1 entries
@@ -300,6 +306,7 @@ typedef struct kamsta_completion {
   uint64_t ticket;             /* from kamsta_server_submit                  */
   uint64_t user_tag;
   kamsta_status status;        /* KAMSTA_OK / KAMSTA_E_INPUT / solver error  */
+                               /* / KAMSTA_E_CANCELLED                       */
   uint32_t batch_size;         /* jobs in the wave that solved this one      */
   uint64_t out_count;
   uint64_t total_weight;
@@ -318,6 +325,11 @@ kamsta_status kamsta_server_submit(kamsta_server* server, const kamsta_request* 
  * KAMSTA_E_NOTREADY (count 0) when none finished in time. */
 kamsta_status kamsta_server_poll(kamsta_server* server, kamsta_completion* out,
                                  uint32_t cap, uint32_t* count, uint32_t timeout_us);
+/* Withdraws a job that is still queued: it completes at once with status
+ * KAMSTA_E_CANCELLED (batch_size 0) and never touches its buffers.
+ * KAMSTA_E_NOTREADY if the ticket is not queued (already in a wave,
+ * finished, or unknown); such a job completes normally. */
+kamsta_status kamsta_server_cancel(kamsta_server* server, uint64_t ticket);
 kamsta_status kamsta_server_stats(kamsta_server* server, uint64_t* queued,
                                   uint64_t* in_flight, uint64_t* bytes_in_use,
                                   uint64_t* waves);

@@ -290,6 +290,15 @@ class Server:
                  "start_us": c.start_us, "finish_us": c.finish_us}
                 for c in self._buf[: cnt.value]]
 
+    def cancel(self, ticket: int) -> bool:
+        """Withdraw a queued job (it completes with E_CANCELLED); False if it
+        is already in a wave or finished."""
+        s = lib().kamsta_server_cancel(self._h, int(ticket))
+        if s == _native.E_NOTREADY:
+            return False
+        check(s)
+        return True
+
     def stats(self) -> dict:
         q, f, b, w = C.c_uint64(), C.c_uint64(), C.c_uint64(), C.c_uint64()
         check(lib().kamsta_server_stats(self._h, C.byref(q), C.byref(f), C.byref(b), C.byref(w)))
@@ -324,6 +333,11 @@ class Context:
     @property
     def handle(self):
         return self._h
+
+    def set_memory_limit(self, nbytes: int) -> None:
+        """Cap the device bytes this context may have in use (0 = no cap);
+        a call over the cap raises E_OOM and the context stays usable."""
+        check(lib().kamsta_ctx_set_memory_limit(self._h, int(nbytes)))
 
     def close(self):
         if self._h:

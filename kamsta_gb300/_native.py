@@ -14,9 +14,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libkamsta_gpu.so")
 
 # status codes (kamsta_gpu.h)
-OK, E_INPUT, E_OOM, E_CUDA, E_NOCONVERGE, E_UNSUPPORTED, E_BUDGET, E_NOTREADY = range(8)
+(OK, E_INPUT, E_OOM, E_CUDA, E_NOCONVERGE, E_UNSUPPORTED, E_BUDGET, E_NOTREADY,
+ E_CANCELLED) = range(9)
 STATUS_NAMES = {0: "OK", 1: "E_INPUT", 2: "E_OOM", 3: "E_CUDA", 4: "E_NOCONVERGE",
-                5: "E_UNSUPPORTED", 6: "E_BUDGET", 7: "E_NOTREADY"}
+                5: "E_UNSUPPORTED", 6: "E_BUDGET", 7: "E_NOTREADY", 8: "E_CANCELLED"}
 
 FLAG_VALIDATE = 0x1
 FLAG_SORT_OUTPUT = 0x2
@@ -131,6 +132,7 @@ SIGNATURES = {
     "kamsta_ctx_destroy": (I32, [P]),
     "kamsta_ctx_trim": (I32, [P]),
     "kamsta_ctx_pool_bytes": (U64, [P]),
+    "kamsta_ctx_set_memory_limit": (I32, [P, U64]),
     "kamsta_mst_boruvka": (I32, [P, U64, U32, C.POINTER(Cfg), P, C.POINTER(U64), C.POINTER(Stats)]),
     "kamsta_mst_filter_boruvka": (I32, [P, U64, U32, C.POINTER(Cfg), P, C.POINTER(U64),
                                         C.POINTER(Stats)]),
@@ -144,6 +146,7 @@ SIGNATURES = {
     "kamsta_server_create": (I32, [C.c_int, C.POINTER(ServerCfg), C.POINTER(P)]),
     "kamsta_server_submit": (I32, [P, C.POINTER(Request), C.POINTER(U64)]),
     "kamsta_server_poll": (I32, [P, C.POINTER(Completion), U32, C.POINTER(U32), U32]),
+    "kamsta_server_cancel": (I32, [P, U64]),
     "kamsta_server_stats": (I32, [P, C.POINTER(U64), C.POINTER(U64), C.POINTER(U64),
                                   C.POINTER(U64)]),
     "kamsta_server_destroy": (I32, [P]),

@@ -97,7 +97,7 @@ kamsta_status solve_host(Algo algo, const kamsta_wedge* edges, uint64_t m, uint3
   // device copies of input and output live in the context's grow-only io pool
   const size_t in_bytes = (m * sizeof(kamsta_wedge) + 255) & ~size_t(255);
   const size_t out_bytes = std::max<uint64_t>(n, 1) * sizeof(kamsta_wedge);
-  cudaError_t e = ctx->io.reserve(in_bytes + out_bytes + 256);
+  cudaError_t e = ctx_reserve(ctx, ctx->io, in_bytes + out_bytes + 256);
   if (e != cudaSuccess) return cuda_status(e, "device buffers for host input");
   kamsta_wedge* din = ctx->io.take<kamsta_wedge>(m);
   kamsta_wedge* dout = ctx->io.take<kamsta_wedge>(std::max<uint64_t>(n, 1));
@@ -178,7 +178,7 @@ kamsta_status solve_7bit_locked(kamsta_ctx* ctx, const kamsta_cgraph& g, kamsta_
   if (stats) std::memset(stats, 0, sizeof(*stats));
   if (g.m_directed == 0 || g.n == 0) return KAMSTA_OK;
   void* buf = nullptr;
-  cudaError_t e = cudaMallocFromPoolAsync(&buf, g.m_directed * sizeof(kamsta_wedge), ctx->pool, st);
+  cudaError_t e = ctx_alloc(ctx, &buf, g.m_directed * sizeof(kamsta_wedge), st);
   if (e != cudaSuccess) return cuda_status(e, "decode buffer");
   struct Free {
     void* p;
@@ -358,6 +358,16 @@ kamsta_status kamsta_ctx_trim(kamsta_ctx* ctx) {
   return KAMSTA_OK;
 }
 
+kamsta_status kamsta_ctx_set_memory_limit(kamsta_ctx* ctx, uint64_t bytes) {
+  if (!ctx) {
+    set_error("null context");
+    return KAMSTA_E_INPUT;
+  }
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  ctx->mem_limit = bytes;
+  return KAMSTA_OK;
+}
+
 uint64_t kamsta_ctx_pool_bytes(const kamsta_ctx* ctx) {
   if (!ctx) return 0;
   uint64_t pool = 0;
@@ -503,7 +513,7 @@ kamsta_status kamsta_mst_boruvka_7bit(const kamsta_cgraph* g, const kamsta_cfg* 
   const size_t fb = (sizeof(kamsta_wedge) * g->num_chunks + 255) & ~size_t(255);
   const size_t db = (g->data_bytes + 255) & ~size_t(255);
   const size_t outb = std::max<uint64_t>(g->n, 1) * sizeof(kamsta_wedge);
-  cudaError_t e = ctx->io.reserve(ob + fb + db + outb + 1024);
+  cudaError_t e = ctx_reserve(ctx, ctx->io, ob + fb + db + outb + 1024);
   if (e != cudaSuccess) return cuda_status(e, "device buffers for compressed input");
   kamsta_cgraph dg = *g;
   uint64_t* doff = ctx->io.take<uint64_t>(g->num_chunks + 1);

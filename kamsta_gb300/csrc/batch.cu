@@ -208,7 +208,7 @@ struct PoolBuf {
   cudaError_t alloc(kamsta_ctx* ctx, size_t bytes, cudaStream_t s) {
     reset();
     st = s;
-    return cudaMallocFromPoolAsync(&p, std::max<size_t>(bytes, 256), ctx->pool, s);
+    return ctx_alloc(ctx, &p, std::max<size_t>(bytes, 256), s);
   }
 };
 

@@ -31,7 +31,7 @@ struct GenBuf {
     st = s;
     pool = ctx ? ctx->pool : nullptr;
     const size_t bytes = std::max<uint64_t>(count, 1) * sizeof(T);
-    cudaError_t e = pool ? cudaMallocFromPoolAsync(&p, bytes, pool, s) : cudaMalloc(&p, bytes);
+    cudaError_t e = ctx ? ctx_alloc(ctx, &p, bytes, s) : cudaMalloc(&p, bytes);
     *out = static_cast<T*>(p);
     return e;
   }

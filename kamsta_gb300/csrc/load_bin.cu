@@ -93,7 +93,7 @@ struct PoolMem {
   }
   cudaError_t alloc(kamsta_ctx* ctx, cudaStream_t s, size_t bytes) {
     st = s;
-    return cudaMallocFromPoolAsync(&p, std::max<size_t>(bytes, 256), ctx->pool, s);
+    return ctx_alloc(ctx, &p, std::max<size_t>(bytes, 256), s);
   }
 };
 

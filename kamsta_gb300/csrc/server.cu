@@ -284,6 +284,31 @@ kamsta_status kamsta_server_poll(kamsta_server* s, kamsta_completion* out, uint3
   return KAMSTA_OK;
 }
 
+kamsta_status kamsta_server_cancel(kamsta_server* s, uint64_t ticket) {
+  if (!s) {
+    set_error("null pointer argument");
+    return KAMSTA_E_INPUT;
+  }
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = std::find_if(s->queue.begin(), s->queue.end(),
+                         [ticket](const kamsta_server::Job& j) { return j.ticket == ticket; });
+  if (it == s->queue.end()) {
+    set_error("ticket not queued (in a wave, finished or unknown)");
+    return KAMSTA_E_NOTREADY;
+  }
+  kamsta_completion c{};
+  c.ticket = it->ticket;
+  c.user_tag = it->req.user_tag;
+  c.status = KAMSTA_E_CANCELLED;
+  c.submit_us = it->submit_us;
+  c.start_us = c.finish_us = s->now_us();
+  s->queue.erase(it);
+  s->done.push_back(c);
+  s->cv_done.notify_all();
+  s->cv_work.notify_all();  // the queue head may fit the budget now
+  return KAMSTA_OK;
+}
+
 kamsta_status kamsta_server_stats(kamsta_server* s, uint64_t* queued, uint64_t* in_flight,
                                   uint64_t* bytes_in_use, uint64_t* waves) {
   if (!s) {

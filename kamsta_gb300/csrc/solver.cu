@@ -56,6 +56,29 @@ cudaError_t Arena::reserve(size_t bytes) {
   return cudaSuccess;
 }
 
+uint64_t ctx_device_bytes(const kamsta_ctx* ctx) {
+  uint64_t used = 0;
+  if (ctx->pool) cudaMemPoolGetAttribute(ctx->pool, cudaMemPoolAttrUsedMemCurrent, &used);
+  return used + ctx->fixed.cap + ctx->io.cap;
+}
+
+cudaError_t ctx_alloc(kamsta_ctx* ctx, void** p, size_t bytes, cudaStream_t st) {
+  *p = nullptr;
+  if (ctx->mem_limit && ctx_device_bytes(ctx) + bytes > ctx->mem_limit)
+    return cudaErrorMemoryAllocation;
+  return cudaMallocFromPoolAsync(p, bytes, ctx->pool, st);
+}
+
+cudaError_t ctx_reserve(kamsta_ctx* ctx, Arena& a, size_t bytes) {
+  // growing releases the old buffer first
+  if (bytes > a.cap && ctx->mem_limit &&
+      ctx_device_bytes(ctx) - a.cap + bytes > ctx->mem_limit) {
+    a.reset();
+    return cudaErrorMemoryAllocation;
+  }
+  return a.reserve(bytes);
+}
+
 void Arena::release() {
   if (base) cudaFree(base);
   base = nullptr;
@@ -276,7 +299,7 @@ kamsta_status Solve::alloc_fixed() {
   add(2 * kMaxSeg, 4);
   add(n / 32 + 2, 4);
   add(4, 8);  // dweight
-  CU_TRY(ctx_->fixed.reserve(bytes + 4096));
+  CU_TRY(ctx_reserve(ctx_, ctx_->fixed, bytes + 4096));
   Arena& A = ctx_->fixed;
   P_ = A.take<uint32_t>(n + 1);
   D_ = A.take<uint32_t>(n + 1);
@@ -308,7 +331,7 @@ kamsta_status Solve::alloc_list(SegList* L, uint32_t nseg, uint64_t cap) {
   const size_t cnt_bytes = round_up(sizeof(uint32_t) * kMaxSeg, 256);
   const size_t bytes = cnt_bytes + static_cast<size_t>(nseg) * cap * sizeof(Rec);
   void* mem = nullptr;
-  CU_TRY(cudaMallocFromPoolAsync(&mem, bytes, ctx_->pool, st_));
+  CU_TRY(ctx_alloc(ctx_, &mem, bytes, st_));
   L->mem = mem;
   L->d_count = static_cast<uint32_t*>(mem);
   L->base = reinterpret_cast<Rec*>(static_cast<char*>(mem) + cnt_bytes);
@@ -593,7 +616,7 @@ kamsta_status Solve::dedupe(SegList* L, uint32_t nr) {
   const size_t cb = round_up(rs.counts * sizeof(uint32_t), 256);
   const size_t sb = round_up(rs.status * sizeof(uint64_t), 256);
   void* mem = nullptr;
-  CU_TRY(cudaMallocFromPoolAsync(&mem, 2 * kb + 2 * vb + cb + sb, ctx_->pool, st_));
+  CU_TRY(ctx_alloc(ctx_, &mem, 2 * kb + 2 * vb + cb + sb, st_));
   char* m = static_cast<char*>(mem);
   uint64_t* keys = reinterpret_cast<uint64_t*>(m);
   uint64_t* keys2 = reinterpret_cast<uint64_t*>(m + kb);
@@ -895,8 +918,7 @@ kamsta_status Solve::contract_rows(uint32_t wmin, uint32_t wmax, SegList* E, boo
   // outside vertices, their row starts, then the input's fence index
   const uint64_t nfence = (md_ + kFenceStep - 1) / kFenceStep;
   void* smem = nullptr;
-  CU_TRY(cudaMallocFromPoolAsync(&smem, sizeof(uint32_t) * (2 * uint64_t(cap_s) + nfence + 1),
-                                 ctx_->pool, st_));
+  CU_TRY(ctx_alloc(ctx_, &smem, sizeof(uint32_t) * (2 * uint64_t(cap_s) + nfence + 1), st_));
   struct Free {
     void* p;
     cudaStream_t s;
@@ -936,7 +958,7 @@ kamsta_status Solve::contract_rows(uint32_t wmin, uint32_t wmax, SegList* E, boo
     const size_t rb = round_up(k * sizeof(Rec), 256), kb = round_up(k * 8, 256),
                  ib = round_up(k * 4, 256), cb = round_up(rs.counts * 4, 256),
                  sb = round_up(rs.status * 8, 256);
-    CU_TRY(cudaMallocFromPoolAsync(&tmem, rb + 2 * kb + 2 * ib + cb + sb, ctx_->pool, st_));
+    CU_TRY(ctx_alloc(ctx_, &tmem, rb + 2 * kb + 2 * ib + cb + sb, st_));
     Free ft{tmem, st_};
     char* m = static_cast<char*>(tmem);
     Rec* tmp = reinterpret_cast<Rec*>(m);

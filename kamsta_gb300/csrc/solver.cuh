@@ -69,6 +69,7 @@ struct kamsta_ctx {
   kamsta::Arena io;      // host-buffer entry points: device copies of in/out
   cudaEvent_t piece_ev[kamsta::kInputPieces] = {};  // host input piece k is on the device
   cudaEvent_t ev_early = nullptr;  // the first round's forest edges are written
+  uint64_t mem_limit = 0;          // kamsta_ctx_set_memory_limit; 0 = none
   std::mutex mu;
 };
 
@@ -112,5 +113,11 @@ kamsta_status solve_device(kamsta_ctx* ctx, Algo algo, const kamsta_wedge* d_in,
 
 void set_error(const std::string& msg);
 kamsta_status cuda_status(cudaError_t e, const char* what);
+// Device memory of a context under its limit (mem_limit): stream-ordered
+// scratch from its pool and the growth of its arenas.  Going over the limit
+// fails like a device allocation (cudaErrorMemoryAllocation -> KAMSTA_E_OOM).
+uint64_t ctx_device_bytes(const kamsta_ctx* ctx);
+cudaError_t ctx_alloc(kamsta_ctx* ctx, void** p, size_t bytes, cudaStream_t st);
+cudaError_t ctx_reserve(kamsta_ctx* ctx, Arena& a, size_t bytes);
 
 }  // namespace kamsta

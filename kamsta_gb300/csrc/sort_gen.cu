@@ -169,6 +169,7 @@ __global__ void k_gnm_unpack(const uint64_t* dkeys, uint64_t md, uint32_t b, uin
 // a generator runs with a context (set by PoolScope), plain cudaMalloc
 // otherwise.
 struct GenPool {
+  kamsta_ctx* ctx = nullptr;
   cudaMemPool_t pool = nullptr;
   cudaStream_t st = nullptr;
 };
@@ -177,7 +178,7 @@ thread_local GenPool g_gen_pool;
 struct PoolScope {
   GenPool saved;
   PoolScope(kamsta_ctx* ctx, cudaStream_t st) : saved(g_gen_pool) {
-    g_gen_pool = ctx ? GenPool{ctx->pool, st} : GenPool{};
+    g_gen_pool = ctx ? GenPool{ctx, ctx->pool, st} : GenPool{};
   }
   ~PoolScope() { g_gen_pool = saved; }
 };
@@ -197,8 +198,7 @@ struct Tmp {
   cudaError_t alloc(T** out, uint64_t count) {
     reset();
     const size_t bytes = std::max<uint64_t>(count, 1) * sizeof(T);
-    cudaError_t e = gp.pool ? cudaMallocFromPoolAsync(&p, bytes, gp.pool, gp.st)
-                            : cudaMalloc(&p, bytes);
+    cudaError_t e = gp.ctx ? ctx_alloc(gp.ctx, &p, bytes, gp.st) : cudaMalloc(&p, bytes);
     *out = static_cast<T*>(p);
     return e;
   }

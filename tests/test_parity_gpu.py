@@ -138,6 +138,36 @@ def test_validation_rejects_unsorted_and_out_of_range(kamsta, oracle):
     _check(oracle, kamsta.boruvka(e, cfg, n=100), e, 100)
 
 
+def test_memory_limit_fails_cleanly(kamsta, oracle):
+    """A context over its memory limit fails with E_OOM, before any device
+    memory is taken or in the middle of a solve, and stays usable."""
+    import torch
+    n = 1 << 16
+    e = oracle.gen_gnm(n, 1 << 20, 21)
+    d = torch.from_numpy(e.view(np.uint32).reshape(-1, 3).view(np.int32)).cuda()
+    out = torch.empty((n, 3), dtype=torch.int32, device="cuda")
+    ctx = kamsta.Context(0)
+
+    def solve():
+        k = ctx.boruvka_dev(d.data_ptr(), len(e), n, out.data_ptr())
+        return out[:k].cpu().numpy().view(np.uint32).reshape(-1).view(kamsta.WEDGE)
+
+    ctx.set_memory_limit(1 << 20)  # below the vertex arrays alone
+    with pytest.raises(kamsta.KamstaError) as ei:
+        solve()
+    assert ei.value.status == kamsta._native.E_OOM
+    ctx.set_memory_limit(0)
+    _check(oracle, solve(), e, n)
+    # the vertex arrays stay reserved, so now the edge lists go over
+    ctx.set_memory_limit(1 << 20)
+    with pytest.raises(kamsta.KamstaError) as ei:
+        solve()
+    assert ei.value.status == kamsta._native.E_OOM
+    ctx.set_memory_limit(0)
+    _check(oracle, solve(), e, n)
+    ctx.close()
+
+
 def test_validation_across_input_pieces(kamsta, oracle):
     """The host entry point copies the input in 16 pieces and starts the
     first pass on each as it lands; validation must still compare every

@@ -120,3 +120,43 @@ def test_bad_job_does_not_disturb_mix(kamsta):
         k = got[i]["out_count"]
         assert np.array_equal(outs[i][:k].cpu().numpy().astype(np.uint32),
                               _plain(kamsta, ctx, d, md, n))
+
+
+def test_cancel_queued_job(kamsta):
+    import torch
+    ctx = kamsta.Context(0)
+    # a large job keeps the single worker busy while the others queue
+    nb, mb = 1 << 21, 1 << 25
+    big = torch.empty((2 * mb, 3), dtype=torch.int32, device="cuda")
+    assert ctx.gen_gnm_dev(nb, mb, 77, 254, big.data_ptr()) == 2 * mb
+    out_big = torch.zeros((nb, 3), dtype=torch.int32, device="cuda")
+    gs = _graphs(kamsta, ctx, 6, 11)
+    outs = [torch.zeros((max(n, 1), 3), dtype=torch.int32, device="cuda") for _, _, n in gs]
+    srv = kamsta.Server(0, workers=1)
+    t_big = srv.submit(big.data_ptr(), 2 * mb, nb, out_big.data_ptr(), tag=100)
+    t0 = time.time()
+    while srv.stats()["in_flight"] == 0:
+        assert time.time() - t0 < 30, "the worker did not take the large job"
+        time.sleep(0.0002)
+    tickets = [srv.submit(d.data_ptr(), md, n, outs[i].data_ptr(), tag=i)
+               for i, (d, md, n) in enumerate(gs)]
+    assert srv.cancel(tickets[2])
+    assert not srv.cancel(tickets[2])        # no longer queued
+    assert not srv.cancel(t_big)             # already in a wave
+    assert not srv.cancel(10 ** 12)          # unknown ticket
+    got = _drain(srv, len(gs) + 1)
+    srv.close()
+    assert got[2]["status"] == kamsta._native.E_CANCELLED
+    assert got[2]["batch_size"] == 0 and got[2]["out_count"] == 0
+    assert not outs[2].any()                 # its buffers were never touched
+    assert got[100]["status"] == 0
+    k = got[100]["out_count"]
+    assert np.array_equal(out_big[:k].cpu().numpy().astype(np.uint32),
+                          _plain(kamsta, ctx, big, 2 * mb, nb))
+    for i, (d, md, n) in enumerate(gs):
+        if i == 2:
+            continue
+        assert got[i]["status"] == 0
+        k = got[i]["out_count"]
+        assert np.array_equal(outs[i][:k].cpu().numpy().astype(np.uint32),
+                              _plain(kamsta, ctx, d, md, n))
