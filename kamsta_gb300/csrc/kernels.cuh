@@ -662,7 +662,18 @@ __global__ void k_hook(uint32_t n, const uint64_t* __restrict__ minval,
         if (vv >= n) continue;
         const uint32_t v = static_cast<uint32_t>(vv), u = static_cast<uint32_t>(val[k]);
         const uint64_t back = (val[k] & 0xffffffff00000000ull) | v;  // u's key if mutual
-        parent[v] = (val[k] == kInf64 || (mu[k] == back && v < u)) ? v : u;
+        const bool mutual = mu[k] == back;
+        if (val[k] == kInf64 || (mutual && v < u)) {
+          parent[v] = v;
+          continue;
+        }
+        // v hooks on u, and u on its own partner x (the low word of u's key)
+        // unless u is the root of a mutual pair, in which case x hooks on u.
+        // Either way x is in v's tree and one step nearer its root pair, so
+        // v points at x directly: a pointer-jumping step for free.  The
+        // mutual pair's upper vertex keeps its root u.
+        const uint32_t x = static_cast<uint32_t>(mu[k]);
+        parent[v] = (mutual || mu[k] == kInf64 || x == v || x >= n) ? u : x;
       }
     }
     return;
