@@ -789,6 +789,11 @@ __global__ void k_jump(uint32_t n, uint32_t* parent, uint32_t* __restrict__ root
 // reset) and hooked vertices (class 1: forest edge appended); k_vertex_write
 // sums the counts of the CTAs before it and writes, in vertex order, so ids
 // and the forest order are deterministic.
+// Root tags: bit 31 marks a root's parent entry, the low bits carry its new
+// id; kRootTagNone marks a finished root (no new id).  Needs n < 2^31.
+constexpr uint32_t kRootTag = 0x80000000u;
+constexpr uint32_t kRootTagNone = 0xffffffffu;
+
 struct VertexScanArgs {
   uint32_t n;
   uint32_t chunk;  // vertices per CTA (multiple of kBlock)
@@ -811,6 +816,10 @@ struct VertexScanArgs {
   // summed into direct_weight.  Null: msf_out receives input positions.
   uint32_t* direct_out;
   unsigned long long* direct_weight;
+  // Root tags (k_jump_label): when set (the parent array, n < 2^31), each
+  // root's entry receives kRootTag | its new id (kRootTagNone when finished)
+  // instead of newid[v], so the walks that end at it read its label.
+  uint32_t* root_tag;
 };
 
 // Vertices per thread per step of the compaction kernels: the loads of a
@@ -926,12 +935,16 @@ __global__ void __launch_bounds__(kBlock) k_vertex_write(VertexScanArgs p) {
       if (cls[j] == 0) {
         const uint32_t id = run0 + offs[j];
         if (id < p.orig_cap) {
-          p.newid[v] = id;
+          if (p.root_tag) p.root_tag[v] = kRootTag | id;
+          else p.newid[v] = id;
           p.orig_next[id] = carry[j];
           p.minval_next[id] = kInf64;
         } else {
+          if (p.root_tag) p.root_tag[v] = kRootTagNone;
           atomicOr(p.err, kErrOverflow);
         }
+      } else if (cls[j] == 0xff) {
+        if (p.root_tag && v < hi) p.root_tag[v] = kRootTagNone;  // finished root
       } else if (cls[j] == 1) {
         const uint32_t k = run1 + offs[j];
         if (k >= p.msf_cap) {
@@ -955,6 +968,78 @@ __global__ void __launch_bounds__(kBlock) k_vertex_write(VertexScanArgs p) {
   if (direct) {
     wsum = warp_sum(wsum);
     if (lane_id() == 0 && wsum) atomicAdd(p.direct_weight, static_cast<unsigned long long>(wsum));
+  }
+}
+
+// Pointer jumping and the round's label map in one walk: the roots' parent
+// entries carry kRootTag | new id (k_vertex_write ran first), so the walk
+// that reaches a root reads its label with the same load that tells it the
+// walk is over -- no gather of newid[root] afterwards.  Path halving as in
+// k_jump, writing only non-root entries (the tags are never overwritten),
+// then parent[v] = root.  label[v] = the new id of v's root, or kNone when
+// that root is finished.  Capped like k_jump.
+__global__ void k_jump_label(uint32_t n, uint32_t* parent, uint32_t* __restrict__ label,
+                             uint32_t* err) {
+  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
+  auto decode = [](uint32_t t) { return t == kRootTagNone ? kNone : (t & ~kRootTag); };
+  for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; base < n;
+       base += kIlp * stride) {
+    // kIlp walks side by side; x: current vertex (never a root while a walk
+    // runs), p: x's parent entry, root / lab: the result
+    uint32_t x[kIlp], p[kIlp], root[kIlp], lab[kIlp];
+    bool run[kIlp];
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k) {
+      const uint64_t v = base + k * stride;
+      x[k] = static_cast<uint32_t>(v);
+      p[k] = v < n ? ld_relaxed(parent + v) : kRootTagNone;
+      run[k] = !(p[k] & kRootTag);
+      root[k] = x[k];
+      lab[k] = run[k] ? kNone : decode(p[k]);
+    }
+    uint32_t steps = 0;
+    for (;;) {
+      bool any = false;
+      uint32_t gp[kIlp];
+#pragma unroll
+      for (int k = 0; k < kIlp; ++k) gp[k] = run[k] ? ld_relaxed(parent + p[k]) : 0u;
+#pragma unroll
+      for (int k = 0; k < kIlp; ++k) {
+        if (!run[k]) continue;
+        if (gp[k] & kRootTag) {  // p is the root
+          root[k] = p[k];
+          lab[k] = decode(gp[k]);
+          run[k] = false;
+          continue;
+        }
+        st_relaxed(parent + x[k], gp[k]);  // halving: x skips its parent
+        x[k] = gp[k];
+        any = true;
+      }
+      if (!any) break;
+#pragma unroll
+      for (int k = 0; k < kIlp; ++k) {
+        if (!run[k]) continue;
+        p[k] = ld_relaxed(parent + x[k]);
+        if (p[k] & kRootTag) {  // x is the root
+          root[k] = x[k];
+          lab[k] = decode(p[k]);
+          run[k] = false;
+        }
+      }
+      ++steps;
+      if ((steps & 1023u) == 0 && (steps > kJumpCap || (ld_relaxed(err) & kErrJump))) {
+        atomicOr(err, kErrJump);
+        break;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k) {
+      const uint64_t v = base + k * stride;
+      if (v >= n) continue;
+      if (root[k] != static_cast<uint32_t>(v)) st_relaxed(parent + v, root[k]);
+      label[v] = lab[k];
+    }
   }
 }
 

@@ -685,7 +685,11 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
     k_hook<<<gv, kBlock, 0, st_>>>(nr, minv, cur->base, parent_, msfoid_, direct ? 1u : 0u,
                                    ctx_->d_err);
     uint32_t* R = Rbuf_ + roff;
-    k_jump<<<gv, kBlock, 0, st_>>>(nr, parent_, R, ctx_->d_err);
+    // below 2^31 vertices the compaction runs first and tags the roots, and
+    // one walk per vertex yields its label (k_jump_label); otherwise the
+    // walk finds the roots and k_map gathers their new ids
+    const bool tagged = nr < kRootTag;
+    if (!tagged) k_jump<<<gv, kBlock, 0, st_>>>(nr, parent_, R, ctx_->d_err);
     uint32_t* onext = Obuf_ + ooff;
     VertexScanArgs va{};
     va.n = nr;
@@ -713,9 +717,11 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
       va.direct_weight = dweight_;
       va.msf_cap = n_ - 1;  // the caller's output capacity
     }
+    va.root_tag = tagged ? parent_ : nullptr;
     k_vertex_count<<<gvs, kBlock, 0, st_>>>(va);
     k_vertex_write<<<gvs, kBlock, 0, st_>>>(va);
-    k_map<<<gv, kBlock, 0, st_>>>(nr, minv, newid_, R);
+    if (tagged) k_jump_label<<<gv, kBlock, 0, st_>>>(nr, parent_, R, ctx_->d_err);
+    else k_map<<<gv, kBlock, 0, st_>>>(nr, minv, newid_, R);
     tock(KAMSTA_PHASE_ROUND_VERTS, tv);
     // relabel + self-loop removal + compaction + next-round minimum
     SegList* nxt = new_list();
@@ -726,13 +732,14 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
     const uint64_t added = ctx_->h_counters[kCVertex].cnt[1];
     // hook: minimum, record gather, partner minimum, parent + edge id;
     // jump: parent reads/writes; scan: parent, minimum, orig per vertex and
-    // id/orig/minimum per root, edge id per hooked vertex; map: 3 reads + 1 write.
+    // id/orig/minimum per root, edge id per hooked vertex; map: 3 reads + 1
+    // write, or with root tags only the label write.
     // The direct first round gathers no record and writes no edge id; it
     // reads each hooked vertex's key and writes its 12-byte forest edge.
     account(KAMSTA_PHASE_ROUND_VERTS,
-            uint64_t(nr) * ((8 + 16 + 8 + 8) + 16 + (4 + 8 + 4) + (8 + 4 + 4)) + n_next * 16 +
-                added * (direct ? 8 + 12 : 8) - (direct ? uint64_t(nr) * 20 : 0),
-            6);
+            uint64_t(nr) * ((8 + 16 + 8 + 8) + 16 + (4 + 8 + 4) + (tagged ? 4 : 8 + 4 + 4)) +
+                n_next * 16 + added * (direct ? 8 + 12 : 8) - (direct ? uint64_t(nr) * 20 : 0),
+            tagged ? 5 : 6);
     if (direct) {
       direct_count_ = added;
       if (io_ && io_->host_out && added > 0) {
