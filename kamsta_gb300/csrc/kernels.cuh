@@ -3,7 +3,8 @@
 // Reference steps (KaMSTa tree) and the kernel that replaces each:
 //   compute_min_edges             mst_utils_common.hpp:84-105     -> fused into k_pass_*
 //   determine_mst_edges(_exhausted) mst_utils_cut_edges.hpp:102-166 -> k_hook
-//   update_parents                gbbs_reimplementation.hpp:161-169 -> k_jump
+//   update_parents                gbbs_reimplementation.hpp:161-169 -> k_jump_label
+//                                    (k_jump + k_map beyond 2^31 vertices)
 //   add_new_mst_edges_to_mst_array gbbs_reimplementation.hpp:137-159 -> k_vertex_count/write
 //   compactify_vertices           mst_utils_common.hpp:122-132    -> k_vertex_count/write
 //   relabel_edges + filter_out_self_loops  mst_utils_plain.hpp:7-29,
