@@ -5,8 +5,8 @@
 //   determine_mst_edges(_exhausted) mst_utils_cut_edges.hpp:102-166 -> k_hook
 //   update_parents                gbbs_reimplementation.hpp:161-169 -> k_jump_label
 //                                    (k_jump + k_map beyond 2^31 vertices)
-//   add_new_mst_edges_to_mst_array gbbs_reimplementation.hpp:137-159 -> k_vertex_count/write
-//   compactify_vertices           mst_utils_common.hpp:122-132    -> k_vertex_count/write
+//   add_new_mst_edges_to_mst_array gbbs_reimplementation.hpp:137-159 -> k_hook (counts) + k_vertex_write
+//   compactify_vertices           mst_utils_common.hpp:122-132    -> k_hook (counts) + k_vertex_write
 //   relabel_edges + filter_out_self_loops  mst_utils_plain.hpp:7-29,
 //                                 mst_utils_common.hpp:157-175    -> k_pass_seg
 //   localMST::partition / filter  mst_utils_filter.hpp:39-126     -> k_pass_dir / k_pass_seg
@@ -634,91 +634,99 @@ constexpr int kIlp = 4;
 // msfoid receives the record's input position.
 __global__ void k_hook(uint32_t n, const uint64_t* __restrict__ minval,
                        const Rec* __restrict__ list, uint32_t* __restrict__ parent,
-                       uint32_t* __restrict__ msfoid, uint32_t partner_keys, uint32_t* err) {
-  const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
-  if (partner_keys) {
-    for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; base < n;
-         base += kIlp * stride) {
-      uint64_t val[kIlp], mu[kIlp];
-#pragma unroll
-      for (int k = 0; k < kIlp; ++k) {
-        const uint64_t v = base + k * stride;
-        val[k] = v < n ? minval[v] : kInf64;
-      }
-#pragma unroll
-      for (int k = 0; k < kIlp; ++k) {
-        mu[k] = kInf64;
-        if (val[k] == kInf64) continue;
-        const uint32_t u = static_cast<uint32_t>(val[k]);
-        if (u >= n) {
-          val[k] = kInf64;
-          atomicOr(err, kErrHook);
-          continue;
-        }
-        mu[k] = minval[u];
-      }
-#pragma unroll
-      for (int k = 0; k < kIlp; ++k) {
-        const uint64_t vv = base + k * stride;
-        if (vv >= n) continue;
-        const uint32_t v = static_cast<uint32_t>(vv), u = static_cast<uint32_t>(val[k]);
-        const uint64_t back = (val[k] & 0xffffffff00000000ull) | v;  // u's key if mutual
-        const bool mutual = mu[k] == back;
-        if (val[k] == kInf64 || (mutual && v < u)) {
-          parent[v] = v;
-          continue;
-        }
-        // v hooks on u, and u on its own partner x (the low word of u's key)
-        // unless u is the root of a mutual pair, in which case x hooks on u.
-        // Either way x is in v's tree and one step nearer its root pair, so
-        // v points at x directly: a pointer-jumping step for free.  The
-        // mutual pair's upper vertex keeps its root u.
-        const uint32_t x = static_cast<uint32_t>(mu[k]);
-        parent[v] = (mutual || mu[k] == kInf64 || x == v || x >= n) ? u : x;
-      }
-    }
-    return;
-  }
-  for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; base < n;
-       base += kIlp * stride) {
+                       uint32_t* __restrict__ msfoid, uint32_t partner_keys, uint32_t chunk,
+                       uint32_t* __restrict__ cta_counts, unsigned long long* counts,
+                       uint32_t* err) {
+  // CTA b hooks vertices [b * chunk, ...) -- the compaction's chunks -- and
+  // counts its live roots and hooked vertices for the compaction
+  const uint32_t lo = blockIdx.x * chunk;
+  const uint32_t hi = static_cast<uint32_t>(min(static_cast<uint64_t>(lo) + chunk, uint64_t(n)));
+  uint32_t c0 = 0, c1 = 0;
+  for (uint64_t base = lo + threadIdx.x; base < hi; base += kIlp * kBlock) {
     uint64_t val[kIlp], mu[kIlp];
     Rec r[kIlp];
     uint32_t u[kIlp];
+    bool live[kIlp];
 #pragma unroll
     for (int k = 0; k < kIlp; ++k) {
-      const uint64_t v = base + k * stride;
-      val[k] = v < n ? minval[v] : kInf64;
+      const uint64_t v = base + k * kBlock;
+      val[k] = v < hi ? minval[v] : kInf64;
+      live[k] = val[k] != kInf64;
     }
+    if (!partner_keys) {
 #pragma unroll
-    for (int k = 0; k < kIlp; ++k)
-      if (val[k] != kInf64) r[k] = list[static_cast<uint32_t>(val[k])];
+      for (int k = 0; k < kIlp; ++k)
+        if (val[k] != kInf64) r[k] = list[static_cast<uint32_t>(val[k])];
+    }
 #pragma unroll
     for (int k = 0; k < kIlp; ++k) {
       mu[k] = kInf64;
       u[k] = 0;
       if (val[k] == kInf64) continue;
-      const uint32_t v = static_cast<uint32_t>(base + k * stride);
-      if (r[k].a != v && r[k].b != v) {
-        val[k] = kInf64;  // reported below, hooks nowhere
-        atomicOr(err, kErrHook);
-        continue;
+      const uint32_t v = static_cast<uint32_t>(base + k * kBlock);
+      if (partner_keys) {
+        u[k] = static_cast<uint32_t>(val[k]);
+        if (u[k] >= n) {
+          val[k] = kInf64;  // reported, hooks nowhere
+          atomicOr(err, kErrHook);
+          continue;
+        }
+      } else {
+        if (r[k].a != v && r[k].b != v) {
+          val[k] = kInf64;  // reported, hooks nowhere
+          atomicOr(err, kErrHook);
+          continue;
+        }
+        u[k] = r[k].a ^ r[k].b ^ v;
       }
-      u[k] = r[k].a ^ r[k].b ^ v;
       mu[k] = minval[u[k]];
     }
 #pragma unroll
     for (int k = 0; k < kIlp; ++k) {
-      const uint64_t vv = base + k * stride;
-      if (vv >= n) continue;
-      const uint32_t v = static_cast<uint32_t>(vv);
-      if (val[k] == kInf64 || (mu[k] == val[k] && v < u[k])) {
+      if (base + k * kBlock >= hi) continue;
+      const uint32_t v = static_cast<uint32_t>(base + k * kBlock);
+      if (partner_keys) {
+        const uint64_t back = (val[k] & 0xffffffff00000000ull) | v;  // u's key if mutual
+        const bool mutual = mu[k] == back;
+        if (val[k] == kInf64 || (mutual && v < u[k])) {
+          parent[v] = v;
+          c0 += live[k] ? 1u : 0u;
+          continue;
+        }
+        // v hooks on u, and u on its own partner x (the low word of u's
+        // key) unless u is the root of a mutual pair, in which case x hooks
+        // on u.  Either way x is in v's tree and one step nearer its root
+        // pair, so v points at x directly: a pointer-jumping step for free.
+        // The mutual pair's upper vertex keeps its root u.
+        const uint32_t x = static_cast<uint32_t>(mu[k]);
+        parent[v] = (mutual || mu[k] == kInf64 || x == v || x >= n) ? u[k] : x;
+        ++c1;
+      } else if (val[k] == kInf64 || (mu[k] == val[k] && v < u[k])) {
         parent[v] = v;
         msfoid[v] = kNone;
+        c0 += live[k] ? 1u : 0u;
       } else {
         parent[v] = u[k];
         msfoid[v] = r[k].oid;
+        ++c1;
       }
     }
+  }
+  __shared__ uint32_t s_c[2];
+  if (threadIdx.x < 2) s_c[threadIdx.x] = 0;
+  __syncthreads();
+  c0 = warp_sum(c0);
+  c1 = warp_sum(c1);
+  if (lane_id() == 0) {
+    if (c0) atomicAdd(&s_c[0], c0);
+    if (c1) atomicAdd(&s_c[1], c1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    cta_counts[2 * blockIdx.x] = s_c[0];
+    cta_counts[2 * blockIdx.x + 1] = s_c[1];
+    if (s_c[0]) atomicAdd(&counts[0], static_cast<unsigned long long>(s_c[0]));
+    if (s_c[1]) atomicAdd(&counts[1], static_cast<unsigned long long>(s_c[1]));
   }
 }
 
@@ -785,11 +793,12 @@ __global__ void k_jump(uint32_t n, uint32_t* parent, uint32_t* __restrict__ root
 
 // Renumbering and forest-edge emission (compactify_vertices +
 // add_new_mst_edges_to_mst_array), without a cross-CTA scan: CTA c owns the
-// vertex chunk [c*chunk, (c+1)*chunk).  k_vertex_count counts its live roots
-// (class 0: dense new ids, original representative carried, next minimum
-// reset) and hooked vertices (class 1: forest edge appended); k_vertex_write
-// sums the counts of the CTAs before it and writes, in vertex order, so ids
-// and the forest order are deterministic.
+// vertex chunk [c*chunk, (c+1)*chunk).  k_hook, which hooks the same
+// chunks, counts each chunk's live roots (class 0: dense new ids, original
+// representative carried, next minimum reset) and hooked vertices (class 1:
+// forest edge appended); k_vertex_write sums the counts of the CTAs before
+// it and writes, in vertex order, so ids and the forest order are
+// deterministic.
 // Root tags: bit 31 marks a root's parent entry, the low bits carry its new
 // id; kRootTagNone marks a finished root (no new id).  Needs n < 2^31.
 constexpr uint32_t kRootTag = 0x80000000u;
@@ -859,38 +868,6 @@ __device__ __forceinline__ void vertex_step(const VertexScanArgs& p, uint32_t r0
   }
 }
 
-__global__ void __launch_bounds__(kBlock) k_vertex_count(VertexScanArgs p) {
-  const uint32_t lo = blockIdx.x * p.chunk;
-  const uint32_t hi = min(lo + p.chunk, p.n);
-  uint32_t c0 = 0, c1 = 0;
-  for (uint32_t r0 = lo; r0 < hi; r0 += kScanItems * kBlock) {
-    uint8_t cls[kScanItems];
-    uint64_t mv[kScanItems];
-    vertex_step(p, r0, hi, false, cls, mv);
-#pragma unroll
-    for (int j = 0; j < kScanItems; ++j) {
-      c0 += cls[j] == 0;
-      c1 += cls[j] == 1;
-    }
-  }
-  __shared__ uint32_t s_c[2];
-  if (threadIdx.x < 2) s_c[threadIdx.x] = 0;
-  __syncthreads();
-  c0 = warp_sum(c0);
-  c1 = warp_sum(c1);
-  if (lane_id() == 0) {
-    if (c0) atomicAdd(&s_c[0], c0);
-    if (c1) atomicAdd(&s_c[1], c1);
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    p.cta_counts[2 * blockIdx.x] = s_c[0];
-    p.cta_counts[2 * blockIdx.x + 1] = s_c[1];
-    if (s_c[0]) atomicAdd(&p.counts[0], static_cast<unsigned long long>(s_c[0]));
-    if (s_c[1]) atomicAdd(&p.counts[1], static_cast<unsigned long long>(s_c[1]));
-  }
-}
-
 __global__ void __launch_bounds__(kBlock) k_vertex_write(VertexScanArgs p) {
   __shared__ uint32_t s_base[2];
   __shared__ uint32_t s_rank[2 * kScanItems * (kBlock / 32)];
@@ -910,7 +887,8 @@ __global__ void __launch_bounds__(kBlock) k_vertex_write(VertexScanArgs p) {
   }
   __syncthreads();
   const uint32_t lo = blockIdx.x * p.chunk;
-  const uint32_t hi = min(lo + p.chunk, p.n);
+  const uint32_t hi =
+      static_cast<uint32_t>(min(static_cast<uint64_t>(lo) + p.chunk, uint64_t(p.n)));
   const bool direct = p.direct_out != nullptr;
   uint32_t run0 = s_base[0], run1 = s_base[1];
   uint64_t wsum = 0;
@@ -1146,7 +1124,8 @@ __device__ __forceinline__ void rep_step(const RepScanArgs& p, uint32_t r0, uint
 
 __global__ void __launch_bounds__(kBlock) k_rep_count(RepScanArgs p) {
   const uint32_t lo = blockIdx.x * p.chunk;
-  const uint32_t hi = min(lo + p.chunk, p.n);
+  const uint32_t hi =
+      static_cast<uint32_t>(min(static_cast<uint64_t>(lo) + p.chunk, uint64_t(p.n)));
   uint32_t c0 = 0;
   for (uint32_t r0 = lo; r0 < hi; r0 += kScanItems * kBlock) {
     uint8_t cls[kScanItems];
@@ -1179,7 +1158,8 @@ __global__ void __launch_bounds__(kBlock) k_rep_write(RepScanArgs p) {
   }
   __syncthreads();
   const uint32_t lo = blockIdx.x * p.chunk;
-  const uint32_t hi = min(lo + p.chunk, p.n);
+  const uint32_t hi =
+      static_cast<uint32_t>(min(static_cast<uint64_t>(lo) + p.chunk, uint64_t(p.n)));
   uint32_t run = s_base;
   for (uint32_t r0 = lo; r0 < hi; r0 += kScanItems * kBlock) {
     uint8_t cls[kScanItems];

@@ -682,15 +682,6 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
     // the first round of the first contraction: original ids, minima keyed
     // by partner (first pass), forest edges written directly
     const bool direct = direct_emit_ && r == 0;
-    k_hook<<<gv, kBlock, 0, st_>>>(nr, minv, cur->base, parent_, msfoid_, direct ? 1u : 0u,
-                                   ctx_->d_err);
-    uint32_t* R = Rbuf_ + roff;
-    // below 2^31 vertices the compaction runs first and tags the roots, and
-    // one walk per vertex yields its label (k_jump_label); otherwise the
-    // walk finds the roots and k_map gathers their new ids
-    const bool tagged = nr < kRootTag;
-    if (!tagged) k_jump<<<gv, kBlock, 0, st_>>>(nr, parent_, R, ctx_->d_err);
-    uint32_t* onext = Obuf_ + ooff;
     VertexScanArgs va{};
     va.n = nr;
     {
@@ -699,6 +690,17 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
       va.chunk = static_cast<uint32_t>(round_up(ceil_div(nr, g), kBlock));
     }
     const uint32_t gvs = std::max<uint32_t>(1, ceil_div(nr, va.chunk));
+    // the hook also counts each chunk's roots and hooked vertices
+    k_hook<<<gvs, kBlock, 0, st_>>>(nr, minv, cur->base, parent_, msfoid_, direct ? 1u : 0u,
+                                    va.chunk, cta_counts_, ctx_->d_counters[kCVertex].cnt,
+                                    ctx_->d_err);
+    uint32_t* R = Rbuf_ + roff;
+    // below 2^31 vertices the compaction runs first and tags the roots, and
+    // one walk per vertex yields its label (k_jump_label); otherwise the
+    // walk finds the roots and k_map gathers their new ids
+    const bool tagged = nr < kRootTag;
+    if (!tagged) k_jump<<<gv, kBlock, 0, st_>>>(nr, parent_, R, ctx_->d_err);
+    uint32_t* onext = Obuf_ + ooff;
     va.parent = parent_;
     va.minval = minv;
     va.msfoid = msfoid_;
@@ -718,7 +720,6 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
       va.msf_cap = n_ - 1;  // the caller's output capacity
     }
     va.root_tag = tagged ? parent_ : nullptr;
-    k_vertex_count<<<gvs, kBlock, 0, st_>>>(va);
     k_vertex_write<<<gvs, kBlock, 0, st_>>>(va);
     if (tagged) k_jump_label<<<gv, kBlock, 0, st_>>>(nr, parent_, R, ctx_->d_err);
     else k_map<<<gv, kBlock, 0, st_>>>(nr, minv, newid_, R);
@@ -739,7 +740,7 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
     account(KAMSTA_PHASE_ROUND_VERTS,
             uint64_t(nr) * ((8 + 16 + 8 + 8) + 16 + (4 + 8 + 4) + (tagged ? 4 : 8 + 4 + 4)) +
                 n_next * 16 + added * (direct ? 8 + 12 : 8) - (direct ? uint64_t(nr) * 20 : 0),
-            tagged ? 5 : 6);
+            tagged ? 4 : 5);
     if (direct) {
       direct_count_ = added;
       if (io_ && io_->host_out && added > 0) {
