@@ -11,7 +11,7 @@
 //                                 mst_utils_common.hpp:157-175    -> k_pass_seg
 //   localMST::partition / filter  mst_utils_filter.hpp:39-126     -> k_pass_dir / k_pass_seg
 //   final parent shortcut         local_mst_respecting_cut_edges.hpp:199-203
-//                                                                  -> k_compose + k_rep_* + k_relabel_all
+//                                                                  -> k_compose(_last) + k_rep_write + k_relabel_all
 #pragma once
 #include "common.cuh"
 
@@ -1089,6 +1089,49 @@ __global__ void k_compose(uint32_t n, uint32_t* __restrict__ R, const uint32_t* 
   }
 }
 
+// The last composition step (round 0, P set) over the compaction's chunks
+// (RepScanArgs::chunk): besides P[orig[x]] = x's final representative it
+// counts, per chunk, the level vertices that are their own representative
+// -- the count half of the representatives' compaction (k_rep_write).
+__global__ void k_compose_last(uint32_t n, const uint32_t* __restrict__ R,
+                               const uint32_t* __restrict__ next,
+                               const uint32_t* __restrict__ orig, uint32_t* __restrict__ P,
+                               uint32_t chunk, uint32_t* __restrict__ cta_counts,
+                               unsigned long long* counts) {
+  const uint32_t lo = blockIdx.x * chunk;
+  const uint32_t hi = static_cast<uint32_t>(min(static_cast<uint64_t>(lo) + chunk, uint64_t(n)));
+  uint32_t c0 = 0;
+  for (uint64_t base = lo + threadIdx.x; base < hi; base += kIlp * kBlock) {
+    uint32_t y[kIlp], o[kIlp];
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k) {
+      const uint64_t x = base + k * kBlock;
+      y[k] = x < hi ? R[x] : kNone;
+      o[k] = x < hi ? orig[x] : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k)
+      if (y[k] != kNone) y[k] = next[y[k]];
+#pragma unroll
+    for (int k = 0; k < kIlp; ++k) {
+      if (base + k * kBlock >= hi) continue;
+      const uint32_t f = y[k] == kNone ? o[k] : y[k];
+      P[o[k]] = f;
+      c0 += f == o[k] ? 1u : 0u;
+    }
+  }
+  __shared__ uint32_t s_c;
+  if (threadIdx.x == 0) s_c = 0;
+  __syncthreads();
+  c0 = warp_sum(c0);
+  if (lane_id() == 0 && c0) atomicAdd(&s_c, c0);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    cta_counts[blockIdx.x] = s_c;
+    if (s_c) atomicAdd(counts, static_cast<unsigned long long>(s_c));
+  }
+}
+
 struct RepScanArgs {
   uint32_t n;
   uint32_t chunk;
@@ -1120,30 +1163,6 @@ __device__ __forceinline__ void rep_step(const RepScanArgs& p, uint32_t r0, uint
   }
 #pragma unroll
   for (int j = 0; j < kScanItems; ++j) cls[j] = pv[j] == v[j] ? 0 : 0xff;
-}
-
-__global__ void __launch_bounds__(kBlock) k_rep_count(RepScanArgs p) {
-  const uint32_t lo = blockIdx.x * p.chunk;
-  const uint32_t hi =
-      static_cast<uint32_t>(min(static_cast<uint64_t>(lo) + p.chunk, uint64_t(p.n)));
-  uint32_t c0 = 0;
-  for (uint32_t r0 = lo; r0 < hi; r0 += kScanItems * kBlock) {
-    uint8_t cls[kScanItems];
-    uint32_t v[kScanItems];
-    rep_step(p, r0, hi, cls, v);
-#pragma unroll
-    for (int j = 0; j < kScanItems; ++j) c0 += cls[j] == 0;
-  }
-  __shared__ uint32_t s_c;
-  if (threadIdx.x == 0) s_c = 0;
-  __syncthreads();
-  c0 = warp_sum(c0);
-  if (lane_id() == 0 && c0) atomicAdd(&s_c, c0);
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    p.cta_counts[blockIdx.x] = s_c;
-    if (s_c) atomicAdd(&p.counts[0], static_cast<unsigned long long>(s_c));
-  }
 }
 
 __global__ void __launch_bounds__(kBlock) k_rep_write(RepScanArgs p) {

@@ -782,13 +782,6 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
   if (r == 0) return KAMSTA_OK;  // nothing contracted; labels unchanged
   if (final_contraction_) return KAMSTA_OK;  // no later pass needs the labels
   const int tf = tick();
-  uint64_t composed = 0;
-  for (int k = static_cast<int>(r) - 1; k >= 0; --k) {
-    const uint32_t* next = k + 1 == static_cast<int>(r) ? origs[r] : maps[k + 1];
-    k_compose<<<grid_for(sizes[k]), kBlock, 0, st_>>>(sizes[k], maps[k], next, origs[k],
-                                                      k == 0 ? P_ : nullptr);
-    composed += sizes[k];
-  }
   CU_TRY(cudaMemsetAsync(ctx_->d_counters + kCRep, 0, sizeof(DevCounters), st_));
   RepScanArgs ra{};
   ra.n = n0;
@@ -798,6 +791,17 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
     ra.chunk = static_cast<uint32_t>(round_up(ceil_div(n0, g), kBlock));
   }
   const uint32_t gr = std::max<uint32_t>(1, ceil_div(n0, ra.chunk));
+  uint64_t composed = 0;
+  for (int k = static_cast<int>(r) - 1; k >= 0; --k) {
+    const uint32_t* next = k + 1 == static_cast<int>(r) ? origs[r] : maps[k + 1];
+    if (k > 0)
+      k_compose<<<grid_for(sizes[k]), kBlock, 0, st_>>>(sizes[k], maps[k], next, origs[k],
+                                                        nullptr);
+    else  // also counts the representatives per chunk for k_rep_write
+      k_compose_last<<<gr, kBlock, 0, st_>>>(sizes[0], maps[0], next, origs[0], P_, ra.chunk,
+                                             cta_counts_, &ctx_->d_counters[kCRep].cnt[0]);
+    composed += sizes[k];
+  }
   ra.V = V_;
   ra.P = P_;
   ra.Vout = Vn_;
@@ -805,7 +809,6 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
   ra.cta_counts = cta_counts_;
   ra.counts = ctx_->d_counters[kCRep].cnt;
   ra.err = ctx_->d_err;
-  k_rep_count<<<gr, kBlock, 0, st_>>>(ra);
   k_rep_write<<<gr, kBlock, 0, st_>>>(ra);
   k_relabel_all<<<grid_for(n_), kBlock, 0, st_>>>(n_, P_, dense_of_, D_);
   tock(KAMSTA_PHASE_FINALIZE, tf);
@@ -814,7 +817,7 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
   // compose: map + orig read, one gather, one write per round vertex; rep
   // scan: 16 per level vertex; relabel_all: 16 per vertex
   account(KAMSTA_PHASE_FINALIZE, composed * 16 + uint64_t(n0) * 16 + uint64_t(n_) * 16,
-          static_cast<uint32_t>(r) + 3);
+          static_cast<uint32_t>(r) + 2);
   nreps_ = static_cast<uint32_t>(ctx_->h_counters[kCRep].cnt[0]);
   std::swap(V_, Vn_);
   return KAMSTA_OK;
