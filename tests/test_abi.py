@@ -133,3 +133,17 @@ int main(int argc, char**) {
                    check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
     assert out == ["1", "0", "4"]
+
+
+def test_status_codes_and_flags_match_header(kamsta):
+    """Every KAMSTA_E_* / KAMSTA_FLAG_* value in the header equals the
+    ctypes mirror's constant of the same name."""
+    from kamsta_gb300 import _native
+    src = open(HEADER).read()
+    defs = dict((k, int(v, 0)) for k, v in
+                re.findall(r"#define\s+KAMSTA_((?:E|FLAG)_[A-Z0-9_]+)\s+(0x[0-9a-fA-F]+|\d+)", src))
+    assert "E_CANCELLED" in defs and "FLAG_VALIDATE" in defs
+    for name, value in defs.items():
+        assert getattr(_native, name) == value, name
+        if name.startswith("E_"):
+            assert _native.STATUS_NAMES[value] == name
