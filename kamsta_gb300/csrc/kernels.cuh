@@ -1059,12 +1059,13 @@ __global__ void k_map(uint32_t n, const uint64_t* __restrict__ minval,
 // representative of x's final component:
 //   F_r[x] = R_r[x] == kNone ? orig_r[x] : F_{r+1}[R_r[x]],
 // with F_rounds = orig_rounds (the components left after the last round).
-// Launched for r = rounds-1 down to 0, so each map is read and gathered
-// once (sum of n_r gathers, not n_0 walks through every round).  For r = 0
-// the result goes to P at each vertex's original id instead.
+// Launched for r = rounds-1 down to 1, so each map is read and gathered
+// once (sum of n_r gathers, not n_0 walks through every round); r = 0 is
+// k_compose_last, which writes the result to P at each vertex's original
+// id instead.
 constexpr int kMaxRounds = 40;
 __global__ void k_compose(uint32_t n, uint32_t* __restrict__ R, const uint32_t* __restrict__ next,
-                          const uint32_t* __restrict__ orig, uint32_t* __restrict__ P) {
+                          const uint32_t* __restrict__ orig) {
   const uint64_t stride = static_cast<uint64_t>(gridDim.x) * blockDim.x;
   for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; base < n;
        base += kIlp * stride) {
@@ -1082,9 +1083,7 @@ __global__ void k_compose(uint32_t n, uint32_t* __restrict__ R, const uint32_t* 
     for (int k = 0; k < kIlp; ++k) {
       const uint64_t x = base + k * stride;
       if (x >= n) continue;
-      const uint32_t f = y[k] == kNone ? o[k] : y[k];
-      if (P) P[o[k]] = f;
-      else R[x] = f;
+      R[x] = y[k] == kNone ? o[k] : y[k];
     }
   }
 }

@@ -795,8 +795,7 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
   for (int k = static_cast<int>(r) - 1; k >= 0; --k) {
     const uint32_t* next = k + 1 == static_cast<int>(r) ? origs[r] : maps[k + 1];
     if (k > 0)
-      k_compose<<<grid_for(sizes[k]), kBlock, 0, st_>>>(sizes[k], maps[k], next, origs[k],
-                                                        nullptr);
+      k_compose<<<grid_for(sizes[k]), kBlock, 0, st_>>>(sizes[k], maps[k], next, origs[k]);
     else  // also counts the representatives per chunk for k_rep_write
       k_compose_last<<<gr, kBlock, 0, st_>>>(sizes[0], maps[0], next, origs[0], P_, ra.chunk,
                                              cta_counts_, &ctx_->d_counters[kCRep].cnt[0]);
