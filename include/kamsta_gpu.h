@@ -89,7 +89,14 @@ typedef struct kamsta_wedge64 {
 #define KAMSTA_FLAG_TRACE 0x10u       /* record per-round (m_r, n_r) in stats  */
 #define KAMSTA_FLAG_FILTER 0x20u      /* batch / serving: run filter_boruvka   */
 
-/* AlgorithmConfig (algorithm_configurations.hpp:27-34) plus GPU knobs. */
+/* AlgorithmConfig (algorithm_configurations.hpp:27-34) plus GPU knobs.
+ * compression = KAMSTA_SEVEN_BIT_DIFF_ENCODING: the host-buffer entry points
+ * (kamsta_mst_boruvka, kamsta_mst_filter_boruvka, kamsta_mst_boruvka_wedge64)
+ * encode the input on the host as the reference's boruvka() does
+ * (hybrid_boruvka.hpp:277-299), copy only the compressed bytes to the device
+ * and decode them there; the forest is the same as uncompressed.  Device-
+ * buffer and batch entry points already hold 12-byte entries on the device
+ * and solve them as they are. */
 typedef struct kamsta_cfg {
   int32_t local_preprocessing; /* KAMSTA_*_PREPROCESSING / _BORUVKA         */
   int32_t compression;         /* KAMSTA_*_COMPRESSION                       */
@@ -202,11 +209,14 @@ kamsta_status kamsta_mst_filter_boruvka_dev(kamsta_ctx* ctx,
  * kamsta_mst_boruvka_dev, computed by one kernel whose scratch is a fixed
  * array inside the library (about 5 MB, held by every device that loads the
  * library until exit).  Limits: n <= 32768 and m_directed <= 262144, larger
- * graphs are rejected with KAMSTA_E_INPUT.  d_edges / d_out are device
- * pointers, out_count / total_weight host pointers; the call returns after
- * the result is known.  The first call on a device looks up the array's
- * device address, so make it before any stream capture.  Calls share the
- * array: calls that overlap on the GPU race and must be serialised. */
+ * graphs are rejected with KAMSTA_E_INPUT, and so is an entry with an id
+ * >= n.  d_edges / d_out are device pointers, out_count / total_weight host
+ * pointers; the call waits for `stream` and returns once the result is
+ * known.  The first call on a device looks up the array's device address,
+ * so make that first call before any stream capture; the address is kept
+ * for the life of the device's primary context, so do not use the library
+ * across a cudaDeviceReset.  Calls share the array: calls that overlap on
+ * the GPU race and must be serialised. */
 kamsta_status kamsta_mst_boruvka_noalloc(const kamsta_wedge* d_edges, uint64_t m_directed,
                                          uint32_t n, kamsta_wedge* d_out, uint64_t* out_count,
                                          uint64_t* total_weight, kamsta_stream stream);
@@ -318,7 +328,9 @@ typedef struct kamsta_completion {
 kamsta_status kamsta_server_cfg_default(kamsta_server_cfg* cfg);
 kamsta_status kamsta_server_create(int device, const kamsta_server_cfg* cfg,
                                    kamsta_server** out);
-/* KAMSTA_E_BUDGET if the job alone exceeds the budget. */
+/* KAMSTA_E_BUDGET if the job alone exceeds one worker's share of the
+ * budget (budget_bytes / workers), which is also the hard device-memory
+ * limit of each worker's context. */
 kamsta_status kamsta_server_submit(kamsta_server* server, const kamsta_request* req,
                                    uint64_t* ticket);
 /* Up to `cap` completions; waits up to timeout_us for the first one.
@@ -333,6 +345,11 @@ kamsta_status kamsta_server_cancel(kamsta_server* server, uint64_t ticket);
 kamsta_status kamsta_server_stats(kamsta_server* server, uint64_t* queued,
                                   uint64_t* in_flight, uint64_t* bytes_in_use,
                                   uint64_t* waves);
+/* The per-worker device-memory limit (budget_bytes / workers) and the most
+ * device memory any worker's context held during a wave so far (its pool's
+ * high-water mark plus its arenas). */
+kamsta_status kamsta_server_memory(kamsta_server* server, uint64_t* worker_limit,
+                                   uint64_t* peak_worker_bytes);
 /* Finishes every queued job, then stops the workers and frees the server. */
 kamsta_status kamsta_server_destroy(kamsta_server* server);
 

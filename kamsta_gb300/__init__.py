@@ -305,6 +305,13 @@ class Server:
         return {"queued": q.value, "in_flight": f.value, "bytes_in_use": b.value,
                 "waves": w.value}
 
+    def memory(self) -> dict:
+        """Per-worker device-memory limit and the largest amount any worker's
+        context held during a wave so far."""
+        lim, peak = C.c_uint64(), C.c_uint64()
+        check(lib().kamsta_server_memory(self._h, C.byref(lim), C.byref(peak)))
+        return {"worker_limit": lim.value, "peak_worker_bytes": peak.value}
+
     def close(self):
         if self._h:
             check(lib().kamsta_server_destroy(self._h))

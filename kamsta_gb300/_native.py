@@ -149,6 +149,7 @@ SIGNATURES = {
     "kamsta_server_cancel": (I32, [P, U64]),
     "kamsta_server_stats": (I32, [P, C.POINTER(U64), C.POINTER(U64), C.POINTER(U64),
                                   C.POINTER(U64)]),
+    "kamsta_server_memory": (I32, [P, C.POINTER(U64), C.POINTER(U64)]),
     "kamsta_server_destroy": (I32, [P]),
     "kamsta_encode_7bit": (I32, [P, U64, U32, P, P, P, U64, C.POINTER(U64)]),
     "kamsta_decode_7bit_dev": (I32, [P, C.POINTER(CGraph), P, P]),

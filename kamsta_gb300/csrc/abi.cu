@@ -16,13 +16,10 @@ namespace {
 
 kamsta_status check_cfg(const kamsta_cfg* cfg) {
   if (!cfg) return KAMSTA_OK;
-  if (cfg->compression != KAMSTA_NO_COMPRESSION) {
-    set_error(cfg->compression == KAMSTA_SEVEN_BIT_DIFF_ENCODING
-                  ? "compression: SEVEN_BIT_DIFF_ENCODING input goes through "
-                    "kamsta_mst_boruvka_7bit / kamsta_mst_boruvka_7bit_dev"
-                  : "compression: unknown value");
-    return cfg->compression == KAMSTA_SEVEN_BIT_DIFF_ENCODING ? KAMSTA_E_UNSUPPORTED
-                                                               : KAMSTA_E_INPUT;
+  if (cfg->compression != KAMSTA_NO_COMPRESSION &&
+      cfg->compression != KAMSTA_SEVEN_BIT_DIFF_ENCODING) {
+    set_error("compression: unknown value");
+    return KAMSTA_E_INPUT;
   }
   if (cfg->items_per_thread != 0 && cfg->items_per_thread != 6 && cfg->items_per_thread != 8 &&
       cfg->items_per_thread != 12) {
@@ -74,6 +71,10 @@ struct DefaultCtx {
 };
 thread_local DefaultCtx g_default;
 
+kamsta_status solve_host_7bit(Algo algo, const kamsta_wedge* edges, uint64_t m, uint32_t n,
+                              kamsta_cfg c, kamsta_wedge* out, uint64_t* out_count,
+                              kamsta_stats* stats);
+
 // Host-to-device copy of a large input as pieces alternating between the
 // context's two streams (two copy engines in flight); the main stream waits
 // for both before the solve.
@@ -87,6 +88,8 @@ kamsta_status solve_host(Algo algo, const kamsta_wedge* edges, uint64_t m, uint3
   kamsta_status s = check_cfg(cfg);
   if (s != KAMSTA_OK) return s;
   kamsta_cfg c = cfg_or_default(cfg);
+  if (c.compression == KAMSTA_SEVEN_BIT_DIFF_ENCODING)
+    return solve_host_7bit(algo, edges, m, n, c, out, out_count, stats);
   kamsta_ctx* ctx = nullptr;
   s = g_default.get(&ctx);
   if (s != KAMSTA_OK) return s;
@@ -173,7 +176,7 @@ kamsta_status solve_dev(Algo algo, kamsta_ctx* ctx, const kamsta_wedge* d_edges,
 // Decode a compressed graph (device pointers) into pool scratch and solve it.
 kamsta_status solve_7bit_locked(kamsta_ctx* ctx, const kamsta_cgraph& g, kamsta_cfg c,
                                 kamsta_wedge* d_out, uint64_t* out_count, kamsta_stats* stats,
-                                cudaStream_t st) {
+                                cudaStream_t st, Algo algo = Algo::kBoruvka) {
   *out_count = 0;
   if (stats) std::memset(stats, 0, sizeof(*stats));
   if (g.m_directed == 0 || g.n == 0) return KAMSTA_OK;
@@ -198,8 +201,8 @@ kamsta_status solve_7bit_locked(kamsta_ctx* ctx, const kamsta_cgraph& g, kamsta_
   }
   c.compression = KAMSTA_NO_COMPRESSION;
   SolveOut so;
-  s = solve_device(ctx, Algo::kBoruvka, static_cast<kamsta_wedge*>(buf), g.m_directed, g.n, c,
-                   d_out, &so, stats, st);
+  s = solve_device(ctx, algo, static_cast<kamsta_wedge*>(buf), g.m_directed, g.n, c, d_out, &so,
+                   stats, st);
   *out_count = so.count;
   return s;
 }
@@ -239,6 +242,99 @@ kamsta_status batch_call(kamsta_ctx* ctx, kamsta_graph_desc* graphs, uint32_t co
   s = solve_batch(ctx, algo, graphs, count, c, budget, host_buffers, stats, st);
   if (cur != ctx->device) cudaSetDevice(cur);
   return s;
+}
+
+// A compressed graph in host memory: only the compressed bytes cross to the
+// device, where they are decoded and solved (kamsta_mst_boruvka_7bit).
+kamsta_status solve_cgraph_host(Algo algo, const kamsta_cgraph* g, kamsta_cfg c,
+                                kamsta_wedge* out, uint64_t* out_count, kamsta_stats* stats) {
+  kamsta_status s = check_cgraph(g);
+  if (s != KAMSTA_OK) return s;
+  if (!out_count || (g->n > 1 && !out)) {
+    set_error("null pointer argument");
+    return KAMSTA_E_INPUT;
+  }
+  c.compression = KAMSTA_NO_COMPRESSION;
+  s = check_cfg(&c);
+  if (s != KAMSTA_OK) return s;
+  kamsta_ctx* ctx = nullptr;
+  s = g_default.get(&ctx);
+  if (s != KAMSTA_OK) return s;
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  *out_count = 0;
+  if (g->m_directed == 0 || g->n == 0) {
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    return KAMSTA_OK;
+  }
+  // compressed bytes, chunk table and the forest in the context's io arena
+  const size_t ob = (sizeof(uint64_t) * (g->num_chunks + 1) + 255) & ~size_t(255);
+  const size_t fb = (sizeof(kamsta_wedge) * g->num_chunks + 255) & ~size_t(255);
+  const size_t db = (g->data_bytes + 255) & ~size_t(255);
+  const size_t outb = std::max<uint64_t>(g->n, 1) * sizeof(kamsta_wedge);
+  cudaError_t e = ctx_reserve(ctx, ctx->io, ob + fb + db + outb + 1024);
+  if (e != cudaSuccess) return cuda_status(e, "device buffers for compressed input");
+  kamsta_cgraph dg = *g;
+  uint64_t* doff = ctx->io.take<uint64_t>(g->num_chunks + 1);
+  kamsta_wedge* dfirst = ctx->io.take<kamsta_wedge>(g->num_chunks);
+  uint8_t* ddata = ctx->io.take<uint8_t>(std::max<uint64_t>(g->data_bytes, 1));
+  kamsta_wedge* dout = ctx->io.take<kamsta_wedge>(std::max<uint64_t>(g->n, 1));
+  cudaStream_t st = ctx->stream;
+  e = cudaMemcpyAsync(doff, g->chunk_offset, sizeof(uint64_t) * (g->num_chunks + 1),
+                      cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dfirst, g->chunk_first, sizeof(kamsta_wedge) * g->num_chunks,
+                        cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && g->data_bytes)
+    e = cudaMemcpyAsync(ddata, g->data, g->data_bytes, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_status(e, "cudaMemcpyAsync(H2D)");
+  dg.chunk_offset = doff;
+  dg.chunk_first = dfirst;
+  dg.data = ddata;
+  uint64_t cnt = 0;
+  s = solve_7bit_locked(ctx, dg, c, dout, &cnt, stats, st, algo);
+  if (s != KAMSTA_OK) return s;
+  if (cnt) {
+    e = cudaMemcpyAsync(out, dout, cnt * sizeof(kamsta_wedge), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_status(e, "cudaMemcpyAsync(D2H)");
+  }
+  *out_count = cnt;
+  return KAMSTA_OK;
+}
+
+// AlgorithmConfig::compression = SEVEN_BIT_DIFF_ENCODING on the plain
+// host-buffer entry points: as the reference's boruvka() compresses its
+// input itself (hybrid_boruvka.hpp:277-299), the input is encoded here on
+// the host cores (chunks of 4096 edges), only the compressed bytes are
+// copied to the device, and the device decodes and solves them.
+kamsta_status solve_host_7bit(Algo algo, const kamsta_wedge* edges, uint64_t m, uint32_t n,
+                              kamsta_cfg c, kamsta_wedge* out, uint64_t* out_count,
+                              kamsta_stats* stats) {
+  constexpr uint32_t kChunk = 4096;
+  kamsta_cgraph g{};
+  g.m_directed = m;
+  g.n = n;
+  g.chunk_edges = kChunk;
+  g.num_chunks = (m + kChunk - 1) / kChunk;
+  std::vector<uint64_t> off(g.num_chunks + 1);
+  std::vector<kamsta_wedge> first(std::max<uint64_t>(g.num_chunks, 1));
+  uint64_t bytes = 0;
+  kamsta_status s = encode_7bit(edges, m, kChunk, off.data(), first.data(), nullptr, 0, &bytes);
+  if (s != KAMSTA_OK) return s;
+  std::unique_ptr<uint8_t[]> data(new uint8_t[std::max<uint64_t>(bytes, 1)]);
+  s = encode_7bit(edges, m, kChunk, off.data(), first.data(), data.get(), bytes, &bytes);
+  if (s != KAMSTA_OK) return s;
+  g.data_bytes = bytes;
+  g.chunk_offset = off.data();
+  g.chunk_first = first.data();
+  g.data = data.get();
+  s = solve_cgraph_host(algo, &g, c, out, out_count, stats);
+  if (s != KAMSTA_OK) return s;
+  if (c.flags & KAMSTA_FLAG_SORT_OUTPUT)
+    std::sort(out, out + *out_count, [](const kamsta_wedge& a, const kamsta_wedge& b) {
+      return a.src != b.src ? a.src < b.src : a.dst < b.dst;
+    });
+  return KAMSTA_OK;
 }
 
 }  // namespace
@@ -489,59 +585,7 @@ kamsta_status kamsta_mst_boruvka_7bit_dev(kamsta_ctx* ctx, const kamsta_cgraph* 
 kamsta_status kamsta_mst_boruvka_7bit(const kamsta_cgraph* g, const kamsta_cfg* cfg,
                                       kamsta_wedge* out, uint64_t* out_count,
                                       kamsta_stats* stats) {
-  kamsta_status s = check_cgraph(g);
-  if (s != KAMSTA_OK) return s;
-  if (!out_count || (g->n > 1 && !out)) {
-    set_error("null pointer argument");
-    return KAMSTA_E_INPUT;
-  }
-  kamsta_cfg c = cfg_or_default(cfg);
-  c.compression = KAMSTA_NO_COMPRESSION;
-  s = check_cfg(&c);
-  if (s != KAMSTA_OK) return s;
-  kamsta_ctx* ctx = nullptr;
-  s = g_default.get(&ctx);
-  if (s != KAMSTA_OK) return s;
-  std::lock_guard<std::mutex> lock(ctx->mu);
-  *out_count = 0;
-  if (g->m_directed == 0 || g->n == 0) {
-    if (stats) std::memset(stats, 0, sizeof(*stats));
-    return KAMSTA_OK;
-  }
-  // compressed bytes, chunk table and the forest in the context's io arena
-  const size_t ob = (sizeof(uint64_t) * (g->num_chunks + 1) + 255) & ~size_t(255);
-  const size_t fb = (sizeof(kamsta_wedge) * g->num_chunks + 255) & ~size_t(255);
-  const size_t db = (g->data_bytes + 255) & ~size_t(255);
-  const size_t outb = std::max<uint64_t>(g->n, 1) * sizeof(kamsta_wedge);
-  cudaError_t e = ctx_reserve(ctx, ctx->io, ob + fb + db + outb + 1024);
-  if (e != cudaSuccess) return cuda_status(e, "device buffers for compressed input");
-  kamsta_cgraph dg = *g;
-  uint64_t* doff = ctx->io.take<uint64_t>(g->num_chunks + 1);
-  kamsta_wedge* dfirst = ctx->io.take<kamsta_wedge>(g->num_chunks);
-  uint8_t* ddata = ctx->io.take<uint8_t>(std::max<uint64_t>(g->data_bytes, 1));
-  kamsta_wedge* dout = ctx->io.take<kamsta_wedge>(std::max<uint64_t>(g->n, 1));
-  cudaStream_t st = ctx->stream;
-  e = cudaMemcpyAsync(doff, g->chunk_offset, sizeof(uint64_t) * (g->num_chunks + 1),
-                      cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(dfirst, g->chunk_first, sizeof(kamsta_wedge) * g->num_chunks,
-                        cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess && g->data_bytes)
-    e = cudaMemcpyAsync(ddata, g->data, g->data_bytes, cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return cuda_status(e, "cudaMemcpyAsync(H2D)");
-  dg.chunk_offset = doff;
-  dg.chunk_first = dfirst;
-  dg.data = ddata;
-  uint64_t cnt = 0;
-  s = solve_7bit_locked(ctx, dg, c, dout, &cnt, stats, st);
-  if (s != KAMSTA_OK) return s;
-  if (cnt) {
-    e = cudaMemcpyAsync(out, dout, cnt * sizeof(kamsta_wedge), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return cuda_status(e, "cudaMemcpyAsync(D2H)");
-  }
-  *out_count = cnt;
-  return KAMSTA_OK;
+  return solve_cgraph_host(Algo::kBoruvka, g, cfg_or_default(cfg), out, out_count, stats);
 }
 
 kamsta_status kamsta_mst_batch_dev(kamsta_ctx* ctx, kamsta_graph_desc* graphs, uint32_t count,

@@ -231,6 +231,13 @@ uint64_t batch_graph_bytes(uint64_t m_directed, uint32_t n) {
   return 48ull * m_directed + 96ull * n + 4096;
 }
 
+uint64_t serve_job_bytes(const kamsta_ctx* ctx, const kamsta_graph_desc& g) {
+  kamsta_graph_desc d = g;
+  d.edges = nullptr;
+  if (is_small_graph(ctx, d)) return small::kScratchBytes + 4096;
+  return batch_graph_bytes(g.m_directed, g.n);
+}
+
 std::vector<std::pair<uint32_t, uint32_t>> plan_waves(const kamsta_graph_desc* g, uint32_t count,
                                                       uint64_t budget) {
   std::vector<std::pair<uint32_t, uint32_t>> waves;
@@ -355,8 +362,16 @@ kamsta_status launch_small(kamsta_ctx* ctx, kamsta_graph_desc* g, const std::vec
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int threads = ctx->tune_small_threads ? static_cast<int>(ctx->tune_small_threads)
                                               : kSmallThreadsDefault;
-  const uint32_t grid = std::max<uint32_t>(
+  uint32_t grid = std::max<uint32_t>(
       1, std::min<uint32_t>(S, static_cast<uint32_t>(small_per_sm(threads) * sms)));
+  if (ctx->mem_limit) {
+    // under a memory limit, only as many scratch slots as the limit leaves
+    // room for; the work queue spreads the graphs over however many CTAs run
+    const uint64_t used = ctx_device_bytes(ctx);
+    const uint64_t room = ctx->mem_limit > used ? ctx->mem_limit - used : 0;
+    const uint64_t slots = room / (small::kScratchBytes + 4096);
+    grid = std::max<uint32_t>(1, static_cast<uint32_t>(std::min<uint64_t>(grid, slots)));
+  }
   B_TRY(scr->alloc(ctx, static_cast<size_t>(grid) * small::kScratchBytes, st));
   SmallTable t;
   t.edges = reinterpret_cast<const uint32_t* const*>(d + o_edges);

@@ -28,6 +28,11 @@ bool is_small_graph(const kamsta_ctx* ctx, const kamsta_graph_desc& g);
 // forest sort, vertex arrays); used for wave planning and serving admission.
 uint64_t batch_graph_bytes(uint64_t m_directed, uint32_t n);
 
+// Device bytes the serving loop admits a device-buffer job for: one scratch
+// slot of the persistent small-graph kernel when the graph goes there (its
+// input is read in place), batch_graph_bytes otherwise.
+uint64_t serve_job_bytes(const kamsta_ctx* ctx, const kamsta_graph_desc& g);
+
 // Consecutive runs [first, last) of graphs whose summed bytes fit `budget`
 // (a graph larger than the budget forms a wave of its own).
 std::vector<std::pair<uint32_t, uint32_t>> plan_waves(const kamsta_graph_desc* g, uint32_t count,

@@ -43,11 +43,13 @@ namespace noalloc {
 
 // The whole solve in one CTA (small_solve.cuh), forest edges in the order
 // the rounds find them; the result header sits at the start of the scratch.
+// Ids are always checked against n (one compare per entry in the pass that
+// reads them anyway), so an id >= n is reported instead of skipped.
 __global__ void __launch_bounds__(kThreads, 1)
     k_noalloc_boruvka(const uint32_t* __restrict__ in, uint32_t md, uint32_t n,
                       unsigned char* __restrict__ scratch, uint32_t* __restrict__ out) {
   small::solve<kThreads, small::Out::kFound>(in, md, n, scratch, out,
-                                             reinterpret_cast<NaResult*>(scratch), false);
+                                             reinterpret_cast<NaResult*>(scratch), true);
 }
 
 }  // namespace noalloc
@@ -61,7 +63,9 @@ kamsta_status cuda_status(cudaError_t e, const char* what);
 namespace {
 
 // Device address of g_noalloc_scratch per device, looked up once per device
-// (with that device current) on the first call made there.
+// (with that device current) on the first call made there.  The address
+// belongs to the device's primary context: after cudaDeviceReset the module
+// may load elsewhere, so the library must not be used across a reset.
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mu;
 void* g_scratch_ptr[kMaxDevices] = {};
@@ -118,6 +122,10 @@ extern "C" kamsta_status kamsta_mst_boruvka_noalloc(const kamsta_wedge* d_edges,
   e = cudaMemcpyAsync(&h, scratch, sizeof(h), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return kamsta::cuda_status(e, "kamsta_mst_boruvka_noalloc result");
+  if (h.err & kamsta::kErrRange) {
+    kamsta::set_error("kamsta_mst_boruvka_noalloc: input: vertex id >= n");
+    return KAMSTA_E_INPUT;
+  }
   if (h.err) {
     kamsta::set_error("kamsta_mst_boruvka_noalloc: device check failed (code " +
                       std::to_string(h.err) + ")");

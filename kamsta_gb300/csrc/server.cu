@@ -5,7 +5,11 @@
 // take whatever is queued, in arrival order, as long as the summed device
 // footprint of the admitted jobs stays under the memory budget, and solve
 // them as one wave (batch.cu: disjoint union -> one solve -> per-graph
-// split).  A job that arrives while a wave is on the GPU joins the next wave
+// split).  The budget is enforced, not only estimated: each worker's
+// context carries a memory limit of budget / workers (every pool
+// allocation and arena growth is checked against it), a wave is admitted
+// only within that share, and the peak each worker's context held is
+// recorded per wave (kamsta_server_memory).  A job that arrives while a wave is on the GPU joins the next wave
 // of the first worker that frees up, so with two or more workers waves
 // overlap on the device.  Completions carry submit / start / finish times
 // (steady clock) for latency accounting.
@@ -45,6 +49,8 @@ struct kamsta_server {
   uint64_t bytes_in_use = 0;
   uint64_t in_flight = 0;
   uint64_t waves = 0;
+  uint64_t worker_limit = 0;  // budget / workers: each worker context's memory limit
+  uint64_t peak_worker_bytes = 0;
   bool stop = false;
   std::vector<std::thread> workers;
   std::vector<kamsta_ctx*> ctxs;
@@ -60,6 +66,17 @@ namespace kamsta {
 namespace {
 constexpr uint64_t kServerDefaultBudget = 64ull << 30;
 constexpr uint32_t kServerDefaultMaxBatch = 4096;
+
+// The most device memory the context held during the last wave (pool
+// high-water mark plus its arenas); resets the pool's high-water mark.
+uint64_t wave_peak_bytes(kamsta_ctx* ctx) {
+  uint64_t high = 0, zero = 0;
+  if (ctx->pool) {
+    cudaMemPoolGetAttribute(ctx->pool, cudaMemPoolAttrUsedMemHigh, &high);
+    cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrUsedMemHigh, &zero);
+  }
+  return high + ctx->fixed.cap + ctx->io.cap;
+}
 }  // namespace
 }  // namespace kamsta
 
@@ -73,6 +90,7 @@ void kamsta_server::worker(int w) {
   for (;;) {
     batch.clear();
     uint64_t bytes = 0;
+    bool more = false;
     {
       std::unique_lock<std::mutex> lk(mu);
       cv_work.wait(lk, [&] {
@@ -81,9 +99,11 @@ void kamsta_server::worker(int w) {
         return !queue.empty() && bytes_in_use + queue.front().bytes <= cfg.budget_bytes;
       });
       if (queue.empty()) return;  // stop requested and drained
-      // take jobs in arrival order while they fit
+      // take jobs in arrival order while they fit the free budget and this
+      // worker's share of it (the head always fits the share: submit checks)
       while (!queue.empty() && batch.size() < cfg.max_batch &&
-             bytes_in_use + bytes + queue.front().bytes <= cfg.budget_bytes) {
+             bytes_in_use + bytes + queue.front().bytes <= cfg.budget_bytes &&
+             bytes + queue.front().bytes <= worker_limit) {
         bytes += queue.front().bytes;
         batch.push_back(queue.front());
         queue.pop_front();
@@ -91,8 +111,9 @@ void kamsta_server::worker(int w) {
       bytes_in_use += bytes;
       in_flight += batch.size();
       ++waves;
+      more = !queue.empty();
     }
-    if (!queue.empty()) cv_work.notify_one();  // more work for another worker
+    if (more) cv_work.notify_one();  // more work for another worker
     // small jobs first (one persistent launch, finished in well under a
     // millisecond), then the rest as one union solve; each group completes
     // as soon as it is done
@@ -128,13 +149,28 @@ void kamsta_server::worker(int w) {
       }
       BatchWaveStats ws;
       kamsta_status s;
+      uint64_t peak = 0;
       {
         std::lock_guard<std::mutex> clk(ctx->mu);
         s = solve_wave(ctx, algo, descs.data(), static_cast<uint32_t>(descs.size()), scfg, false,
                        ctx->stream, &ws);
+        peak = wave_peak_bytes(ctx);
+      }
+      if (s == KAMSTA_E_OOM && z - a > 1) {
+        // the estimate was short for this mix: give the cached arenas back
+        // and solve the jobs one at a time under the same limit
+        kamsta_ctx_trim(ctx);
+        s = KAMSTA_OK;
+        for (auto& d : descs) {
+          std::lock_guard<std::mutex> clk(ctx->mu);
+          const kamsta_status s1 = solve_wave(ctx, algo, &d, 1, scfg, false, ctx->stream, &ws);
+          if (s1 != KAMSTA_OK) d.status = s1;
+          peak = std::max(peak, wave_peak_bytes(ctx));
+        }
       }
       const double finish = now_us();
       std::lock_guard<std::mutex> lk(mu);
+      peak_worker_bytes = std::max(peak_worker_bytes, peak);
       for (size_t i = a; i < z; ++i) {
         const kamsta_graph_desc& d = descs[i - a];
         kamsta_completion c{};
@@ -192,13 +228,15 @@ kamsta_status kamsta_server_create(int device, const kamsta_server_cfg* cfg,
     set_error("server: at most 8 workers");
     return KAMSTA_E_INPUT;
   }
-  if (c.solver.compression != KAMSTA_NO_COMPRESSION) {
-    set_error("compression: only NO_COMPRESSION is implemented");
-    return KAMSTA_E_UNSUPPORTED;
+  if (c.solver.compression != KAMSTA_NO_COMPRESSION &&
+      c.solver.compression != KAMSTA_SEVEN_BIT_DIFF_ENCODING) {
+    set_error("compression: unknown value");
+    return KAMSTA_E_INPUT;
   }
   auto* s = new kamsta_server();
   s->device = device;
   s->cfg = c;
+  s->worker_limit = c.budget_bytes / c.workers;
   s->scfg = c.solver;
   s->scfg.flags &= ~KAMSTA_FLAG_SORT_OUTPUT;
   s->t0 = std::chrono::steady_clock::now();
@@ -210,9 +248,11 @@ kamsta_status kamsta_server_create(int device, const kamsta_server_cfg* cfg,
       delete s;
       return st;
     }
-    // cached pool memory above the worker's share of the budget goes back
-    // to the device at the wave's synchronisation points
+    // the worker's share of the budget is a hard limit on what its context
+    // holds; cached pool memory above it goes back to the device at the
+    // wave's synchronisation points
     uint64_t keep = c.budget_bytes / c.workers;
+    kamsta_ctx_set_memory_limit(ctx, keep);
     cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep);
     kamsta_tuning tune{};
     tune.small_threads = c.small_threads;
@@ -241,9 +281,13 @@ kamsta_status kamsta_server_submit(kamsta_server* s, const kamsta_request* req,
     set_error("server: n too large");
     return KAMSTA_E_INPUT;
   }
-  const uint64_t bytes = batch_graph_bytes(req->m_directed, req->n);
-  if (bytes > s->cfg.budget_bytes) {
-    set_error("server: request needs more device memory than the whole budget");
+  kamsta_graph_desc g{};
+  g.m_directed = req->m_directed;
+  g.n = req->n;
+  const uint64_t bytes = serve_job_bytes(s->ctxs[0], g);
+  if (bytes > s->worker_limit) {
+    set_error("server: request needs more device memory than one worker's share of the "
+              "budget (budget_bytes / workers)");
     return KAMSTA_E_BUDGET;
   }
   {
@@ -320,6 +364,18 @@ kamsta_status kamsta_server_stats(kamsta_server* s, uint64_t* queued, uint64_t* 
   if (in_flight) *in_flight = s->in_flight;
   if (bytes_in_use) *bytes_in_use = s->bytes_in_use;
   if (waves) *waves = s->waves;
+  return KAMSTA_OK;
+}
+
+kamsta_status kamsta_server_memory(kamsta_server* s, uint64_t* worker_limit,
+                                   uint64_t* peak_worker_bytes) {
+  if (!s) {
+    set_error("null pointer argument");
+    return KAMSTA_E_INPUT;
+  }
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (worker_limit) *worker_limit = s->worker_limit;
+  if (peak_worker_bytes) *peak_worker_bytes = s->peak_worker_bytes;
   return KAMSTA_OK;
 }
 

@@ -104,6 +104,14 @@ __device__ void solve(const uint32_t* __restrict__ in, uint32_t md, uint32_t n,
   __shared__ uint32_t s_err;
   __shared__ unsigned long long s_weight;
   const uint32_t tid = threadIdx.x;
+  // Error bits this thread raised.  Every break decision is taken with
+  // __syncthreads_or over these, so all threads leave the rounds together;
+  // s_err only collects the codes for the result.
+  uint32_t terr = 0;
+  auto flag_err = [&](uint32_t code) {
+    terr |= code;
+    atomicOr(&s_err, code);
+  };
   if (tid == 0) {
     s_err = 0;
     s_weight = 0;
@@ -121,10 +129,10 @@ __device__ void solve(const uint32_t* __restrict__ in, uint32_t md, uint32_t n,
       d = in[3ull * i + 1];
       w = in[3ull * i + 2];
       keep = s < d && d < n;
-      if (check_ids && (s >= n || d >= n)) atomicOr(&s_err, kErrRange);
+      if (check_ids && (s >= n || d >= n)) flag_err(kErrRange);
       if (check_order && i > 0) {
         const uint32_t ps = in[3ull * (i - 1)], pd = in[3ull * (i - 1) + 1];
-        if (s < ps || (s == ps && d <= pd)) atomicOr(&s_err, kErrOrder);
+        if (s < ps || (s == ps && d <= pd)) flag_err(kErrOrder);
       }
     }
     uint32_t r0, r1, t0, t1;
@@ -142,16 +150,16 @@ __device__ void solve(const uint32_t* __restrict__ in, uint32_t md, uint32_t n,
         atomicMin(reinterpret_cast<unsigned long long*>(&mv[0][s]), key);
         atomicMin(reinterpret_cast<unsigned long long*>(&mv[0][d]), key);
       } else {
-        atomicOr(&s_err, kErrOverflow);
+        flag_err(kErrOverflow);
       }
     }
     m += t0;
   }
-  __syncthreads();
   uint32_t nr = n, cur = 0, msf_count = 0, round = 0;
   while (m > 0) {
-    if (s_err & ~kErrRange) break;
-    if (round >= kMaxRounds) {
+    if (__syncthreads_or((terr & ~kErrRange) != 0)) break;
+    if (round >= kMaxRounds) {  // round is the same in every thread
+      terr |= kErrChase;
       if (tid == 0) s_err |= kErrChase;
       break;
     }
@@ -166,7 +174,7 @@ __device__ void solve(const uint32_t* __restrict__ in, uint32_t md, uint32_t n,
       if (val != kInf64) {
         const Rec x = Lc[static_cast<uint32_t>(val)];
         if (x.a != v && x.b != v) {
-          atomicOr(&s_err, kErrHook);
+          flag_err(kErrHook);
         } else {
           const uint32_t u = x.a ^ x.b ^ v;
           if (!(mc[u] == val && v < u)) {
@@ -191,7 +199,7 @@ __device__ void solve(const uint32_t* __restrict__ in, uint32_t md, uint32_t n,
         x = gp;
         p = ld_relaxed(parent + x);
         if (++steps > 2 * kMaxN) {
-          atomicOr(&s_err, kErrJump);
+          flag_err(kErrJump);
           break;
         }
       }
@@ -207,8 +215,7 @@ __device__ void solve(const uint32_t* __restrict__ in, uint32_t md, uint32_t n,
       }
       st_relaxed(parent + v, p);
     }
-    __syncthreads();
-    if (s_err & ~kErrRange) break;
+    if (__syncthreads_or((terr & ~kErrRange) != 0)) break;
     // renumber live roots, append the forest edges of hooked vertices
     uint32_t n_next = 0;
     for (uint32_t vb = 0; vb < nr; vb += THREADS) {
@@ -229,7 +236,7 @@ __device__ void solve(const uint32_t* __restrict__ in, uint32_t md, uint32_t n,
         if (msf_count + r1 < kMaxN)
           msf[msf_count + r1] = msfoid[v];
         else
-          atomicOr(&s_err, kErrOverflow);
+          flag_err(kErrOverflow);
       }
       n_next += t0;
       msf_count += t1;
@@ -273,10 +280,9 @@ __device__ void solve(const uint32_t* __restrict__ in, uint32_t md, uint32_t n,
     cur ^= 1;
     ++round;
   }
-  __syncthreads();
   // forest output: the src<dst input copy of every forest edge
   unsigned long long local = 0;
-  const bool ok = (s_err & ~kErrRange) == 0;
+  const bool ok = !__syncthreads_or((terr & ~kErrRange) != 0);
   if (OUT == Out::kFound) {
     if (ok) {
       for (uint32_t k = tid; k < msf_count; k += THREADS) {

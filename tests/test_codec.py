@@ -127,3 +127,30 @@ def test_malformed_compressed_input_is_rejected(kamsta, oracle):
     assert ei.value.status == kamsta._native.E_INPUT
     # the context stays usable
     ctx.decode_7bit_dev(kamsta.Compressed(e, 1000, 256), d.data_ptr())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("algo", ["boruvka", "filter_boruvka"])
+def test_compression_config_on_plain_entry_points(kamsta, oracle, algo):
+    """AlgorithmConfig.compression = SEVEN_BIT_DIFF_ENCODING on the plain
+    entry points: the library encodes the input itself (as the reference's
+    boruvka() does, hybrid_boruvka.hpp:277-299) and returns the identical
+    forest as with NO_COMPRESSION, through the host and the device calls."""
+    import torch
+    from tests.test_parity_gpu import _check
+    fn = getattr(kamsta, algo)
+    ctx = kamsta.Context(0)
+    for name, e, n in _graphs(oracle):
+        outs = []
+        for comp in (kamsta.Compression.NO_COMPRESSION,
+                     kamsta.Compression.SEVEN_BIT_DIFF_ENCODING):
+            cfg = kamsta.AlgorithmConfig(local_preprocessing=1, compression=comp)
+            got = fn(e, cfg, n=n)
+            _check(oracle, got, e, n)
+            outs.append(np.sort(oracle.canon_keys(got)))
+            d = torch.from_numpy(e.view(np.uint32).reshape(-1, 3).view(np.int32)).cuda()
+            o = torch.empty((max(n, 1), 3), dtype=torch.int32, device="cuda")
+            k = getattr(ctx, algo + "_dev")(d.data_ptr(), len(e), n, o.data_ptr(), config=cfg)
+            got2 = o[:k].cpu().numpy().view(np.uint32).reshape(-1).view(kamsta.WEDGE)
+            _check(oracle, got2, e, n)
+        assert np.array_equal(outs[0], outs[1]), name

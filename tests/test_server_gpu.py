@@ -66,13 +66,17 @@ def test_same_result_alone_and_in_mix(kamsta):
         alone[i] = c[i]
     srv.close()
     # in the mix: all at once, 3 workers, a budget that forces several waves
-    srv = kamsta.Server(0, budget_bytes=64 << 20, workers=3)
+    srv = kamsta.Server(0, budget_bytes=3 * (48 << 20), workers=3)
     for i, (d, md, n) in enumerate(gs):
         srv.submit(d.data_ptr(), md, n, outs_mix[i].data_ptr(), tag=i)
     mix = _drain(srv, len(gs))
     waves = srv.stats()["waves"]
+    mem = srv.memory()
     srv.close()
     assert waves > 1
+    # the budget is enforced: no worker's context went over its share
+    assert mem["worker_limit"] == 48 << 20
+    assert 0 < mem["peak_worker_bytes"] <= mem["worker_limit"]
     assert max(c["batch_size"] for c in mix.values()) > 1
     for i, (d, md, n) in enumerate(gs):
         assert alone[i]["status"] == 0 and mix[i]["status"] == 0
@@ -160,3 +164,55 @@ def test_cancel_queued_job(kamsta):
         k = got[i]["out_count"]
         assert np.array_equal(outs[i][:k].cpu().numpy().astype(np.uint32),
                               _plain(kamsta, ctx, d, md, n))
+
+
+def test_job_submitted_mid_wave_overlaps_and_finishes_first(kamsta):
+    """Continuous batching: while worker 0 solves a large job, a small job
+    submitted after that wave started is taken by the other worker, its
+    [start, finish] interval overlaps the large job's, and it finishes
+    first; both forests equal the plain solver's."""
+    import torch
+    ctx = kamsta.Context(0)
+    nb, mb = 1 << 24, 1 << 28                 # about 25 ms of device work
+    big = torch.empty((2 * mb, 3), dtype=torch.int32, device="cuda")
+    assert ctx.gen_gnm_dev(nb, mb, 78, 254, big.data_ptr()) == 2 * mb
+    out_big = torch.zeros((nb, 3), dtype=torch.int32, device="cuda")
+    (d, md, n), = _graphs(kamsta, ctx, 1, 12)
+    out = torch.zeros((max(n, 1), 3), dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    srv = kamsta.Server(0, budget_bytes=2 * (40 << 30), workers=2)
+    srv.submit(big.data_ptr(), 2 * mb, nb, out_big.data_ptr(), tag=1)
+    t0 = time.time()
+    while srv.stats()["in_flight"] == 0:
+        assert time.time() - t0 < 30, "no worker took the large job"
+        time.sleep(0.0001)
+    srv.submit(d.data_ptr(), md, n, out.data_ptr(), tag=2)
+    got = _drain(srv, 2)
+    mem = srv.memory()
+    srv.close()
+    a, b = got[1], got[2]
+    assert a["status"] == 0 and b["status"] == 0
+    assert a["batch_size"] == 1 and b["batch_size"] == 1    # two separate waves
+    assert b["submit_us"] > a["start_us"]                  # submitted mid-wave
+    assert b["start_us"] < a["finish_us"]                  # the intervals overlap
+    assert b["finish_us"] < a["finish_us"]                 # and it finished first
+    assert mem["peak_worker_bytes"] <= mem["worker_limit"]
+    k = b["out_count"]
+    assert np.array_equal(out[:k].cpu().numpy().astype(np.uint32), _plain(kamsta, ctx, d, md, n))
+    k = a["out_count"]
+    assert np.array_equal(out_big[:k].cpu().numpy().astype(np.uint32),
+                          _plain(kamsta, ctx, big, 2 * mb, nb))
+
+
+def test_worker_share_is_the_job_limit(kamsta):
+    """A job that fits the whole budget but not one worker's share is refused
+    (each worker's context is limited to budget / workers)."""
+    import torch
+    ctx = kamsta.Context(0)
+    (d, md, n), = _graphs(kamsta, ctx, 1, 13)
+    out = torch.zeros((max(n, 1), 3), dtype=torch.int32, device="cuda")
+    srv = kamsta.Server(0, budget_bytes=8 << 20, workers=4)    # 2 MiB per worker
+    with pytest.raises(kamsta.KamstaError) as ei:
+        srv.submit(d.data_ptr(), md, n, out.data_ptr())
+    assert ei.value.status == kamsta._native.E_BUDGET
+    srv.close()
