@@ -10,9 +10,10 @@ input already in HBM, `e2e` = the same through the host-buffer C ABI call
 (pinned host input, H2D + solve + D2H of the forest inside the timed region).
 The input (24 GiB) is far larger than L2, so no flush is needed between steps.
 
---impl reference times the CPU restatement of the reference's own local
-filter-Boruvka (oracle/, OpenMP, all host cores) on a bounded sample of the
-same workload family.
+--impl reference times the reference's own single-rank local filter-Boruvka,
+compiled from its sources into oracle/_ref (OpenMP, all host cores), on the
+same workload when host RAM allows (about 80 bytes per directed entry), else
+on a bounded sample with the RAM figure stated.
 """
 from __future__ import annotations
 
@@ -150,56 +151,134 @@ def load_traffic(kernel: str):
         return None, None
 
 
-def cpu_port_baseline(n: int, m: int, seed: int, runs: int, warmup: int = 1):
-    """Time the oracle port (restated reference local filter-Boruvka)."""
+# Peak host memory of the reference build per directed input entry: 73 B
+# measured at 2^29 entries (the input's std::vector<WEdge>, the WEdge_4_1
+# container, the 16-byte WEdgeId copy, the local edges and the caller's
+# 12-byte array), plus a margin.
+REF_BYTES_PER_ENTRY = 80
+
+
+def host_info():
+    """CPU model, core counts and RAM of this host (context of every CPU figure)."""
+    info = {"cpu_model": None, "logical_cpus": os.cpu_count(), "physical_cores": None,
+            "ram_gb": None, "ram_available_gb": None}
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=20).stdout
+        kv = {}
+        for ln in out.splitlines():
+            if ":" in ln:
+                k, v = ln.split(":", 1)
+                kv[k.strip()] = v.strip()
+        info["cpu_model"] = kv.get("Model name")
+        tpc = int(kv.get("Thread(s) per core", "1") or 1)
+        info["physical_cores"] = (os.cpu_count() or 0) // max(tpc, 1)
+    except Exception:
+        pass
+    try:
+        mem = {}
+        with open("/proc/meminfo") as f:
+            for ln in f:
+                k, v = ln.split(":", 1)
+                mem[k] = int(v.split()[0])
+        info["ram_gb"] = round(mem["MemTotal"] / 1e6, 1)
+        info["ram_available_gb"] = round(mem["MemAvailable"] / 1e6, 1)
+    except Exception:
+        pass
+    return info
+
+
+def reference_runs(edges, n, runs: int, warmup: int):
+    """Times the reference's own single-rank path (oracle/_ref) on one input:
+    per run the seconds of its timed part (the reference benchmark's
+    "mst_complete" boundary, benchmarks/mst.cpp:210-229) plus the Kruskal
+    finish of the edges left at its two cut vertices."""
     from tests import _oracle as O
-    edges = O.gen_gnm(n, m, seed)
-    threads = O.lib().oracle_max_threads()
-    times = []
-    res = None
+    sess = O.RefSession(edges, n)
+    times, last = [], None
+    try:
+        for i in range(warmup + runs):
+            f, w, inf = sess.run()
+            if i >= warmup:
+                times.append(inf["reference_s"] + inf["finish_s"])
+            last = (len(f), w, inf)
+    finally:
+        sess.close()
+    return times, last
+
+
+def port_runs(edges, n, runs: int, warmup: int = 0):
+    """Times the oracle's restatement (oracle.cpp port::filter_rec)."""
+    from tests import _oracle as O
+    times, res = [], None
     for i in range(warmup + runs):
         t0 = time.perf_counter()
         res = O.boruvka_filter(edges, n, 0)
-        dt = time.perf_counter() - t0
         if i >= warmup:
-            times.append(dt)
-    return edges, res, times, threads
+            times.append(time.perf_counter() - t0)
+    return times, res
+
+
+def workload_name(log_n: int, log_m: int) -> str:
+    return f"GNM n=2^{log_n} m=2^{log_m} (2^{log_m + 1} directed 12-byte entries), single graph"
 
 
 def run_reference(args, rep):
-    """--impl reference: rank 0 times the CPU restatement; others exit."""
+    """--impl reference: rank 0 times KaMSTa's own single-rank local
+    filter-Boruvka, compiled from its sources (oracle/_ref), on all host cores
+    and on the same workload as the GPU arm when host RAM allows; the other
+    ranks exit."""
     if rep.rank != 0:
         return 0
-    n, m = 1 << args.sample_log_n, 1 << args.sample_log_m
     from tests import _oracle as O
+    host = host_info()
+    need_gb = REF_BYTES_PER_ENTRY * (2 << args.log_m) / 1e9
+    avail = host.get("ram_available_gb") or 0.0
+    full = avail >= need_gb
+    L, M = (args.log_n, args.log_m) if full else (args.sample_log_n, args.sample_log_m)
+    n, m = 1 << L, 1 << M
+    kind = "reference" if O.ref_available() else "port"
+    t0 = time.perf_counter()
     edges = O.gen_gnm(n, m, args.seed)
-    threads = O.lib().oracle_max_threads()
-    times = []
-    for i in range(args.warmup + args.steps):
-        t0 = time.perf_counter()
-        O.boruvka_filter(edges, n, 0)
-        dt = time.perf_counter() - t0
-        if i >= args.warmup:
-            times.append(dt)
-    per = statistics.median(times)
-    value = 2 * m / per
-    sample = (f"GNM n=2^{args.sample_log_n} m=2^{args.sample_log_m} seed={args.seed} "
-              f"(1/{(1 << (args.log_m - args.sample_log_m))} of the n=2^{args.log_n} m=2^{args.log_m} "
-              f"workload), median of {args.steps} runs")
+    gen_s = time.perf_counter() - t0
+    detail = {"generation_s": round(gen_s, 2)}
+    if kind == "reference":
+        threads = O.ref_lib().ref_max_threads()
+        times, (cnt, weight, inf) = reference_runs(edges, n, args.steps, args.warmup)
+        detail.update({"local_forest_edges": inf["local_forest_edges"],
+                       "edges_left_to_distributed_rounds": inf["finish_edges"],
+                       "finish_s_last": round(inf["finish_s"], 4)})
+        pt, pres = port_runs(edges, n, 1)
+        assert pres[1] == weight, "reference build and port disagree on the MSF weight"
+        detail["port_s"] = round(pt[0], 4)
+    else:
+        threads = O.lib().oracle_max_threads()
+        times, pres = port_runs(edges, n, args.steps, args.warmup)
+        cnt, weight = len(pres[0]), pres[1]
+    total = sum(times)
+    value = 2 * m * args.steps / total
+    wl = workload_name(L, M) + ("" if full else " (bounded sample)")
+    algo = ("KaMSTa's own single-rank local filter-Boruvka (execute_contraction -> "
+            "boruvka_filter, local_contraction.hpp:114-150) compiled from its sources with "
+            "single-rank MPI / parlay / IPS4o shims; the edges it leaves at its two cut "
+            "vertices finished by Kruskal" if kind == "reference" else
+            "the oracle's restatement of the reference's local filter-Boruvka")
+    sample = (f"{wl}, seed={args.seed}, {args.steps} runs after {args.warmup} warm-up runs, "
+              f"{total / args.steps:.3f} s each")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic (seeded G(n,m), uniform weights [1,254])",
-        "config": {"workload": f"GNM n=2^{args.sample_log_n} m=2^{args.sample_log_m} (bounded sample)",
-                   "algorithm": "restated reference local filter-Boruvka (boruvka_filter), OpenMP",
-                   "threads": threads},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+        "config": {"workload": wl, "algorithm": algo, "threads": threads, "host": host},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": ("the reference cannot be compiled here (MPI, TBB and all git submodules absent); "
-                 "this arm is the oracle's line-by-line restatement of its local filter-Boruvka"),
+        "forest_edges": cnt, "forest_weight": weight, "reference_detail": detail,
+        "step_s": [round(t, 4) for t in times],
     }
+    if not full:
+        line["note"] = (f"large config infeasible on this host: {avail} GB of RAM available, "
+                        f"about {need_gb:.0f} GB needed")
     print(json.dumps(line), flush=True)
     return 0
 
@@ -580,8 +659,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic (seeded G(n,m) generated on device, uniform weights [1,254])",
-        "config": {"workload": f"GNM n=2^{args.log_n} m=2^{args.log_m} (2^{args.log_m + 1} directed "
-                               "12-byte entries), single graph",
+        "config": {"workload": workload_name(args.log_n, args.log_m),
                    "algorithm": "boruvka (hybridBoruvka), local_preprocessing="
                                 f"{args.local_preprocessing} (reference benchmark default 1)",
                    "l2": "input (24 GiB) >> L2 (129 MB); no flush needed",
@@ -671,10 +749,20 @@ def main():
                        "api": "kamsta_mst_boruvka (host buffers, pinned input and output)"}
         del h_edges, h_out
 
-    # ---- CPU baseline (rank 0, N=1 only): restated reference on a sample
+    # ---- CPU baseline (rank 0, N=1 only): the reference's own code on a
+    # bounded sample of the workload, the oracle's restatement beside it
     if not args.no_cpu_baseline and rep.rank == 0 and args.gpus == 1:
+        from tests import _oracle as O
         sn, sm = 1 << args.sample_log_n, 1 << args.sample_log_m
-        edges_s, res, times, threads = cpu_port_baseline(sn, sm, args.seed, args.cpu_runs)
+        edges_s = O.gen_gnm(sn, sm, args.seed)
+        ptimes, pres = port_runs(edges_s, sn, args.cpu_runs, 1)
+        kind = "reference" if O.ref_available() else "port"
+        if kind == "reference":
+            times, (rcnt, rweight, _) = reference_runs(edges_s, sn, args.cpu_runs, 1)
+            threads = O.ref_lib().ref_max_threads()
+            assert (rcnt, rweight) == (len(pres[0]), pres[1]), "reference build / port mismatch"
+        else:
+            times, threads = ptimes, O.lib().oracle_max_threads()
         per = statistics.median(times)
         # the GPU on the same sample, for the record
         d_s = torch.from_numpy(edges_s.view(np.uint32).reshape(-1, 3).view(np.int32)).cuda()
@@ -682,12 +770,15 @@ def main():
         ks = ctx.boruvka_dev(d_s.data_ptr(), 2 * sm, sn, d_o.data_ptr(), cfg, stream=sh)
         sts = {}
         ks = ctx.boruvka_dev(d_s.data_ptr(), 2 * sm, sn, d_o.data_ptr(), cfg, stream=sh, stats=sts)
-        assert ks == len(res[0]) and sts["total_weight"] == res[1], "GPU/CPU forest mismatch"
+        assert ks == len(pres[0]) and sts["total_weight"] == pres[1], "GPU/CPU forest mismatch"
         line["cpu_baseline"] = {
-            "value": 2 * sm / per, "unit": UNIT, "cores": threads, "kind": "port",
+            "value": 2 * sm / per, "unit": UNIT, "cores": threads, "kind": kind,
             "sample": f"GNM n=2^{args.sample_log_n} m=2^{args.sample_log_m} seed={args.seed}, "
                       f"median of {len(times)} runs ({per:.3f} s each)",
+            "port_value": 2 * sm / statistics.median(ptimes),
+            "host": host_info(),
             "gpu_same_sample_ms": sts["device_ms"]}
+        del d_s, d_o
     # ---- geometric / skewed families and the many-graph workloads
     if not (args.no_batch and args.no_serving and args.no_geometric):
         del d_edges, d_out

@@ -404,53 +404,105 @@ extern "C" int oracle_gen_gnm(uint32_t n, uint64_t m, uint64_t seed,
       c[i] = {key, i};
     }
     __gnu_parallel::sort(c.begin(), c.end());
+    // first occurrence of every key: the head of its run (invalid keys, ~0,
+    // sort last and are no pair)
     std::vector<uint8_t> first(K, 0);
+#pragma omp parallel for schedule(static)
     for (uint64_t j = 0; j < K; ++j) {
-      if (c[j].first == ~0ull) break;
+      if (c[j].first == ~0ull) continue;
       if (j == 0 || c[j].first != c[j - 1].first) first[c[j].second] = 1;
     }
+    // T = the candidate index of the m-th first occurrence (blocked count)
+    const uint64_t nb = 256;
+    const uint64_t bs = (K + nb - 1) / nb;
+    std::vector<uint64_t> bc(nb, 0);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (uint64_t b = 0; b < nb; ++b) {
+      uint64_t k = 0;
+      for (uint64_t i = b * bs; i < std::min(K, (b + 1) * bs); ++i) k += first[i];
+      bc[b] = k;
+    }
     uint64_t cnt = 0, T = K;
-    for (uint64_t i = 0; i < K; ++i) {
-      cnt += first[i];
-      if (cnt == m) {
-        T = i;
-        break;
+    for (uint64_t b = 0; b < nb && T == K; ++b) {
+      if (cnt + bc[b] < m) {
+        cnt += bc[b];
+        continue;
+      }
+      for (uint64_t i = b * bs; i < std::min(K, (b + 1) * bs); ++i) {
+        cnt += first[i];
+        if (cnt == m) {
+          T = i;
+          break;
+        }
       }
     }
     if (T == K) {  // not enough distinct pairs yet: draw more
       K = K + (m - cnt) * 2 + 4096;
       continue;
     }
-    sel.reserve(m);
-    for (uint64_t j = 0; j < K; ++j) {
-      if (c[j].first == ~0ull) break;
-      if ((j == 0 || c[j].first != c[j - 1].first) && c[j].second <= T)
-        sel.push_back(c[j].first);
+    // the selected keys in key order: run heads with candidate index <= T
+    auto take = [&](uint64_t j) {
+      return c[j].first != ~0ull && (j == 0 || c[j].first != c[j - 1].first) && c[j].second <= T;
+    };
+    std::vector<uint64_t> sc(nb, 0);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (uint64_t b = 0; b < nb; ++b) {
+      uint64_t k = 0;
+      for (uint64_t j = b * bs; j < std::min(K, (b + 1) * bs); ++j) k += take(j);
+      sc[b] = k;
+    }
+    uint64_t tot = 0;
+    for (auto& x : sc) {
+      const uint64_t y = x;
+      x = tot;
+      tot += y;
+    }
+    sel.resize(tot);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (uint64_t b = 0; b < nb; ++b) {
+      uint64_t o = sc[b];
+      for (uint64_t j = b * bs; j < std::min(K, (b + 1) * bs); ++j)
+        if (take(j)) sel[o++] = c[j].first;
     }
     break;
   }
-  // Both directions sorted by (src, dst): row x = lower neighbours (from
-  // pairs (u, x), in increasing u) followed by upper neighbours (pairs (x, v),
-  // in increasing v).
-  std::vector<uint64_t> lowdeg(n, 0), deg(n, 0);
-  for (uint64_t key : sel) {
-    uint32_t u = static_cast<uint32_t>(key >> 32), v = static_cast<uint32_t>(key);
-    deg[u]++;
-    deg[v]++;
-    lowdeg[v]++;
+  // Both directions sorted by (src, dst): row x = lower neighbours (pairs
+  // (u, x), in increasing u) followed by upper neighbours (pairs (x, v), in
+  // increasing v).  sel is sorted by (u, v); the reversed keys (v << 32 | u),
+  // sorted, give every row's lower neighbours in order.
+  const uint64_t ms = sel.size();
+  std::vector<uint64_t> rev(ms);
+#pragma omp parallel for schedule(static)
+  for (uint64_t j = 0; j < ms; ++j) rev[j] = (sel[j] << 32) | (sel[j] >> 32);
+  __gnu_parallel::sort(rev.begin(), rev.end());
+  std::vector<uint64_t> updeg(n + 1, 0), lowdeg(n + 1, 0);
+#pragma omp parallel for schedule(static)
+  for (uint64_t j = 0; j < ms; ++j) {
+    __atomic_fetch_add(&updeg[sel[j] >> 32], 1, __ATOMIC_RELAXED);
+    __atomic_fetch_add(&lowdeg[rev[j] >> 32], 1, __ATOMIC_RELAXED);
   }
-  std::vector<uint64_t> lo_cur(n), hi_cur(n);
-  uint64_t off = 0;
+  // row offsets, and the first index of each row's run in sel and in rev
+  std::vector<uint64_t> row(n + 1), up0(n + 1), low0(n + 1);
+  uint64_t off = 0, a = 0, b = 0;
   for (uint32_t x = 0; x < n; ++x) {
-    lo_cur[x] = off;
-    hi_cur[x] = off + lowdeg[x];
-    off += deg[x];
+    row[x] = off;
+    up0[x] = a;
+    low0[x] = b;
+    off += lowdeg[x] + updeg[x];
+    a += updeg[x];
+    b += lowdeg[x];
   }
-  for (uint64_t key : sel) {
-    uint32_t u = static_cast<uint32_t>(key >> 32), v = static_cast<uint32_t>(key);
-    uint32_t w = 1 + static_cast<uint32_t>(hi64(mix64(wseed ^ key), max_weight));
-    out[hi_cur[u]++] = kamsta_wedge{u, v, w};
-    out[lo_cur[v]++] = kamsta_wedge{v, u, w};
+#pragma omp parallel for schedule(static)
+  for (uint64_t j = 0; j < ms; ++j) {
+    const uint64_t key = sel[j];
+    const uint32_t u = static_cast<uint32_t>(key >> 32), v = static_cast<uint32_t>(key);
+    const uint32_t w = 1 + static_cast<uint32_t>(hi64(mix64(wseed ^ key), max_weight));
+    out[row[u] + lowdeg[u] + (j - up0[u])] = kamsta_wedge{u, v, w};
+    const uint64_t rk = rev[j];
+    const uint32_t rv = static_cast<uint32_t>(rk >> 32), ru = static_cast<uint32_t>(rk);
+    const uint64_t ckey = (static_cast<uint64_t>(ru) << 32) | rv;
+    const uint32_t rw = 1 + static_cast<uint32_t>(hi64(mix64(wseed ^ ckey), max_weight));
+    out[row[rv] + (j - low0[rv])] = kamsta_wedge{rv, ru, rw};
   }
   *m_directed_out = 2 * sel.size();
   return 0;

@@ -134,6 +134,85 @@ def boruvka_filter(edges: np.ndarray, n: int, threads: int = 0):
     return out[: cnt.value].copy(), int(w.value), int(r.value)
 
 
+_ref = None
+
+
+def ref_available() -> bool:
+    from oracle import ref_build
+    return ref_build.available()
+
+
+def ref_lib():
+    """The reference's own single-rank local filter-Boruvka, compiled from its
+    sources with the oracle's shims (oracle/ref_build.py)."""
+    global _ref
+    if _ref is None:
+        from oracle import ref_build
+        L = C.CDLL(ref_build.build())
+        P, U64 = C.c_void_p, C.c_uint64
+        for f in (L.ref_local_contraction, L.ref_boruvka_filter_all_local):
+            f.argtypes = [P, U64, C.c_int, P, C.POINTER(U64), C.POINTER(U64),
+                          C.POINTER(C.c_double)]
+        L.ref_set_input.argtypes = [P, U64]
+        L.ref_run.argtypes = [C.c_int, C.c_int, P, C.POINTER(U64), C.POINTER(U64),
+                              C.POINTER(C.c_double)]
+        L.ref_max_threads.restype = C.c_int
+        _ref = L
+    return _ref
+
+
+def _ref_call(fn, edges, n, threads):
+    e = np.ascontiguousarray(edges, dtype=WEDGE)
+    out = np.empty(max(n, 1), WEDGE)
+    cnt, w, info = C.c_uint64(), C.c_uint64(), (C.c_double * 4)()
+    rc = fn(e.ctypes.data, len(e), threads, out.ctypes.data, C.byref(cnt), C.byref(w), info)
+    if rc == 2:
+        raise ValueError("reference build: weights must be <= 255 (WEdge_4_1)")
+    assert rc == 0
+    return out[: cnt.value].copy(), int(w.value), {
+        "local_forest_edges": int(info[0]), "finish_edges": int(info[1]),
+        "reference_s": info[2], "finish_s": info[3]}
+
+
+class RefSession:
+    """Repeated runs of the reference build on one input: the input's
+    std::vector<WEdge> copy is made once (the reference benchmark builds it
+    before its timer starts, benchmarks/mst.cpp:198-212)."""
+
+    def __init__(self, edges: np.ndarray, n: int):
+        self.e = np.ascontiguousarray(edges, dtype=WEDGE)
+        self.n = n
+        rc = ref_lib().ref_set_input(self.e.ctypes.data, len(self.e))
+        if rc == 2:
+            raise ValueError("reference build: weights must be <= 255 (WEdge_4_1)")
+        self.out = np.empty(max(n, 1), WEDGE)
+
+    def run(self, all_local: bool = False, threads: int = 0):
+        cnt, w, info = C.c_uint64(), C.c_uint64(), (C.c_double * 4)()
+        rc = ref_lib().ref_run(threads, int(all_local), self.out.ctypes.data, C.byref(cnt),
+                               C.byref(w), info)
+        assert rc == 0
+        return self.out[: cnt.value], int(w.value), {
+            "local_forest_edges": int(info[0]), "finish_edges": int(info[1]),
+            "reference_s": info[2], "finish_s": info[3]}
+
+    def close(self):
+        ref_lib().ref_clear_input()
+
+
+def ref_local_contraction(edges: np.ndarray, n: int, threads: int = 0):
+    """The reference's single-rank MODIFIED_BORUVKA preprocessing (first and
+    last vertex are cut vertices), the few edges it leaves finished by
+    Kruskal: (forest, weight, info)."""
+    return _ref_call(ref_lib().ref_local_contraction, edges, n, threads)
+
+
+def ref_all_local(edges: np.ndarray, n: int, threads: int = 0):
+    """The reference's boruvka_filter with every vertex local: the whole
+    forest from the reference's own rounds."""
+    return _ref_call(ref_lib().ref_boruvka_filter_all_local, edges, n, threads)
+
+
 def canon_keys(mst: np.ndarray) -> np.ndarray:
     """Sorted (min << 32 | max) keys of a forest: order-free edge-set identity."""
     a = np.minimum(mst["src"], mst["dst"]).astype(np.uint64)

@@ -362,3 +362,31 @@ def test_clique_path(kamsta, oracle, algo):
     fn, cfg = _configs(kamsta)[algo]
     e, n = _clique_path(kamsta, 1024, 32, 256, 47)
     _check(oracle, fn(e, cfg, n=n), e, n)
+
+
+_REF_CASES = {
+    "gnm_2e16_2e20": lambda O: (O.gen_gnm(1 << 16, 1 << 20, 2026), 1 << 16),
+    "gnm_2e22_2e26": lambda O: (O.gen_gnm(1 << 22, 1 << 26, 2026), 1 << 22),
+    "gnm_ties_w4": lambda O: (O.gen_gnm(1 << 18, 1 << 21, 31, 4), 1 << 18),
+    "rgg2d_2e20": lambda O: (O.gen_rgg2d(1 << 20, O.rgg_radius(1 << 20, 16), 32), 1 << 20),
+    "rhg_2e20": lambda O: (O.gen_rhg(1 << 20, 3.0, 16, 33), 1 << 20),
+}
+
+
+@pytest.mark.parametrize("algo", ["boruvka_plain", "boruvka_local", "filter_boruvka"])
+@pytest.mark.parametrize("case", list(_REF_CASES))
+def test_gpu_equals_reference_code(kamsta, oracle, algo, case):
+    """The GPU forest against the REFERENCE'S OWN code on the same input
+    (oracle/_ref, KaMSTa's local filter-Boruvka built from its sources):
+    bit-identical edge set to its all-local run, and the same total weight
+    as its single-rank preprocessing path."""
+    if not oracle.ref_available():
+        pytest.skip("the reference build is not present")
+    fn, cfg = _configs(kamsta)[algo]
+    e, n = _REF_CASES[case](oracle)
+    got = fn(e, cfg, n=n)
+    ref, ref_w, _ = oracle.ref_all_local(e, n)
+    assert int(got["w"].astype(np.uint64).sum()) == ref_w
+    assert np.array_equal(oracle.canon_keys(got), oracle.canon_keys(ref))
+    _, w1, _ = oracle.ref_local_contraction(e, n)
+    assert w1 == ref_w
