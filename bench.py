@@ -131,6 +131,20 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# The kernels behind each solver phase (kamsta_stats.phase_*), as named in
+# the ncu launch list.
+PHASE_KERNELS = {
+    "first_pass": "k_pass_dir (first pass over the directed input)",
+    "round_edges": "k_pass_seg (round relabel + self-loop drop + compaction + next minimum)",
+    "round_verts": "k_hook + k_jump_label + k_vertex_write (hook, pointer jumping, renumbering)",
+    "class_pass": "k_pass_seg (heavier weight classes: relabel + filter) + row-scan kernels",
+    "finalize": "k_compose + k_compose_last + k_rep_write + k_relabel_all (component labels)",
+    "emit": "k_emit (forest output)",
+    "plan": "k_sample_weights (pivot sample)",
+    "dedupe": "radix sort + k_dedupe_* (parallel-edge removal)",
+}
+
+
 def load_peak():
     try:
         with open(PEAKS_PATH) as f:
@@ -140,13 +154,18 @@ def load_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def load_traffic(kernel: str):
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summary."""
+def load_traffic(phase: str, alg_bytes_per_launch: float):
+    """Per-launch DRAM bytes of a phase's kernels: the traffic / algorithmic
+    ratio that ncu measured on a small case of the same kernels (committed
+    in profiles/roofline_traffic.json), times this launch's algorithmic
+    bytes.  (None, None) where no capture exists."""
     try:
         with open(TRAFFIC_PATH) as f:
             t = json.load(f)
-        e = t.get(kernel)
-        return (float(e["bytes_per_launch"]), e.get("source")) if e else (None, None)
+        e = t.get(phase)
+        if not e:
+            return None, None
+        return float(e["traffic_over_algorithmic"]) * alg_bytes_per_launch, e.get("source")
     except Exception:
         return None, None
 
@@ -576,24 +595,19 @@ def main():
     assert got == md
     torch.cuda.synchronize()
 
-    # autotune the first-pass tile (entries per thread) on this workload:
-    # one untimed solve per candidate, the fastest is used for every step
-    tiles = {}
-    cands = ((8, 2), (6, 2), (12, 2), (8, 4), (12, 4), (6, 4))
-    if args.tiles != "auto":
-        cands = (tuple(int(x) for x in args.tiles.split("x")),)
-    for items, seg in cands:
-        c = K.AlgorithmConfig(local_preprocessing=K.LocalPreprocessing(args.local_preprocessing),
-                              items_per_thread=items, seg_items_per_thread=seg)
-        st = {}
-        if len(cands) > 1:
-            ctx.boruvka_dev(d_edges.data_ptr(), md, n, d_out.data_ptr(), c, stream=sh)
-            ctx.boruvka_dev(d_edges.data_ptr(), md, n, d_out.data_ptr(), c, stream=sh, stats=st)
-        tiles[f"{items}x{seg}"] = st.get("device_ms", 0.0)
-    best = min(tiles, key=tiles.get)
-    best_items, best_seg = (int(x) for x in best.split("x"))
-    cfg = K.AlgorithmConfig(local_preprocessing=K.LocalPreprocessing(args.local_preprocessing),
-                            items_per_thread=best_items, seg_items_per_thread=best_seg)
+    # tiles: the library's autotuner (kamsta_autotune_tiles) times every
+    # (first-pass entries, list-pass records) pair on this input, untimed,
+    # and keeps the fastest in the context for every step
+    base = K.AlgorithmConfig(local_preprocessing=K.LocalPreprocessing(args.local_preprocessing))
+    if args.tiles == "auto":
+        tt = ctx.autotune_tiles(d_edges.data_ptr(), md, n, d_out.data_ptr(), base, stream=sh)
+        tiles = tt["ms"]
+        best_items, best_seg = tt["items_per_thread"], tt["seg_items_per_thread"]
+    else:
+        best_items, best_seg = (int(x) for x in args.tiles.split("x"))
+        ctx.set_tiles(best_items, best_seg)
+        tiles = {args.tiles: None}
+    cfg = base  # tiles 0: the context's tuned pair
     results = []
 
     def step(stats=None):
@@ -638,20 +652,32 @@ def main():
             a["ms"] += ph["ms"]
             a["bytes"] += ph["bytes"]
             a["launches"] += ph["launches"]
-    dom = "first_pass"
-    fp = phases[dom]
-    launch_ms = fp["ms"] / max(fp["launches"], 1)
-    bytes_per_launch = fp["bytes"] / max(fp["launches"], 1)
-    achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9 if launch_ms > 0 else 0.0
+    # every kernel group above 10% of the solve gets its own roofline line;
+    # the headline is the group with the largest measured device time
     peak, peak_src = load_peak()
-    traffic, traffic_src = load_traffic("k_pass_dir")
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic,
-                "kernel": "k_pass_dir (first pass over the directed input)",
+    solve_ms = sum(v["ms"] for v in phases.values())
+    kernels = []
+    for name, ph in sorted(phases.items(), key=lambda kv: -kv[1]["ms"]):
+        if ph["ms"] <= 0.10 * solve_ms or ph["launches"] == 0:
+            continue
+        launch_ms = ph["ms"] / ph["launches"]
+        bpl = ph["bytes"] / ph["launches"]
+        ach = bpl / (launch_ms / 1e3) / 1e9 if launch_ms > 0 else 0.0
+        kname = PHASE_KERNELS.get(name, name)
+        traffic, traffic_src = load_traffic(name, bpl)
+        kernels.append({"phase": name, "kernel": kname, "share": ph["ms"] / solve_ms,
+                        "launches_per_step": ph["launches"] / args.steps,
+                        "ms_per_step": ph["ms"] / args.steps, "alg_bytes_per_launch": bpl,
+                        "launch_ms": launch_ms, "achieved": ach, "frac": ach / peak,
+                        "traffic": traffic, "traffic_source": traffic_src})
+    top = kernels[0]
+    roofline = {"bound": "hbm", "achieved": top["achieved"], "peak": peak, "unit": "GB/s",
+                "frac": top["frac"], "traffic": top["traffic"], "kernel": top["kernel"],
+                "phase": top["phase"], "share": top["share"],
                 "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)" if peak_src == "measured"
                 else "fallback 6.8 TB/s",
-                "alg_bytes_per_launch": bytes_per_launch, "launch_ms": launch_ms,
-                "traffic_source": traffic_src}
+                "alg_bytes_per_launch": top["alg_bytes_per_launch"], "launch_ms": top["launch_ms"],
+                "traffic_source": top["traffic_source"], "kernels": kernels}
     solve_total = {k: round(v["ms"] / args.steps, 4) for k, v in phases.items()}
     whole = sum(s["alg_bytes"] for s in per_step) / args.steps
     line = {

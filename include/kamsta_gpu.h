@@ -282,6 +282,29 @@ kamsta_status kamsta_batch_autotune(kamsta_ctx* ctx, kamsta_graph_desc* graphs,
 /* Sets (e.g. from a cached autotune result) or clears (zeros) the tuning. */
 kamsta_status kamsta_ctx_set_tuning(kamsta_ctx* ctx, const kamsta_tuning* tuning);
 
+/* ---- single-graph tile autotuner ----------------------------------------
+ * No counterpart in the reference.  Solves the given device input once
+ * untimed, then once per (items_per_thread, seg_items_per_thread) pair of
+ * {6, 8, 12} x {2, 4} with cfg's algorithm settings (KAMSTA_FLAG_FILTER
+ * selects filter_boruvka), timing each solve with CUDA events, and keeps the
+ * fastest pair in the context: later solves on this context whose cfg leaves
+ * items_per_thread / seg_items_per_thread at 0 use it.  d_out needs room for
+ * n - 1 entries (scratch).  ms[] is in the pair order (6,2) (8,2) (12,2)
+ * (6,4) (8,4) (12,4). */
+typedef struct kamsta_tile_tuning {
+  uint32_t items_per_thread;      /* chosen first-pass entries per thread   */
+  uint32_t seg_items_per_thread;  /* chosen list-pass records per thread    */
+  double ms[6];                   /* device ms of each pair's solve          */
+} kamsta_tile_tuning;
+kamsta_status kamsta_autotune_tiles(kamsta_ctx* ctx, const kamsta_wedge* d_edges,
+                                    uint64_t m_directed, uint32_t n, const kamsta_cfg* cfg,
+                                    kamsta_wedge* d_out, kamsta_tile_tuning* out,
+                                    kamsta_stream stream);
+/* Sets (e.g. from a cached autotune result) or clears (zeros) the context's
+ * single-graph tiles. */
+kamsta_status kamsta_ctx_set_tiles(kamsta_ctx* ctx, uint32_t items_per_thread,
+                                   uint32_t seg_items_per_thread);
+
 /* ---- serving loop -------------------------------------------------------
  * No counterpart in the reference.  A continuous-batching request loop:
  * clients submit jobs whose edge arrays already sit in device memory (their

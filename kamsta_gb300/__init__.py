@@ -526,6 +526,22 @@ class Context:
                                           C.c_void_p(stream or 0)))
         return t.as_dict()
 
+    def autotune_tiles(self, d_edges: int, m: int, n: int, d_out: int, config=None,
+                       stream=0) -> dict:
+        """kamsta_autotune_tiles: times every tile pair on this input and
+        keeps the fastest in the context (used when the config leaves the
+        tiles at 0)."""
+        cfg = (config or AlgorithmConfig()).to_c()
+        t = _native.TileTuning()
+        check(lib().kamsta_autotune_tiles(self._h, C.c_void_p(d_edges), int(m), int(n),
+                                          C.byref(cfg), C.c_void_p(d_out), C.byref(t),
+                                          C.c_void_p(stream or 0)))
+        return t.as_dict()
+
+    def set_tiles(self, items_per_thread: int = 0, seg_items_per_thread: int = 0):
+        check(lib().kamsta_ctx_set_tiles(self._h, int(items_per_thread),
+                                         int(seg_items_per_thread)))
+
     def set_tuning(self, small_threads: int = 0, small_max_n: int = 0):
         t = _native.Tuning()
         t.small_threads, t.small_max_n = int(small_threads), int(small_max_n)

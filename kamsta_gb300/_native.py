@@ -119,6 +119,17 @@ class Tuning(C.Structure):
                 "cutoff_ms": dict(zip((4096, 8192, 16384, 32768), list(self.cutoff_ms)))}
 
 
+class TileTuning(C.Structure):
+    _fields_ = [("items_per_thread", C.c_uint32), ("seg_items_per_thread", C.c_uint32),
+                ("ms", C.c_double * 6)]
+    PAIRS = ("6x2", "8x2", "12x2", "6x4", "8x4", "12x4")
+
+    def as_dict(self) -> dict:
+        return {"items_per_thread": self.items_per_thread,
+                "seg_items_per_thread": self.seg_items_per_thread,
+                "ms": dict(zip(self.PAIRS, list(self.ms)))}
+
+
 _lib = None
 
 # Every symbol declared in include/kamsta_gpu.h, with its ctypes signature.
@@ -180,6 +191,8 @@ SIGNATURES = {
     "kamsta_batch_autotune": (I32, [P, C.POINTER(GraphDesc), U32, C.POINTER(Cfg),
                                     C.POINTER(Tuning), P]),
     "kamsta_ctx_set_tuning": (I32, [P, C.POINTER(Tuning)]),
+    "kamsta_autotune_tiles": (I32, [P, P, U64, U32, P, P, C.POINTER(TileTuning), P]),
+    "kamsta_ctx_set_tiles": (I32, [P, U32, U32]),
     "kamsta_mst_batch": (I32, [P, C.POINTER(GraphDesc), U32, C.POINTER(Cfg), U64,
                                C.POINTER(BatchStats)]),
 }

@@ -630,6 +630,68 @@ kamsta_status kamsta_ctx_set_tuning(kamsta_ctx* ctx, const kamsta_tuning* t) {
   return KAMSTA_OK;
 }
 
+kamsta_status kamsta_ctx_set_tiles(kamsta_ctx* ctx, uint32_t items, uint32_t seg_items) {
+  if (!ctx) {
+    set_error("null context");
+    return KAMSTA_E_INPUT;
+  }
+  if ((items != 0 && items != 6 && items != 8 && items != 12) ||
+      (seg_items != 0 && seg_items != 2 && seg_items != 4 && seg_items != 8)) {
+    set_error("tiles: items_per_thread 0, 6, 8 or 12; seg_items_per_thread 0, 2, 4 or 8");
+    return KAMSTA_E_INPUT;
+  }
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  ctx->tune_dir_items = items;
+  ctx->tune_seg_items = seg_items;
+  return KAMSTA_OK;
+}
+
+kamsta_status kamsta_autotune_tiles(kamsta_ctx* ctx, const kamsta_wedge* d_edges,
+                                    uint64_t m, uint32_t n, const kamsta_cfg* cfg,
+                                    kamsta_wedge* d_out, kamsta_tile_tuning* out,
+                                    kamsta_stream stream) {
+  if (!ctx || !out || (m && !d_edges) || (n > 1 && !d_out)) {
+    set_error("null pointer argument");
+    return KAMSTA_E_INPUT;
+  }
+  kamsta_status s = check_cfg(cfg);
+  if (s != KAMSTA_OK) return s;
+  const kamsta_cfg base = cfg_or_default(cfg);
+  const Algo algo = (base.flags & KAMSTA_FLAG_FILTER) ? Algo::kFilterBoruvka : Algo::kBoruvka;
+  static const uint32_t kPairs[6][2] = {{6, 2}, {8, 2}, {12, 2}, {6, 4}, {8, 4}, {12, 4}};
+  std::memset(out, 0, sizeof(*out));
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  int cur = 0;
+  cudaGetDevice(&cur);
+  if (cur != ctx->device) {
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return cuda_status(e, "cudaSetDevice");
+  }
+  const cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  int best = -1;
+  for (int i = -1; i < 6 && s == KAMSTA_OK; ++i) {  // i = -1: the untimed warm-up
+    kamsta_cfg c = base;
+    c.items_per_thread = kPairs[i < 0 ? 0 : i][0];
+    c.seg_items_per_thread = kPairs[i < 0 ? 0 : i][1];
+    c.flags &= ~static_cast<uint32_t>(KAMSTA_FLAG_SORT_OUTPUT);
+    SolveOut so;
+    kamsta_stats stt;
+    s = solve_device(ctx, algo, d_edges, m, n, c, d_out, &so, &stt, st);
+    if (s != KAMSTA_OK || i < 0) continue;
+    out->ms[i] = stt.device_ms;
+    if (best < 0 || stt.device_ms < out->ms[best]) best = i;
+  }
+  if (cur != ctx->device) cudaSetDevice(cur);
+  if (s != KAMSTA_OK) return s;
+  if (best >= 0) {
+    out->items_per_thread = kPairs[best][0];
+    out->seg_items_per_thread = kPairs[best][1];
+    ctx->tune_dir_items = out->items_per_thread;
+    ctx->tune_seg_items = out->seg_items_per_thread;
+  }
+  return KAMSTA_OK;
+}
+
 kamsta_status kamsta_mst_batch(kamsta_ctx* ctx, kamsta_graph_desc* graphs, uint32_t count,
                                const kamsta_cfg* cfg, uint64_t budget_bytes,
                                kamsta_batch_stats* stats) {

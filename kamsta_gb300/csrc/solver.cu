@@ -1147,11 +1147,11 @@ kamsta_status Solve::run(Algo algo, kamsta_wedge* d_out, SolveOut* out) {
   CU_TRY(cudaGetDevice(&dev));
   CU_TRY(cudaDeviceGetAttribute(&sms_, cudaDevAttrMultiProcessorCount, dev));
   aligned16_ = (reinterpret_cast<uintptr_t>(in_) & 15u) == 0;
-  if (cfg_.items_per_thread == 6 || cfg_.items_per_thread == 8 || cfg_.items_per_thread == 12)
-    dir_items_ = static_cast<int>(cfg_.items_per_thread);
-  if (cfg_.seg_items_per_thread == 2 || cfg_.seg_items_per_thread == 4 ||
-      cfg_.seg_items_per_thread == 8)
-    seg_items_ = static_cast<int>(cfg_.seg_items_per_thread);
+  // tiles: the call's cfg, else the context's tuned pair, else the defaults
+  const uint32_t di = cfg_.items_per_thread ? cfg_.items_per_thread : ctx_->tune_dir_items;
+  const uint32_t si = cfg_.seg_items_per_thread ? cfg_.seg_items_per_thread : ctx_->tune_seg_items;
+  if (di == 6 || di == 8 || di == 12) dir_items_ = static_cast<int>(di);
+  if (si == 2 || si == 4 || si == 8) seg_items_ = static_cast<int>(si);
   samples_ = ctx_->d_samples;
   {
     const char* dbg = std::getenv("KAMSTA_DEBUG_CHECKS");

@@ -57,6 +57,9 @@ struct kamsta_ctx {
   // batch tuning (kamsta_batch_autotune); 0 = built-in default
   uint32_t tune_small_threads = 0;  // CTA size of the persistent small-graph kernel
   uint32_t tune_small_max_n = 0;    // largest n taken by that kernel
+  // single-graph tiles (kamsta_autotune_tiles); 0 = built-in default
+  uint32_t tune_dir_items = 0;      // entries per thread of the first pass
+  uint32_t tune_seg_items = 0;      // records per thread of the list passes
   kamsta::Arena fixed;   // vertex arrays and look-back words
   cudaMemPool_t pool = nullptr;  // edge lists (stream-ordered, cached between calls)
   kamsta::DevCounters* d_counters = nullptr;  // kCSlots blocks

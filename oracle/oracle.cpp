@@ -59,18 +59,36 @@ extern "C" int oracle_max_threads(void) { return omp_get_max_threads(); }
 extern "C" int oracle_kruskal(const kamsta_wedge* edges, uint64_t m_directed,
                               uint32_t n, kamsta_wedge* out,
                               uint64_t* out_count, uint64_t* total_weight) {
-  std::vector<kamsta_wedge> und;
-  und.reserve(m_directed / 2 + 1);
-  for (uint64_t i = 0; i < m_directed; ++i) {
-    if (edges[i].src < edges[i].dst) {
-      if (edges[i].dst >= n) return 1;
-      und.push_back(edges[i]);
+  // the src<dst copies in input order (a blocked, order-preserving filter)
+  const uint64_t nb = 256, bs = (m_directed + nb - 1) / nb;
+  std::vector<uint64_t> cnts(nb + 1, 0);
+  int bad = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(| : bad)
+  for (uint64_t b = 0; b < nb; ++b) {
+    uint64_t c = 0;
+    for (uint64_t i = b * bs; i < std::min(m_directed, (b + 1) * bs); ++i) {
+      if (edges[i].src < edges[i].dst) {
+        bad |= edges[i].dst >= n;
+        ++c;
+      }
     }
+    cnts[b + 1] = c;
   }
-  std::stable_sort(und.begin(), und.end(),
-                   [](const kamsta_wedge& a, const kamsta_wedge& b) {
-                     return a.w < b.w;
-                   });
+  if (bad) return 1;
+  for (uint64_t b = 0; b < nb; ++b) cnts[b + 1] += cnts[b];
+  std::vector<kamsta_wedge> und(cnts[nb]);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (uint64_t b = 0; b < nb; ++b) {
+    uint64_t o = cnts[b];
+    for (uint64_t i = b * bs; i < std::min(m_directed, (b + 1) * bs); ++i)
+      if (edges[i].src < edges[i].dst) und[o++] = edges[i];
+  }
+  // stable by weight: ties keep the (src, dst) input order, i.e. the
+  // (w, min, max) order of the reference's WeightSrcDstOrder
+  __gnu_parallel::stable_sort(und.begin(), und.end(),
+                              [](const kamsta_wedge& a, const kamsta_wedge& b) {
+                                return a.w < b.w;
+                              });
   UnionFind uf(n);
   uint64_t cnt = 0, weight = 0;
   for (const auto& e : und) {

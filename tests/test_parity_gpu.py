@@ -390,3 +390,28 @@ def test_gpu_equals_reference_code(kamsta, oracle, algo, case):
     assert np.array_equal(oracle.canon_keys(got), oracle.canon_keys(ref))
     _, w1, _ = oracle.ref_local_contraction(e, n)
     assert w1 == ref_w
+
+
+def test_tile_autotuner_in_the_library(kamsta, oracle):
+    """kamsta_autotune_tiles times every tile pair on the input, keeps the
+    fastest in the context, and later solves with default tiles use it and
+    give the same forest."""
+    import torch
+    n, m = 1 << 18, 1 << 22
+    e = oracle.gen_gnm(n, m, 61)
+    ctx = kamsta.Context(0)
+    d = torch.from_numpy(e.view(np.uint32).reshape(-1, 3).view(np.int32)).cuda()
+    o = torch.empty((n, 3), dtype=torch.int32, device="cuda")
+    t = ctx.autotune_tiles(d.data_ptr(), len(e), n, o.data_ptr())
+    assert (t["items_per_thread"], t["seg_items_per_thread"]) in [(6, 2), (8, 2), (12, 2),
+                                                                  (6, 4), (8, 4), (12, 4)]
+    assert all(v > 0 for v in t["ms"].values())
+    key = f'{t["items_per_thread"]}x{t["seg_items_per_thread"]}'
+    assert t["ms"][key] == min(t["ms"].values())
+    k = ctx.boruvka_dev(d.data_ptr(), len(e), n, o.data_ptr())
+    got = o[:k].cpu().numpy().view(np.uint32).reshape(-1).view(kamsta.WEDGE)
+    _check(oracle, got, e, n)
+    ctx.set_tiles(12, 4)
+    with pytest.raises(kamsta.KamstaError):
+        ctx.set_tiles(7, 2)
+    ctx.close()
