@@ -183,23 +183,64 @@ __device__ __forceinline__ void seg_tile_finish(const uint8_t (&cls)[ITEMS],
     const uint32_t cap = static_cast<uint32_t>(p.out[c].cap);
     const uint32_t run0 = static_cast<uint32_t>(run[c]);
     const uint64_t seg0 = static_cast<uint64_t>(seg_id(p)) * p.out[c].cap + run0;
-    for (uint32_t i = threadIdx.x; i < tot[c]; i += kBlock) {
-      const uint32_t local = run0 + i;
-      if (local >= cap) {
-        atomicOr(p.err, kErrOverflow);
-        continue;
+    if constexpr (ITEMS <= 2) {
+      // a class holds at most the tile's ITEMS * kBlock items: item k of
+      // this thread is i = threadIdx.x + k * kBlock.  Every checking read of
+      // the thread is in flight before the first compare, instead of one
+      // read latency per item (wider tiles keep the per-item loop below:
+      // their records would not fit in registers).
+      bool has[ITEMS];
+      Rec r[ITEMS];
+#pragma unroll
+      for (int k = 0; k < ITEMS; ++k) {
+        const uint32_t i = threadIdx.x + k * kBlock;
+        has[k] = i < tot[c];
+        if (!has[k]) continue;
+        if (run0 + i >= cap) {
+          atomicOr(p.err, kErrOverflow);
+          has[k] = false;
+          continue;
+        }
+        r[k] = rec(s_dense[cbase[c] + i]);
+        sg[run0 + i] = r[k];
       }
-      const Rec r = rec(s_dense[cbase[c] + i]);
-      sg[local] = r;
       if (c != 0 || p.minval == nullptr || p.min_partner) continue;
-      const uint64_t v = (static_cast<uint64_t>(r.w) << 32) | (seg0 + i);
-      if (p.min_checked) {
-        const uint64_t ca = ld_weak(&p.minval[r.a]), cb = ld_weak(&p.minval[r.b]);
-        if (v < ca) red_min(&p.minval[r.a], v);
-        if (v < cb) red_min(&p.minval[r.b], v);
-      } else {
-        red_min(&p.minval[r.a], v);
-        red_min(&p.minval[r.b], v);
+      uint64_t ca[ITEMS], cb[ITEMS];
+#pragma unroll
+      for (int k = 0; k < ITEMS; ++k) {
+        ca[k] = cb[k] = ~0ull;
+        if (has[k] && p.min_checked) {
+          ca[k] = ld_weak(&p.minval[r[k].a]);
+          cb[k] = ld_weak(&p.minval[r[k].b]);
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < ITEMS; ++k) {
+        if (!has[k]) continue;
+        const uint64_t v =
+            (static_cast<uint64_t>(r[k].w) << 32) | (seg0 + threadIdx.x + k * kBlock);
+        if (v < ca[k]) red_min(&p.minval[r[k].a], v);
+        if (v < cb[k]) red_min(&p.minval[r[k].b], v);
+      }
+    } else {
+      for (uint32_t i = threadIdx.x; i < tot[c]; i += kBlock) {
+        const uint32_t local = run0 + i;
+        if (local >= cap) {
+          atomicOr(p.err, kErrOverflow);
+          continue;
+        }
+        const Rec r = rec(s_dense[cbase[c] + i]);
+        sg[local] = r;
+        if (c != 0 || p.minval == nullptr || p.min_partner) continue;
+        const uint64_t v = (static_cast<uint64_t>(r.w) << 32) | (seg0 + i);
+        if (p.min_checked) {
+          const uint64_t ca = ld_weak(&p.minval[r.a]), cb = ld_weak(&p.minval[r.b]);
+          if (v < ca) red_min(&p.minval[r.a], v);
+          if (v < cb) red_min(&p.minval[r.b], v);
+        } else {
+          red_min(&p.minval[r.a], v);
+          red_min(&p.minval[r.b], v);
+        }
       }
     }
   }
