@@ -504,6 +504,7 @@ def serve_once(args, K, b, rate, R, seed):
     th.join(timeout=600)
     stop.set()
     sst = srv.stats()
+    mem = srv.memory()
     srv.close()
     assert len(done) == R, f"serving: {len(done)} of {R} requests finished"
     lat = [(done[i]["finish_us"] - done[i]["submit_us"]) / 1e3 for i in range(R)]
@@ -514,7 +515,9 @@ def serve_once(args, K, b, rate, R, seed):
     res = {"rate_per_s": rate, "requests": R, "throughput": R / span, "unit": "graphs/s",
            **W.percentiles(lat), "mean_ms": float(np.mean(lat)),
            "mean_batch": float(np.mean([done[i]["batch_size"] for i in range(R)])),
-           "waves": sst["waves"], "exact_vs_batch": bool(exact)}
+           "waves": sst["waves"], "exact_vs_batch": bool(exact),
+           "worker_limit_gb": mem["worker_limit"] / 2**30,
+           "peak_worker_gb": mem["peak_worker_bytes"] / 2**30}
     del out
     return res, arrivals, gidx
 
@@ -543,6 +546,20 @@ def run_serving(args, K, ctx, sh, b):
                                               "p99_ms", "p99_9_ms", "mean_batch",
                                               "exact_vs_batch")}
         res["load_points"] = sweep
+        # saturation: the highest offered rate whose p99 stays under 50 ms
+        sat = {}
+        for f in (0.75, 1.0, 1.25, 1.5, 2.0):
+            r, _, _ = serve_once(args, K, b, f * b["graphs_per_s"], R // 4, args.seed + 41)
+            sat[f"{f:.2f}x_batch_rate"] = {k: r[k] for k in
+                                           ("rate_per_s", "throughput", "p50_ms", "p99_ms",
+                                            "exact_vs_batch")}
+        ok = [v for v in sat.values() if v["p99_ms"] < 50.0]
+        res["saturation"] = {
+            "rule": "highest offered rate (Poisson, requests/4 each) whose p99 latency < 50 ms",
+            "rate_per_s": max((v["rate_per_s"] for v in ok), default=None),
+            "throughput": max((v["throughput"] for v in ok), default=None),
+            "max_throughput_seen": max(v["throughput"] for v in sat.values()),
+            "points": sat}
     # sequential plain solves under the same arrivals (FIFO, one at a time)
     cfg = K.AlgorithmConfig(local_preprocessing=K.LocalPreprocessing(args.local_preprocessing))
     P = min(args.serve_plain_requests, R)
@@ -713,8 +730,25 @@ def main():
         torch.cuda.synchronize()
         ms0 = t0.elapsed_time(t1)
         assert k0 == forest and st0["total_weight"] == per_step[-1]["total_weight"]
-        line["variants"] = {"no_preprocessing": {"value": md / (ms0 / 1e3), "ms_per_step": ms0,
-                                                 "rounds": st0["rounds"]}}
+        peak, _ = load_peak()
+        alg0 = st0["alg_bytes"]
+        ph0 = {k: {"ms": round(v["ms"], 3), "gbs": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1)
+                   if v["ms"] > 0 else None} for k, v in st0["phases"].items() if v["ms"] > 0}
+        # parallel-edge removal on this path: off, and by ratio m_r > r * n_r
+        sweep = {}
+        for ratio in (0, 4, 16, 64):
+            c = K.AlgorithmConfig(local_preprocessing=K.LocalPreprocessing.NO_PREPROCESSING,
+                                  dedupe_ratio=ratio)
+            sts = {}
+            kk = ctx.boruvka_dev(d_edges.data_ptr(), md, n, d_out.data_ptr(), c, stream=sh,
+                                 stats=sts)
+            assert kk == forest and sts["total_weight"] == per_step[-1]["total_weight"]
+            sweep[str(ratio)] = round(sts["device_ms"], 2)
+        line["variants"] = {"no_preprocessing": {
+            "value": md / (ms0 / 1e3), "ms_per_step": ms0, "rounds": st0["rounds"],
+            "whole_solve_alg_gbs": alg0 / (ms0 / 1e3) / 1e9,
+            "frac": alg0 / (ms0 / 1e3) / 1e9 / peak, "phases": ph0,
+            "dedupe_ratio_sweep_ms": sweep}}
 
     # ---- e2e through the host-buffer C ABI call (pinned host input)
     if not args.no_e2e:

@@ -260,15 +260,21 @@ inline size_t scan_counts(std::vector<size_t>& c) {
   return t;
 }
 
-// Stable pack: out[k] = in[i] for the k-th i with keep(i).
+// Stable pack: out[k] = in[i] for the k-th i with keep(i).  keep is
+// evaluated once per element (into a byte per element), as ParlayLib's
+// blocked pack does.
 template <typename In, typename Keep, typename Put>
 size_t stable_pack(size_t n, In&& in, Keep&& keep, Put&& put) {
   const size_t nb = blocks_of(n);
   std::vector<size_t> cnt(nb, 0);
+  std::unique_ptr<uint8_t[]> fl(new uint8_t[std::max<size_t>(n, 1)]);
   parallel_for(0, nb, [&](size_t b) {
     size_t c = 0;
     const size_t e = std::min(n, (b + 1) * kBlock);
-    for (size_t i = b * kBlock; i < e; ++i) c += keep(i) ? 1 : 0;
+    for (size_t i = b * kBlock; i < e; ++i) {
+      fl[i] = keep(i) ? 1 : 0;
+      c += fl[i];
+    }
     cnt[b] = c;
   }, 1);
   const size_t total = scan_counts(cnt);
@@ -276,7 +282,7 @@ size_t stable_pack(size_t n, In&& in, Keep&& keep, Put&& put) {
     size_t o = cnt[b];
     const size_t e = std::min(n, (b + 1) * kBlock);
     for (size_t i = b * kBlock; i < e; ++i)
-      if (keep(i)) put(o++, in(i));
+      if (fl[i]) put(o++, in(i));
   }, 1);
   return total;
 }
@@ -361,10 +367,14 @@ auto filter(R const& r, P p, flags = no_flag) {
   const size_t n = r.size();
   const size_t nb = internal::blocks_of(n);
   std::vector<size_t> cnt(nb, 0);
+  std::unique_ptr<uint8_t[]> fl(new uint8_t[std::max<size_t>(n, 1)]);
   parallel_for(0, nb, [&](size_t b) {
     size_t c = 0;
     const size_t e = std::min(n, (b + 1) * internal::kBlock);
-    for (size_t i = b * internal::kBlock; i < e; ++i) c += p(r[i]) ? 1 : 0;
+    for (size_t i = b * internal::kBlock; i < e; ++i) {
+      fl[i] = p(r[i]) ? 1 : 0;
+      c += fl[i];
+    }
     cnt[b] = c;
   }, 1);
   const size_t total = internal::scan_counts(cnt);
@@ -373,7 +383,7 @@ auto filter(R const& r, P p, flags = no_flag) {
     size_t o = cnt[b];
     const size_t e = std::min(n, (b + 1) * internal::kBlock);
     for (size_t i = b * internal::kBlock; i < e; ++i)
-      if (p(r[i])) new (out.data() + o++) T(r[i]);
+      if (fl[i]) new (out.data() + o++) T(r[i]);
   }, 1);
   return out;
 }
