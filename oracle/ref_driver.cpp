@@ -166,22 +166,52 @@ int run(bool all_local, RunOut& r) {
   r.local_forest = found;
   r.forest.assign(mst_ids.begin(), mst_ids.begin() + found);
 
-  // the edges the local phase left: endpoints in different components
-  // (stand-in for the distributed rounds; a parallel filter and sort, then
-  // Kruskal over the few survivors)
-  auto rest_seq = parlay::filter(
-      parlay::delayed_seq<uint64_t>(m, [](size_t i) { return static_cast<uint64_t>(i); }),
-      [&](uint64_t i) {
-        const Edge12& e = in[i];
-        return e.src < e.dst && parents[normal(e.src)] != parents[normal(e.dst)];
+  // The edges the local phase left: endpoints in different components.
+  // Stand-in for the distributed rounds: nearly every vertex ends in one
+  // giant component, so only the rows of the vertices outside it are
+  // scanned (an edge between two components has an endpoint outside the
+  // giant); when many vertices are outside, every entry is checked.  Then
+  // Kruskal over the candidates under the (w, min, max) order.
+  const size_t nr = range.n();
+  const VId giant = parents[nr / 2];
+  auto outside = parlay::filter(
+      parlay::delayed_seq<uint64_t>(nr, [](size_t i) { return static_cast<uint64_t>(i); }),
+      [&](uint64_t i) { return parents[i] != giant; });
+  std::vector<uint64_t> rest;
+  auto differ = [&](uint64_t i) {
+    return parents[normal(in[i].src)] != parents[normal(in[i].dst)];
+  };
+  if (outside.size() <= nr / 16) {
+    std::vector<std::vector<uint64_t>> part(omp_get_max_threads());
+#pragma omp parallel for schedule(dynamic, 64)
+    for (size_t k = 0; k < outside.size(); ++k) {
+      const uint64_t v = range.v_begin + outside[k];
+      const Edge12* row = std::lower_bound(in, in + m, v, [](const Edge12& e, uint64_t x) {
+        return e.src < x;
       });
-  std::vector<uint64_t> rest(rest_seq.begin(), rest_seq.end());
+      auto& mine = part[omp_get_thread_num()];
+      for (const Edge12* e = row; e < in + m && e->src == v; ++e) {
+        const bool u_out = parents[normal(e->dst)] != giant;
+        // an edge between two outside vertices is taken from its src < dst copy
+        if (differ(static_cast<uint64_t>(e - in)) && (!u_out || e->src < e->dst))
+          mine.push_back(static_cast<uint64_t>(e - in));
+      }
+    }
+    for (auto& p : part) rest.insert(rest.end(), p.begin(), p.end());
+  } else {
+    auto rest_seq = parlay::filter(
+        parlay::delayed_seq<uint64_t>(m, [](size_t i) { return static_cast<uint64_t>(i); }),
+        [&](uint64_t i) { return in[i].src < in[i].dst && differ(i); });
+    rest.assign(rest_seq.begin(), rest_seq.end());
+  }
   r.finish_edges = rest.size();
-  ips4o::parallel::sort(rest.begin(), rest.end(), [&](uint64_t a, uint64_t b) {
-    return std::make_tuple(in[a].w, in[a].src, in[a].dst) <
-           std::make_tuple(in[b].w, in[b].src, in[b].dst);
-  });
-  UnionFind uf(range.n());
+  auto key = [&](uint64_t i) {
+    return std::make_tuple(in[i].w, std::min(in[i].src, in[i].dst),
+                           std::max(in[i].src, in[i].dst));
+  };
+  ips4o::parallel::sort(rest.begin(), rest.end(),
+                        [&](uint64_t a, uint64_t b) { return key(a) < key(b); });
+  UnionFind uf(nr);
   for (uint64_t i : rest) {
     const uint64_t a = uf.find(normal(parents[normal(in[i].src)]));
     const uint64_t b = uf.find(normal(parents[normal(in[i].dst)]));
