@@ -82,6 +82,12 @@ struct PassArgs {
   uint32_t validate;  // check id range and (src,dst) order (directed source)
   uint32_t aligned16; // directed source base is 16-byte aligned
   uint32_t cta_base;  // segment / chunk index of block 0 (a pass launched in groups)
+  // List passes of late rounds, whose next round has few labels: the
+  // minimum of labels [0, smin_n) is taken per CTA in shared memory and
+  // flushed with one reduction per label at the end (0 = off).  With few
+  // labels left, every record's update would otherwise hit one of a handful
+  // of L2 addresses.
+  uint32_t smin_n;
 };
 
 // The segment (and input chunk) this CTA owns.
@@ -138,6 +144,17 @@ __device__ __forceinline__ uint32_t next_tile(uint32_t* ticket) {
   return s_tile;
 }
 
+// A next-round minimum update into the CTA's shared minima; a label beyond
+// them (not expected: the host sizes them for every label the round can
+// produce) goes to the global word.
+__device__ __forceinline__ void smin_update(const PassArgs& p, uint64_t* smin, uint32_t x,
+                                            uint64_t v) {
+  if (x < p.smin_n)
+    atomicMin(reinterpret_cast<unsigned long long*>(smin + x), static_cast<unsigned long long>(v));
+  else
+    red_min(&p.minval[x], v);
+}
+
 // Rank the tile's kept items (stable), append them to this CTA's output
 // segments and feed the fused minimum.  rec(t) returns tile item t from
 // shared memory; run[] holds the CTA's running segment sizes (the same in
@@ -152,7 +169,7 @@ __device__ __forceinline__ uint32_t next_tile(uint32_t* ticket) {
 template <int NOUT, int ITEMS, typename RecAt>
 __device__ __forceinline__ void seg_tile_finish(const uint8_t (&cls)[ITEMS],
                                                       uint64_t (&run)[NOUT], const PassArgs& p,
-                                                      RecAt rec) {
+                                                      RecAt rec, uint64_t* smin = nullptr) {
   __shared__ uint32_t s_rank[NOUT * ITEMS * (kBlock / 32)];
   __shared__ uint32_t s_tot[NOUT];
   __shared__ uint16_t s_dense[ITEMS * kBlock];
@@ -205,6 +222,17 @@ __device__ __forceinline__ void seg_tile_finish(const uint8_t (&cls)[ITEMS],
         sg[run0 + i] = r[k];
       }
       if (c != 0 || p.minval == nullptr || p.min_partner) continue;
+      if (smin) {  // per-CTA minima (labels < p.smin_n)
+#pragma unroll
+        for (int k = 0; k < ITEMS; ++k) {
+          if (!has[k]) continue;
+          const uint64_t v =
+              (static_cast<uint64_t>(r[k].w) << 32) | (seg0 + threadIdx.x + k * kBlock);
+          smin_update(p, smin, r[k].a, v);
+          smin_update(p, smin, r[k].b, v);
+        }
+        continue;
+      }
       uint64_t ca[ITEMS], cb[ITEMS];
 #pragma unroll
       for (int k = 0; k < ITEMS; ++k) {
@@ -233,7 +261,10 @@ __device__ __forceinline__ void seg_tile_finish(const uint8_t (&cls)[ITEMS],
         sg[local] = r;
         if (c != 0 || p.minval == nullptr || p.min_partner) continue;
         const uint64_t v = (static_cast<uint64_t>(r.w) << 32) | (seg0 + i);
-        if (p.min_checked) {
+        if (smin) {
+          smin_update(p, smin, r.a, v);
+          smin_update(p, smin, r.b, v);
+        } else if (p.min_checked) {
           const uint64_t ca = ld_weak(&p.minval[r.a]), cb = ld_weak(&p.minval[r.b]);
           if (v < ca) red_min(&p.minval[r.a], v);
           if (v < cb) red_min(&p.minval[r.b], v);
@@ -481,7 +512,8 @@ __global__ void __launch_bounds__(kBlock, ITEMS <= 2 ? 5 : ITEMS <= 4 ? 4 : 3)
     k_pass_seg(SegIn in, PassArgs p) {
   constexpr uint32_t kRecTile = rec_tile(ITEMS);
   constexpr int kItemsRec = ITEMS;
-  extern __shared__ __align__(128) Rec s_rec[];  // two stages
+  extern __shared__ __align__(128) Rec s_rec[];  // two stages, then p.smin_n minima
+  uint64_t* s_min = p.smin_n ? reinterpret_cast<uint64_t*>(s_rec + 2 * kRecTile) : nullptr;
   __shared__ uint64_t s_prefix[kMaxSeg + 1];
   __shared__ __align__(8) uint64_t s_bar[2];
   __shared__ uint32_t s_ok, s_plain[2];
@@ -538,6 +570,7 @@ __global__ void __launch_bounds__(kBlock, ITEMS <= 2 ? 5 : ITEMS <= 4 ? 4 : 3)
     fence_mbar_init();
     if (ntile > 0) issue(0, 0);
   }
+  for (uint32_t x = threadIdx.x; x < p.smin_n; x += kBlock) s_min[x] = kInf64;
   __syncthreads();
   uint64_t run[NOUT];
 #pragma unroll
@@ -593,7 +626,14 @@ __global__ void __launch_bounds__(kBlock, ITEMS <= 2 ? 5 : ITEMS <= 4 ? 4 : 3)
     }
 #pragma unroll
     for (int j = 0; j < kItemsRec; ++j) cls[j] = keep[j] ? weight_class<NOUT>(rw[j], p) : 0xff;
-    seg_tile_finish<NOUT, kItemsRec>(cls, run, p, [&](uint32_t t) { return recs[t]; });
+    seg_tile_finish<NOUT, kItemsRec>(cls, run, p, [&](uint32_t t) { return recs[t]; }, s_min);
+  }
+  if (s_min) {  // one reduction per label this CTA touched
+    __syncthreads();
+    for (uint32_t x = threadIdx.x; x < p.smin_n; x += kBlock) {
+      const uint64_t v = s_min[x];
+      if (v != kInf64) red_min(&p.minval[x], v);
+    }
   }
   seg_pass_end<NOUT>(run, dropped_w, cand, p);
 }

@@ -108,6 +108,11 @@ static inline uint32_t ceil_div(uint64_t a, uint64_t b) {
 }
 
 constexpr uint32_t kSamples = 4096;
+// Round passes over at most this many vertices use 4-record tiles.
+constexpr uint32_t kWideRoundN = 1u << 16;
+// Largest next-round label count whose minima a list pass keeps per CTA in
+// shared memory (32 KB).
+constexpr uint32_t kSminMax = 4096;
 
 template <typename K>
 static int blocks_per_sm(K kernel, size_t dyn_smem) {
@@ -168,6 +173,8 @@ class Solve {
   // share of a chunk's items that can land in class c (1 = all); outputs are
   // (re)allocated here and resized exactly once on overflow.  minval (with
   // minval_n entries) receives the class-0 minimum.
+  // vertices of the round whose relabel pass runs (0 outside the rounds)
+  uint32_t round_nr_ = 0;
   template <int NOUT>
   kamsta_status pass(int phase, const SegList* src, const uint32_t* map, uint32_t wmin,
                      uint32_t wmax, const uint32_t* thr, SegList* const* outs, const double* frac,
@@ -452,9 +459,19 @@ kamsta_status Solve::pass(int phase, const SegList* src, const uint32_t* map, ui
   const bool dir = src == nullptr;
   const uint64_t total = dir ? md_ : src->total;
   const int items = (map != nullptr && dir_items_ == 8) ? kMappedDirItems : dir_items_;
-  const int sitems = seg_items_;
+  int sitems = seg_items_;
+  uint32_t smin_n = 0;
+  if (!dir && phase == KAMSTA_PHASE_ROUND_EDGES && round_nr_ > 0) {
+    // late rounds: their label map and minima sit in the L2, and a wider
+    // tile (4 records per thread) gained 0.1 ms per solve at 2^26/2^30
+    if (round_nr_ <= kWideRoundN && sitems < 4) sitems = 4;
+    // a round's live roots are at most half its vertices, so the next
+    // labels are below round_nr_ / 2: few enough to keep per CTA
+    if (minval && round_nr_ / 2 <= kSminMax) smin_n = std::max<uint32_t>(1, round_nr_ / 2);
+  }
   const uint32_t tile = dir ? dir_tile(items) : rec_tile(sitems);
-  const size_t dyn = dir ? dir_dyn_smem(items) : rec_dyn_smem(sitems);
+  const size_t dyn = dir ? dir_dyn_smem(items)
+                         : rec_dyn_smem(sitems) + round_up(size_t(smin_n) * 8, 16);
   const bool mapped = map != nullptr;
   const int per_sm =
       !dir ? (sitems == 2 ? blocks_per_sm(k_pass_seg<NOUT, 2>, dyn)
@@ -506,6 +523,7 @@ kamsta_status Solve::pass(int phase, const SegList* src, const uint32_t* map, ui
     a.n = n_;
     a.validate = validate ? 1 : 0;
     a.aligned16 = aligned16_ ? 1 : 0;
+    a.smin_n = smin_n;
     const int t0 = tick();
     bool launched = false;
     if (dir && !mapped && !input_complete_ && attempt == 0) {
@@ -727,8 +745,11 @@ kamsta_status Solve::rounds(SegList* L, bool own) {
     // relabel + self-loop removal + compaction + next-round minimum
     SegList* nxt = new_list();
     SegList* outs[1] = {nxt};
-    KS_TRY(pass<1>(KAMSTA_PHASE_ROUND_EDGES, cur, R, 0, 0xffffffffu, nullptr, outs, nullptr, minn,
-                   0, false));
+    round_nr_ = nr;
+    const kamsta_status ps = pass<1>(KAMSTA_PHASE_ROUND_EDGES, cur, R, 0, 0xffffffffu, nullptr,
+                                     outs, nullptr, minn, 0, false);
+    round_nr_ = 0;
+    KS_TRY(ps);
     const uint64_t n_next = ctx_->h_counters[kCVertex].cnt[0];
     const uint64_t added = ctx_->h_counters[kCVertex].cnt[1];
     // hook: minimum, record gather, partner minimum, parent + edge id;
@@ -1183,12 +1204,13 @@ kamsta_status Solve::run(Algo algo, kamsta_wedge* d_out, SolveOut* out) {
     KAMSTA_DIR_ATTR(2, 6, true, d6);
     KAMSTA_DIR_ATTR(3, 6, true, d6);
 #undef KAMSTA_DIR_ATTR
-    CU_TRY(cudaFuncSetAttribute(k_pass_seg<1, 8>, attr, dr));
+    // the round passes (one output) may add up to kSminMax shared minima
+    CU_TRY(cudaFuncSetAttribute(k_pass_seg<1, 8>, attr, dr + int(kSminMax) * 8));
     CU_TRY(cudaFuncSetAttribute(k_pass_seg<2, 8>, attr, dr));
     CU_TRY(cudaFuncSetAttribute(k_pass_seg<3, 8>, attr, dr));
-    CU_TRY(cudaFuncSetAttribute(k_pass_seg<1, 4>, attr, dr4));
+    CU_TRY(cudaFuncSetAttribute(k_pass_seg<1, 4>, attr, dr4 + int(kSminMax) * 8));
     const int dr2 = static_cast<int>(rec_dyn_smem(2));
-    CU_TRY(cudaFuncSetAttribute(k_pass_seg<1, 2>, attr, dr2));
+    CU_TRY(cudaFuncSetAttribute(k_pass_seg<1, 2>, attr, dr2 + int(kSminMax) * 8));
     CU_TRY(cudaFuncSetAttribute(k_pass_seg<2, 2>, attr, dr2));
     CU_TRY(cudaFuncSetAttribute(k_pass_seg<3, 2>, attr, dr2));
     CU_TRY(cudaFuncSetAttribute(k_pass_seg<2, 4>, attr, dr4));

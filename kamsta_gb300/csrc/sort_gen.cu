@@ -35,6 +35,10 @@ static cudaError_t radix_sort_impl(cudaStream_t st, uint64_t* keys, uint64_t* ke
                                    int* result_alt, int sms) {
   *result_alt = 0;
   if (n <= 1 || bits <= 0) return cudaSuccess;
+  // the per-tile digit offsets and the scan are 32-bit: refuse 2^32 or more
+  // keys rather than wrap (every caller sorts fewer: lists and generators
+  // stay below 2^32 entries)
+  if (n >= (1ull << 32)) return cudaErrorInvalidValue;
   const uint32_t nt = cdiv(n, kRsTile);
   const uint64_t ncounts = static_cast<uint64_t>(nt) * 256;
   const uint32_t nst = cdiv(ncounts, kScanTile);
