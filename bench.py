@@ -548,17 +548,21 @@ def run_serving(args, K, ctx, sh, b):
         res["load_points"] = sweep
         # saturation: the highest offered rate whose p99 stays under 50 ms
         sat = {}
-        for f in (0.75, 1.0, 1.25, 1.5, 2.0):
+        for f in (0.5, 0.6, 0.7, 0.8, 0.9, 1.0, 1.25, 1.5):
             r, _, _ = serve_once(args, K, b, f * b["graphs_per_s"], R // 4, args.seed + 41)
             sat[f"{f:.2f}x_batch_rate"] = {k: r[k] for k in
                                            ("rate_per_s", "throughput", "p50_ms", "p99_ms",
                                             "exact_vs_batch")}
-        ok = [v for v in sat.values() if v["p99_ms"] < 50.0]
+        allp = list(sat.values()) + [
+            {"rate_per_s": res["rate_per_s"], "throughput": res["throughput"],
+             "p99_ms": res["p99_ms"]}] + [v for v in sweep.values()]
+        ok = [v for v in allp if v["p99_ms"] < 50.0]
         res["saturation"] = {
-            "rule": "highest offered rate (Poisson, requests/4 each) whose p99 latency < 50 ms",
+            "rule": ("highest offered rate (Poisson) whose p99 latency < 50 ms, over these "
+                     "points (requests/4 each) and the load points above"),
             "rate_per_s": max((v["rate_per_s"] for v in ok), default=None),
             "throughput": max((v["throughput"] for v in ok), default=None),
-            "max_throughput_seen": max(v["throughput"] for v in sat.values()),
+            "max_throughput_seen": max(v["throughput"] for v in allp),
             "points": sat}
     # sequential plain solves under the same arrivals (FIFO, one at a time)
     cfg = K.AlgorithmConfig(local_preprocessing=K.LocalPreprocessing(args.local_preprocessing))
