@@ -68,6 +68,10 @@ def parse_args():
     p.add_argument("--serve-requests", type=int, default=20000)
     p.add_argument("--serve-rate", type=float, default=0.0,
                    help="Poisson arrival rate (requests/s); 0 = 0.35 x the batched graphs/s")
+    p.add_argument("--serve-workers", type=int, default=4,
+                   help="serving worker threads (4: lowest latency in a 2/3/4 sweep)")
+    p.add_argument("--serve-max-batch", type=int, default=0,
+                   help="jobs per serving wave at most (0 = the library default, 4096)")
     p.add_argument("--serve-plain-requests", type=int, default=2000,
                    help="requests replayed through sequential plain solves")
     return p.parse_args()
@@ -463,7 +467,7 @@ def run_batch(args, K, ctx, sh, seed):
 
 def serve_once(args, K, b, rate, R, seed):
     """R Poisson arrivals at `rate` drawn from the batch graphs, served by a
-    2-worker kamsta_server under the memory budget.  Returns the result dict
+    kamsta_server (args.serve_workers workers) under the memory budget.  Returns the result dict
     and the arrival times / graph indices (for the plain replay)."""
     import numpy as np
     import torch
@@ -479,7 +483,8 @@ def serve_once(args, K, b, rate, R, seed):
     base = out.data_ptr()
     cfg = K.AlgorithmConfig(local_preprocessing=K.LocalPreprocessing(args.local_preprocessing))
     srv = K.Server(torch.cuda.current_device(), budget_bytes=int(args.batch_budget_gb * (1 << 30)),
-                   workers=2, config=cfg, tuning=b.get("tuning"))
+                   workers=args.serve_workers, max_batch=args.serve_max_batch, config=cfg,
+                   tuning=b.get("tuning"))
     done = {}
     stop = threading.Event()
 
@@ -535,7 +540,8 @@ def run_serving(args, K, ctx, sh, b):
     rate = args.serve_rate or 0.35 * b["graphs_per_s"]
     res, arrivals, gidx = serve_once(args, K, b, rate, R, args.seed + 17)
     res = {"workload": f"{R} requests, Poisson arrivals, graphs drawn from the batch mix",
-           **res, "workers": 2, "budget_gb": args.batch_budget_gb,
+           **res, "workers": args.serve_workers, "max_batch": args.serve_max_batch or 4096,
+           "budget_gb": args.batch_budget_gb,
            "rate_rule": "0.35 x the batched graphs/s unless --serve-rate is given"}
     if not args.serve_rate:
         sweep = {}
