@@ -889,7 +889,14 @@ std::vector<uint32_t> Solve::plan_classes() {
   double m_est = static_cast<double>(md_) / 2.0;
   const double nv = static_cast<double>(n_);
   size_t len = s.size();
-  while (m_est > 3.0 * nv && len >= 16) {
+  // The split stops once the light part has at most 3n edges, the
+  // reference's rule; any stop gives the same forest.  The batch's disjoint
+  // unions (the only solves that mark the forest in a bitmap) stop at 2n:
+  // on 1024 mixed graphs 78.6 against 86.0 ms, while single graphs are
+  // fastest at 3n (GNM 2^26 deg 32 / deg 16, RGG-2D, RHG, R-MAT 2^24: 0-20%
+  // slower at 2n).
+  const double stop = forest_bits_ != nullptr ? 2.0 : 3.0;
+  while (m_est > stop * nv && len >= 16) {
     const uint32_t pivot = s[static_cast<size_t>(len * 0.25)];
     const size_t light =
         static_cast<size_t>(std::upper_bound(s.begin(), s.begin() + len, pivot) - s.begin());
