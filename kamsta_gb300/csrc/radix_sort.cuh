@@ -4,12 +4,14 @@
 // ips4o by (src, dst, w) and keeps the lightest, duplicate_detection.hpp:
 // 25-64) and by the device graph generators.
 //
-// Per 8-bit digit: (1) k_rs_upsweep: per-tile digit histograms, stored digit
-// major; (2) k_scan_u32: one exclusive scan of all histograms (decoupled
-// look-back) -> every (digit, tile) output offset; (3) k_rs_downsweep: each
-// warp ranks its rows of 32 keys stably (8 ballots give the lanes sharing a
-// digit), the tile is reordered by digit in shared memory and written out in
-// digit runs (coalesced).
+// Per 8-bit digit: (1) k_rs_upsweep: per-tile digit histograms in shared
+// memory from 128-bit key loads, stored digit major; (2) k_scan_u32: one
+// exclusive scan of all histograms (decoupled look-back) -> every (digit,
+// tile) output offset; (3) k_rs_downsweep: each warp ranks its rows of 32
+// keys stably (8 ballots give the lanes sharing a digit), the tile is
+// reordered by digit in shared memory and written out in digit runs
+// (coalesced).  The downsweep loads one key per lane (a warp load moves 256
+// contiguous bytes) because its ranking needs lane order = input order.
 #pragma once
 #include "common.cuh"
 
@@ -41,12 +43,25 @@ __global__ void __launch_bounds__(kRsBlock)
   for (uint32_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     hist[threadIdx.x] = 0;
     __syncthreads();
+    // 128-bit loads: thread t reads key pairs (2q, 2q+1) of the tile, q =
+    // j * kRsBlock + t; a tile starts on a 32 KB boundary of the key array
+    // (pool memory, 256-byte aligned), so every pair is 16-byte aligned
     const uint64_t base = static_cast<uint64_t>(tile) * kRsTile;
+    const ulonglong2* pairs = reinterpret_cast<const ulonglong2*>(keys + base);
 #pragma unroll 4
-    for (int j = 0; j < kRsItems; ++j) {
-      const uint64_t i = base + j * kRsBlock + threadIdx.x;
-      const uint64_t k = i < n ? keys[i] : ~0ull;  // pads sort last
-      atomicAdd(&hist[(k >> shift) & 255u], 1u);
+    for (int j = 0; j < kRsItems / 2; ++j) {
+      const uint64_t q = static_cast<uint64_t>(j) * kRsBlock + threadIdx.x;
+      const uint64_t i = base + 2 * q;
+      uint64_t k0 = ~0ull, k1 = ~0ull;  // pads sort last
+      if (i + 1 < n) {
+        const ulonglong2 kk = pairs[q];
+        k0 = kk.x;
+        k1 = kk.y;
+      } else if (i < n) {
+        k0 = keys[i];
+      }
+      atomicAdd(&hist[(k0 >> shift) & 255u], 1u);
+      atomicAdd(&hist[(k1 >> shift) & 255u], 1u);
     }
     __syncthreads();
     counts[static_cast<uint64_t>(threadIdx.x) * ntiles + tile] = hist[threadIdx.x];

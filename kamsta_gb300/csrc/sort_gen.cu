@@ -39,6 +39,9 @@ static cudaError_t radix_sort_impl(cudaStream_t st, uint64_t* keys, uint64_t* ke
   // keys rather than wrap (every caller sorts fewer: lists and generators
   // stay below 2^32 entries)
   if (n >= (1ull << 32)) return cudaErrorInvalidValue;
+  // the upsweep reads key pairs with 128-bit loads
+  if ((reinterpret_cast<uintptr_t>(keys) | reinterpret_cast<uintptr_t>(keys_alt)) & 15u)
+    return cudaErrorMisalignedAddress;
   const uint32_t nt = cdiv(n, kRsTile);
   const uint64_t ncounts = static_cast<uint64_t>(nt) * 256;
   const uint32_t nst = cdiv(ncounts, kScanTile);
