@@ -146,13 +146,19 @@ __device__ __forceinline__ uint32_t next_tile(uint32_t* ticket) {
 
 // A next-round minimum update into the CTA's shared minima; a label beyond
 // them (not expected: the host sizes them for every label the round can
-// produce) goes to the global word.
+// produce) goes to the global word.  The shared word is read first: with a
+// handful of labels left, every lane of a warp updates one of a few words,
+// and the atomics on one word serialise, while once a CTA has seen a few
+// tiles nearly every candidate is above its minimum.
 __device__ __forceinline__ void smin_update(const PassArgs& p, uint64_t* smin, uint32_t x,
                                             uint64_t v) {
-  if (x < p.smin_n)
-    atomicMin(reinterpret_cast<unsigned long long*>(smin + x), static_cast<unsigned long long>(v));
-  else
+  if (x < p.smin_n) {
+    unsigned long long* s = reinterpret_cast<unsigned long long*>(smin + x);
+    if (v < *reinterpret_cast<volatile unsigned long long*>(s))
+      atomicMin(s, static_cast<unsigned long long>(v));
+  } else {
     red_min(&p.minval[x], v);
+  }
 }
 
 // Rank the tile's kept items (stable), append them to this CTA's output
