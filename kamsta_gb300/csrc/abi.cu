@@ -75,9 +75,10 @@ kamsta_status solve_host_7bit(Algo algo, const kamsta_wedge* edges, uint64_t m, 
                               kamsta_cfg c, kamsta_wedge* out, uint64_t* out_count,
                               kamsta_stats* stats);
 
-// Host-to-device copy of a large input as pieces alternating between the
-// context's two streams (two copy engines in flight); the main stream waits
-// for both before the solve.
+// Host-to-device copy of a large input in pieces on the context's second
+// stream, an event after each: the first pass's CTA groups wait only for the
+// piece that holds their chunks (one stream is enough: the host link gives
+// the same rate to one copy as to several).
 kamsta_status solve_host(Algo algo, const kamsta_wedge* edges, uint64_t m, uint32_t n,
                          const kamsta_cfg* cfg, kamsta_wedge* out, uint64_t* out_count,
                          kamsta_stats* stats) {
