@@ -37,7 +37,7 @@ namespace kamsta {
 namespace {
 
 constexpr int kBatchBlock = 256;
-constexpr int kGatherWords = 16;  // u32 words per thread in k_batch_gather
+constexpr int kGatherWords = 16;  // u32 words per thread and step in k_batch_gather
 constexpr uint32_t kSkipId = 0xffffffffu;
 
 // Device-side wave table (structure of arrays, one allocation).
@@ -63,9 +63,14 @@ __device__ __forceinline__ uint32_t upper_graph(const uint64_t* off, uint32_t G,
   return lo;
 }
 
-// Union words [c0, c1) per CTA; thread-strided inside the chunk so that each
-// warp reads and writes 128 contiguous bytes per step.  Words 0 and 1 of an
-// entry are ids (shifted by voff), word 2 the weight.
+// Union words [c0, c0 + chunk) per CTA; thread-strided inside the chunk so
+// that each warp reads and writes 128 contiguous bytes per step.  Words 0
+// and 1 of an entry are ids (shifted by voff), word 2 the weight.  A chunk
+// inside one graph (nearly all: the union's graphs hold tens of thousands
+// of words or more) issues all of a thread's kGatherWords loads before the
+// first store; a chunk across graph boundaries resolves each word's graph
+// on the way.  The union offset of a graph is a multiple of 3 words, so a
+// word's place in its entry is q mod 3.
 __global__ void __launch_bounds__(kBatchBlock)
     k_batch_gather(WaveTable t, uint32_t* __restrict__ uni, uint64_t words) {
   __shared__ uint32_t s_g0;
@@ -78,20 +83,42 @@ __global__ void __launch_bounds__(kBatchBlock)
     }
     __syncthreads();
     uint32_t g = s_g0;
-    uint64_t gend = 3 * t.eoff[g + 1];
     uint64_t gbeg = 3 * t.eoff[g];
-#pragma unroll 4
-    for (int j = 0; j < kGatherWords; ++j) {
-      const uint64_t q = c0 + static_cast<uint64_t>(j) * kBatchBlock + threadIdx.x;
+    uint64_t gend = 3 * t.eoff[g + 1];
+    const uint64_t q0 = c0 + threadIdx.x;
+    const uint32_t r0 = static_cast<uint32_t>(q0 % 3);  // kBatchBlock = 1 (mod 3)
+    if (c0 + chunk <= gend) {  // the whole chunk in graph g (the same in every thread)
+      const uint32_t* src = t.edges[g] + (q0 - gbeg);
+      const uint32_t add = static_cast<uint32_t>(t.voff[g]), lim = t.n[g];
+      uint32_t v[kGatherWords];
+#pragma unroll
+      for (int j = 0; j < kGatherWords; ++j) v[j] = __ldcs(src + j * kBatchBlock);
+      uint32_t r = r0;
+      bool bad = false;
+#pragma unroll
+      for (int j = 0; j < kGatherWords; ++j) {
+        uint32_t x = v[j];
+        if (r != 2) {
+          bad |= x >= lim;
+          x = x >= lim ? kSkipId : x + add;
+        }
+        uni[q0 + j * kBatchBlock] = x;
+        r = r == 2 ? 0u : r + 1u;
+      }
+      if (bad) atomicOr(&t.err[g], 1u);
+      continue;
+    }
+    uint32_t r = r0;
+    for (int j = 0; j < kGatherWords; ++j, r = r == 2 ? 0u : r + 1u) {
+      const uint64_t q = q0 + static_cast<uint64_t>(j) * kBatchBlock;
       if (q >= words) break;
       while (q >= gend) {
         ++g;
         gbeg = gend;
         gend = 3 * t.eoff[g + 1];
       }
-      const uint64_t local = q - gbeg;
-      uint32_t v = t.edges[g][local];
-      if (local % 3 != 2) {
+      uint32_t v = t.edges[g][q - gbeg];
+      if (r != 2) {
         if (v >= t.n[g]) {
           atomicOr(&t.err[g], 1u);
           v = kSkipId;
@@ -139,14 +166,21 @@ __global__ void k_batch_bounds(WaveTable t, const uint32_t* __restrict__ bits,
 // at that position); it goes, un-shifted, to its graph's output at its rank
 // minus the graph's first rank, so every graph's forest is in input order,
 // i.e. sorted by (src, dst).  Weights are summed per graph (one atomic per
-// warp when the warp's edges share a graph).
+// warp when the warp's edges share a graph).  The graph of the block's first
+// position is searched once per block step; a thread walks on from it (the
+// union's graphs are larger than a step's 8192 positions, so a step crosses
+// at most a boundary or two).
 __global__ void __launch_bounds__(kBatchBlock)
     k_batch_scatter(WaveTable t, const uint32_t* __restrict__ uni,
                     const uint32_t* __restrict__ bits, const uint32_t* __restrict__ pre,
                     uint64_t W) {
+  __shared__ uint32_t s_g;
   const uint32_t lane = threadIdx.x & 31;
   for (uint64_t base = blockIdx.x * static_cast<uint64_t>(blockDim.x); base < W;
        base += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_g = upper_graph(t.eoff, t.G, base * 32);
+    __syncthreads();
     const uint64_t q = base + threadIdx.x;
     uint32_t f = q < W ? bits[q] : 0u;
     uint32_t g0 = 0xffffffffu;
@@ -154,7 +188,8 @@ __global__ void __launch_bounds__(kBatchBlock)
     if (f) {
       uint32_t rank = pre[q];
       uint64_t pos = q * 32 + (__ffs(f) - 1);
-      uint32_t g = upper_graph(t.eoff, t.G, pos);
+      uint32_t g = s_g;
+      while (pos >= t.eoff[g + 1]) ++g;
       g0 = g;
       while (f) {
         const uint32_t b = __ffs(f) - 1;

@@ -1610,19 +1610,15 @@ __global__ void k_emit(uint64_t k, const uint32_t* __restrict__ msf,
 }
 
 // Forest as a bitmap over input positions (batch split): bit oid of every
-// forest edge is set, and the weights are summed.
+// forest edge is set.  The caller's split reads each marked entry anyway and
+// sums the weights per graph, so no weight is gathered here.
 __global__ void k_mark_forest(uint64_t k, const uint32_t* __restrict__ msf,
-                              const uint32_t* __restrict__ in_words, uint32_t* __restrict__ bits,
-                              unsigned long long* weight) {
-  uint64_t local = 0;
+                              uint32_t* __restrict__ bits) {
   for (uint64_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k;
        i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
     const uint32_t oid = msf[i];
     atomicOr(&bits[oid >> 5], 1u << (oid & 31));
-    local += in_words[3ull * oid + 2];
   }
-  local = warp_sum(local);
-  if (lane_id() == 0 && local) atomicAdd(weight, static_cast<unsigned long long>(local));
 }
 
 // Weight samples for pivot selection: sample i reads the weight of the input

@@ -1257,10 +1257,10 @@ kamsta_status Solve::run(Algo algo, kamsta_wedge* d_out, SolveOut* out) {
   CU_TRY(cudaMemsetAsync(ctx_->d_counters + kCMisc, 0, sizeof(DevCounters), st_));
   if (msf_count_ > 0 && forest_bits_) {
     const int tm = tick();
-    k_mark_forest<<<grid_for(msf_count_), kBlock, 0, st_>>>(msf_count_, msf_, in_, forest_bits_,
-                                                             &ctx_->d_counters[kCMisc].weight);
+    // the weight stays 0 here: the caller's split sums it per graph
+    k_mark_forest<<<grid_for(msf_count_), kBlock, 0, st_>>>(msf_count_, msf_, forest_bits_);
     tock(KAMSTA_PHASE_EMIT, tm);
-    account(KAMSTA_PHASE_EMIT, msf_count_ * (4 + 4 + 8), 1);
+    account(KAMSTA_PHASE_EMIT, msf_count_ * (4 + 4 + 4), 1);
   } else if (msf_count_ > 0) {
     // edges [0, direct_count_) are in d_out already; k_emit adds their weight
     const uint64_t k0 = direct_count_;

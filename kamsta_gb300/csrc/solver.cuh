@@ -107,7 +107,8 @@ struct HostIo {
 // Solves one graph whose directed, (src,dst)-sorted input lies in device
 // memory.  Writes the forest to d_out (device, capacity >= n-1), or, when
 // d_forest_bits is given (zeroed, one bit per input entry), sets the bit of
-// the src<dst input copy of every forest edge instead.
+// the src<dst input copy of every forest edge instead (out->weight is then
+// 0: the caller reads the marked entries).
 kamsta_status solve_device(kamsta_ctx* ctx, Algo algo, const kamsta_wedge* d_in,
                            uint64_t m_directed, uint32_t n, const kamsta_cfg& cfg,
                            kamsta_wedge* d_out, SolveOut* out, kamsta_stats* st,
