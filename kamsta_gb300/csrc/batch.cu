@@ -13,7 +13,7 @@
 //   k_batch_order    (KAMSTA_FLAG_VALIDATE) per-graph (src,dst) order check
 //   solve_device     the single-graph solver over the union; the forest comes
 //                    back as one bit per union entry (its src<dst copy)
-//   k_batch_popc + scan  rank of every set bit
+//   k_batch_rank     rank of every set bit (word popcounts, one scan pass)
 //   k_batch_bounds   first rank of every graph
 //   k_batch_scatter  each forest edge, un-shifted, to its graph's output at
 //                    its rank: input order, i.e. sorted by (src, dst); per-
@@ -145,11 +145,91 @@ __global__ void __launch_bounds__(kBatchBlock)
   }
 }
 
-__global__ void k_batch_popc(const uint32_t* __restrict__ bits, uint64_t W,
-                             uint32_t* __restrict__ pc) {
-  for (uint64_t q = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; q < W;
-       q += static_cast<uint64_t>(gridDim.x) * blockDim.x)
-    pc[q] = __popc(bits[q]);
+// pre[q] = set bits in words [0, q) of the forest bitmap: one pass, the word
+// popcounts scanned with a decoupled look-back over tiles of kRankTile words
+// taken in ticket order.  A thread reads 16 consecutive words as four
+// 16-byte loads (the bitmap and every tile start are 64-byte aligned).
+constexpr int kRankItems = 16;
+constexpr uint32_t kRankTile = kBatchBlock * kRankItems;
+
+__global__ void __launch_bounds__(kBatchBlock)
+    k_batch_rank(const uint32_t* __restrict__ bits, uint64_t W, uint32_t* __restrict__ pre,
+                 uint64_t* status, uint32_t* ticket, uint32_t ntiles, uint32_t* err) {
+  __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_warp[kBatchBlock / 32];
+  __shared__ uint64_t s_pre;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    if (tile >= ntiles) return;
+    const uint64_t base = static_cast<uint64_t>(tile) * kRankTile + threadIdx.x * kRankItems;
+    uint32_t v[kRankItems];
+    if (base + kRankItems <= W) {
+      const uint4* p = reinterpret_cast<const uint4*>(bits + base);
+#pragma unroll
+      for (int k = 0; k < kRankItems / 4; ++k) {
+        const uint4 x = p[k];
+        v[4 * k] = __popc(x.x);
+        v[4 * k + 1] = __popc(x.y);
+        v[4 * k + 2] = __popc(x.z);
+        v[4 * k + 3] = __popc(x.w);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < kRankItems; ++j) v[j] = base + j < W ? __popc(bits[base + j]) : 0u;
+    }
+    uint32_t sum = 0;
+#pragma unroll
+    for (int j = 0; j < kRankItems; ++j) sum += v[j];
+    const uint32_t lane = lane_id(), warp = threadIdx.x >> 5;
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFull, incl, o);
+      if (lane >= static_cast<uint32_t>(o)) incl += y;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+      const uint32_t wv = lane < kBatchBlock / 32 ? s_warp[lane] : 0u;
+      uint32_t wi = wv;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(kFull, wi, o);
+        if (lane >= static_cast<uint32_t>(o)) wi += y;
+      }
+      const uint32_t total = __shfl_sync(kFull, wi, kBatchBlock / 32 - 1);
+      if (lane < kBatchBlock / 32) s_warp[lane] = wi - wv;
+      const uint64_t tpre = lookback(status, tile, total, err);
+      if (lane == 0) s_pre = tpre;
+    }
+    __syncthreads();
+    uint32_t run = static_cast<uint32_t>(s_pre) + s_warp[warp] + (incl - sum);
+    if (base + kRankItems <= W) {
+      uint4* o = reinterpret_cast<uint4*>(pre + base);
+#pragma unroll
+      for (int k = 0; k < kRankItems / 4; ++k) {
+        uint4 x;
+        x.x = run;
+        run += v[4 * k];
+        x.y = run;
+        run += v[4 * k + 1];
+        x.z = run;
+        run += v[4 * k + 2];
+        x.w = run;
+        run += v[4 * k + 3];
+        o[k] = x;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < kRankItems; ++j) {
+        if (base + j < W) pre[base + j] = run;
+        run += v[j];
+      }
+    }
+  }
 }
 
 // begin[g] = forest edges of the graphs before g: set bits before eoff[g]
@@ -192,23 +272,43 @@ __global__ void __launch_bounds__(kBatchBlock)
       while (pos >= t.eoff[g + 1]) ++g;
       g0 = g;
       while (f) {
-        const uint32_t b = __ffs(f) - 1;
-        f &= f - 1;
-        pos = q * 32 + b;
-        while (pos >= t.eoff[g + 1]) ++g;
-        const uint32_t* e = uni + 3 * pos;
-        const uint32_t v = static_cast<uint32_t>(t.voff[g]);
-        const uint32_t wt = e[2];
-        uint32_t* o = t.out[g] + 3 * (rank - t.begin[g]);
-        o[0] = e[0] - v;
-        o[1] = e[1] - v;
-        o[2] = wt;
-        ++rank;
-        if (g == g0) {
-          w0 += wt;
-        } else {
-          atomicAdd(reinterpret_cast<unsigned long long*>(&t.weight[g]),
-                    static_cast<unsigned long long>(wt));
+        // up to four of the word's edges with their entry loads in flight
+        constexpr int kB = 4;
+        uint64_t ps[kB];
+        uint32_t e0[kB], e1[kB], e2[kB];
+        int c = 0;
+#pragma unroll
+        for (int k = 0; k < kB; ++k) {
+          if (!f) break;
+          ps[k] = q * 32 + (__ffs(f) - 1);
+          f &= f - 1;
+          c = k + 1;
+        }
+#pragma unroll
+        for (int k = 0; k < kB; ++k) {
+          if (k >= c) break;
+          const uint32_t* e = uni + 3 * ps[k];
+          e0[k] = e[0];
+          e1[k] = e[1];
+          e2[k] = e[2];
+        }
+#pragma unroll
+        for (int k = 0; k < kB; ++k) {
+          if (k >= c) break;
+          while (ps[k] >= t.eoff[g + 1]) ++g;
+          const uint32_t v = static_cast<uint32_t>(t.voff[g]);
+          const uint32_t wt = e2[k];
+          uint32_t* o = t.out[g] + 3 * (rank - t.begin[g]);
+          o[0] = e0[k] - v;
+          o[1] = e1[k] - v;
+          o[2] = wt;
+          ++rank;
+          if (g == g0) {
+            w0 += wt;
+          } else {
+            atomicAdd(reinterpret_cast<unsigned long long*>(&t.weight[g]),
+                      static_cast<unsigned long long>(wt));
+          }
         }
       }
     }
@@ -525,7 +625,7 @@ kamsta_status solve_union(kamsta_ctx* ctx, Algo algo, kamsta_graph_desc* g, uint
   ucfg.flags &= ~(KAMSTA_FLAG_VALIDATE | KAMSTA_FLAG_SORT_OUTPUT);
   // the forest comes back as one bit per union entry (its src<dst copy)
   const uint64_t W = (M + 31) / 32;
-  PoolBuf bb, pcb, preb, stb;
+  PoolBuf bb, preb, stb;
   B_TRY(bb.alloc(ctx, sizeof(uint32_t) * (W + 1), st));
   uint32_t* bits = static_cast<uint32_t*>(bb.p);
   B_TRY(cudaMemsetAsync(bits, 0, sizeof(uint32_t) * (W + 1), st));
@@ -537,18 +637,17 @@ kamsta_status solve_union(kamsta_ctx* ctx, Algo algo, kamsta_graph_desc* g, uint
   ws->solve_ms = sst.device_ms;
   // ---- split: ranks of the set bits (word popcounts + exclusive scan), the
   // first rank of every graph, then every forest edge to its graph's output
-  B_TRY(pcb.alloc(ctx, sizeof(uint32_t) * (W + 1), st));
+  const uint32_t ntiles = static_cast<uint32_t>((W + 1 + kRankTile - 1) / kRankTile);
   B_TRY(preb.alloc(ctx, sizeof(uint32_t) * (W + 1), st));
-  B_TRY(stb.alloc(ctx, sizeof(uint64_t) * ((W + 1) / 2048 + 2), st));
-  uint32_t* pc = static_cast<uint32_t*>(pcb.p);
+  B_TRY(stb.alloc(ctx, sizeof(uint64_t) * (ntiles + 1), st));
   uint32_t* pre = static_cast<uint32_t*>(preb.p);
   {
-    const uint32_t blocks = static_cast<uint32_t>(
-        std::min<uint64_t>((W + 1 + kBatchBlock - 1) / kBatchBlock, sms * 8ull));
-    k_batch_popc<<<blocks, kBatchBlock, 0, st>>>(bits, W + 1, pc);
-    B_TRY(exclusive_scan_u32(st, pc, pre, W + 1, static_cast<uint64_t*>(stb.p),
-                             &ctx->d_counters[kCMisc].ticket, ctx->d_err, sms));
-    launches += 2;
+    B_TRY(cudaMemsetAsync(stb.p, 0, sizeof(uint64_t) * ntiles, st));
+    B_TRY(cudaMemsetAsync(&ctx->d_counters[kCMisc].ticket, 0, sizeof(uint32_t), st));
+    k_batch_rank<<<std::min<uint32_t>(ntiles, sms * 4u), kBatchBlock, 0, st>>>(
+        bits, W + 1, pre, static_cast<uint64_t*>(stb.p), &ctx->d_counters[kCMisc].ticket,
+        ntiles, ctx->d_err);
+    ++launches;
   }
   B_TRY(cudaMemsetAsync(d + o_weight, 0, sizeof(uint64_t) * G, st));
   k_batch_bounds<<<(G + 1 + kBatchBlock - 1) / kBatchBlock, kBatchBlock, 0, st>>>(t, bits, pre);
