@@ -1,5 +1,10 @@
 """The benchmark configurations at their stated sizes, against the oracle.
 
+* Headline configuration: GNM n = 2^26, m = 2^30 (the bench's input, seed
+  2026, weights 1..254), generated on the device and solved by boruvka and
+  filter_boruvka with local preprocessing; each forest must equal, edge for
+  edge, the reference's own build (oracle/_ref, every vertex local) where it
+  is built, else the oracle's Kruskal.
 * Geometric / skewed configuration: RGG-2D and RHG (gamma 3) with n = 2^24
   vertices and average degree 16 -- the bench's exact inputs (seed 2026),
   generated on the device -- solved by filter_boruvka with and without local
@@ -23,6 +28,34 @@ SEED = 2026
 
 def _host(d, md, kamsta):
     return d[:md].cpu().numpy().view(np.uint32).reshape(-1).view(kamsta.WEDGE)
+
+
+def test_headline_config_at_full_size(kamsta, oracle):
+    import torch
+    ctx = kamsta.Context(0)
+    n, m = 1 << 26, 1 << 30
+    d = torch.empty((2 * m, 3), dtype=torch.int32, device="cuda")
+    md = ctx.gen_gnm_dev(n, m, SEED, 254, d.data_ptr())
+    o = torch.empty((n, 3), dtype=torch.int32, device="cuda")
+    cfg = kamsta.AlgorithmConfig(local_preprocessing=kamsta.LocalPreprocessing.MODIFIED_BORUVKA)
+    got = {}
+    for name, fn in (("boruvka", ctx.boruvka_dev), ("filter_boruvka", ctx.filter_boruvka_dev)):
+        st = {}
+        k = fn(d.data_ptr(), md, n, o.data_ptr(), cfg, stats=st)
+        got[name] = (oracle.canon_keys(_host(o, k, kamsta)), st["total_weight"])
+    e = _host(d, md, kamsta)
+    del d, o
+    torch.cuda.empty_cache()
+    ctx.close()
+    if oracle.ref_available():
+        ref, rw, _ = oracle.ref_all_local(e, n)
+    else:
+        ref, rw = oracle.kruskal(e, n)
+    want = oracle.canon_keys(ref)
+    del e, ref
+    for name, (keys, w) in got.items():
+        assert w == rw, name
+        assert np.array_equal(keys, want), name
 
 
 @pytest.mark.parametrize("fam", ["rgg2d", "rhg"])
