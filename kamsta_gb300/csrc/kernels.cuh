@@ -161,6 +161,13 @@ __device__ __forceinline__ void smin_update(const PassArgs& p, uint64_t* smin, u
   }
 }
 
+// A kept record to its output segment with an L2 evict-first hint: the
+// lists are streamed once per pass, and the gathered label and minimum arrays
+// of the same pass keep the L2.
+__device__ __forceinline__ void st_stream(Rec* dst, const Rec& r) {
+  __stcs(reinterpret_cast<uint4*>(dst), make_uint4(r.a, r.b, r.w, r.oid));
+}
+
 // Rank the tile's kept items (stable), append them to this CTA's output
 // segments and feed the fused minimum.  rec(t) returns tile item t from
 // shared memory; run[] holds the CTA's running segment sizes (the same in
@@ -225,7 +232,7 @@ __device__ __forceinline__ void seg_tile_finish(const uint8_t (&cls)[ITEMS],
           continue;
         }
         r[k] = rec(s_dense[cbase[c] + i]);
-        sg[run0 + i] = r[k];
+        st_stream(sg + run0 + i, r[k]);
       }
       if (c != 0 || p.minval == nullptr || p.min_partner) continue;
       if (smin) {  // per-CTA minima (labels < p.smin_n)
@@ -264,7 +271,7 @@ __device__ __forceinline__ void seg_tile_finish(const uint8_t (&cls)[ITEMS],
           continue;
         }
         const Rec r = rec(s_dense[cbase[c] + i]);
-        sg[local] = r;
+        st_stream(sg + local, r);
         if (c != 0 || p.minval == nullptr || p.min_partner) continue;
         const uint64_t v = (static_cast<uint64_t>(r.w) << 32) | (seg0 + i);
         if (smin) {
