@@ -174,7 +174,9 @@ class Compressed:
     prev_src), varint(dst), varint(w) per edge (the reference's
     SEVEN_BIT_DIFF_ENCODING container)."""
 
-    def __init__(self, edges, n: int, chunk_edges: int = 2048):
+    def __init__(self, edges, n: int, chunk_edges: int = 2048, pinned: bool = False):
+        """pinned: the compressed bytes go to page-locked host memory (torch),
+        so that their copy to the device runs at the host link's rate."""
         e = as_wedges(edges)
         self.m, self.n, self.chunk_edges = len(e), int(n), int(chunk_edges)
         self.num_chunks = (self.m + self.chunk_edges - 1) // self.chunk_edges
@@ -185,7 +187,12 @@ class Compressed:
         ep = e.ctypes.data if len(e) else None
         check(L.kamsta_encode_7bit(ep, self.m, self.chunk_edges, self.offset.ctypes.data, None,
                                    None, 0, C.byref(nb)))
-        self.data = np.empty(max(nb.value, 1), np.uint8)
+        if pinned:
+            import torch
+            self._pin = torch.empty(max(nb.value, 1), dtype=torch.uint8, pin_memory=True)
+            self.data = self._pin.numpy()
+        else:
+            self.data = np.empty(max(nb.value, 1), np.uint8)
         check(L.kamsta_encode_7bit(ep, self.m, self.chunk_edges, self.offset.ctypes.data,
                                    self.first.ctypes.data, self.data.ctypes.data, nb.value,
                                    C.byref(nb)))

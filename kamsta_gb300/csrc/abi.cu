@@ -267,39 +267,115 @@ kamsta_status solve_cgraph_host(Algo algo, const kamsta_cgraph* g, kamsta_cfg c,
     if (stats) std::memset(stats, 0, sizeof(*stats));
     return KAMSTA_OK;
   }
-  // compressed bytes, chunk table and the forest in the context's io arena
+  // compressed bytes, chunk table, the forest and a decode error word in the
+  // context's io arena
   const size_t ob = (sizeof(uint64_t) * (g->num_chunks + 1) + 255) & ~size_t(255);
   const size_t fb = (sizeof(kamsta_wedge) * g->num_chunks + 255) & ~size_t(255);
   const size_t db = (g->data_bytes + 255) & ~size_t(255);
   const size_t outb = std::max<uint64_t>(g->n, 1) * sizeof(kamsta_wedge);
-  cudaError_t e = ctx_reserve(ctx, ctx->io, ob + fb + db + outb + 1024);
+  cudaError_t e = ctx_reserve(ctx, ctx->io, ob + fb + db + outb + 2048);
   if (e != cudaSuccess) return cuda_status(e, "device buffers for compressed input");
+  // the chunk table is on the host: every chunk's bytes must lie inside data
+  bool layout = g->chunk_edges != 0 && g->chunk_edges <= kMaxChunkEdges &&
+                g->num_chunks == (g->m_directed + g->chunk_edges - 1) / g->chunk_edges &&
+                g->chunk_offset[g->num_chunks] <= g->data_bytes;
+  for (uint64_t k = 0; layout && k < g->num_chunks; ++k)
+    layout = g->chunk_offset[k] <= g->chunk_offset[k + 1];
+  if (!layout) {
+    set_error("decode_7bit: inconsistent chunk layout");
+    return KAMSTA_E_INPUT;
+  }
   kamsta_cgraph dg = *g;
   uint64_t* doff = ctx->io.take<uint64_t>(g->num_chunks + 1);
   kamsta_wedge* dfirst = ctx->io.take<kamsta_wedge>(g->num_chunks);
   uint8_t* ddata = ctx->io.take<uint8_t>(std::max<uint64_t>(g->data_bytes, 1));
   kamsta_wedge* dout = ctx->io.take<kamsta_wedge>(std::max<uint64_t>(g->n, 1));
-  cudaStream_t st = ctx->stream;
-  e = cudaMemcpyAsync(doff, g->chunk_offset, sizeof(uint64_t) * (g->num_chunks + 1),
-                      cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(dfirst, g->chunk_first, sizeof(kamsta_wedge) * g->num_chunks,
-                        cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess && g->data_bytes)
-    e = cudaMemcpyAsync(ddata, g->data, g->data_bytes, cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return cuda_status(e, "cudaMemcpyAsync(H2D)");
+  uint32_t* derr = ctx->io.take<uint32_t>(64);
+  cudaStream_t st = ctx->stream, cp = ctx->aux;
+  void* buf = nullptr;
+  e = ctx_alloc(ctx, &buf, g->m_directed * sizeof(kamsta_wedge), st);
+  if (e != cudaSuccess) return cuda_status(e, "decode buffer");
+  struct Free {
+    void* p;
+    cudaStream_t s;
+    ~Free() { cudaFreeAsync(p, s); }
+  } fr{buf, st};
+  kamsta_wedge* dec = static_cast<kamsta_wedge*>(buf);
   dg.chunk_offset = doff;
   dg.chunk_first = dfirst;
   dg.data = ddata;
-  uint64_t cnt = 0;
-  s = solve_7bit_locked(ctx, dg, c, dout, &cnt, stats, st, algo);
-  if (s != KAMSTA_OK) return s;
-  if (cnt) {
-    e = cudaMemcpyAsync(out, dout, cnt * sizeof(kamsta_wedge), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  // the compressed bytes in pieces on the second stream, an event after
+  // each; the solve's stream decodes piece k as soon as it has landed, while
+  // the next pieces are still being copied
+  e = cudaMemsetAsync(derr, 0, sizeof(uint32_t), st);
+  if (e == cudaSuccess) e = cudaEventRecord(ctx->ev_fork, st);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(cp, ctx->ev_fork, 0);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(doff, g->chunk_offset, sizeof(uint64_t) * (g->num_chunks + 1),
+                        cudaMemcpyHostToDevice, cp);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dfirst, g->chunk_first, sizeof(kamsta_wedge) * g->num_chunks,
+                        cudaMemcpyHostToDevice, cp);
+  if (e != cudaSuccess) return cuda_status(e, "cudaMemcpyAsync(H2D)");
+  const uint64_t nch = g->num_chunks, C = g->chunk_edges;
+  for (int k = 0; k < kInputPieces; ++k) {
+    const uint64_t c0 = nch * k / kInputPieces, c1 = nch * (k + 1) / kInputPieces;
+    const uint64_t b0 = g->chunk_offset[c0], b1 = g->chunk_offset[c1];
+    if (b1 > b0) e = cudaMemcpyAsync(ddata + b0, g->data + b0, b1 - b0, cudaMemcpyHostToDevice, cp);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->piece_ev[k], cp);
+    if (e != cudaSuccess) {
+      cudaStreamSynchronize(cp);
+      return cuda_status(e, "cudaMemcpyAsync(H2D)");
+    }
+  }
+  for (int k = 0; k < kInputPieces; ++k) {
+    const uint64_t c0 = nch * k / kInputPieces, c1 = nch * (k + 1) / kInputPieces;
+    e = cudaStreamWaitEvent(st, ctx->piece_ev[k], 0);
+    if (e != cudaSuccess) {
+      cudaStreamSynchronize(cp);
+      return cuda_status(e, "cudaStreamWaitEvent");
+    }
+    if (c1 <= c0) continue;
+    kamsta_cgraph pg = dg;
+    pg.chunk_offset = doff + c0;
+    pg.chunk_first = dfirst + c0;
+    pg.num_chunks = c1 - c0;
+    pg.m_directed = std::min<uint64_t>(g->m_directed, c1 * C) - c0 * C;
+    s = decode_7bit(pg, dec + c0 * C, derr, st);
+    if (s != KAMSTA_OK) {
+      cudaStreamSynchronize(cp);
+      return s;
+    }
+  }
+  e = cudaMemcpyAsync(ctx->h_err, derr, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_status(e, "decode");
+  if (*ctx->h_err) {
+    set_error("decode_7bit: malformed chunk (value count or length)");
+    return KAMSTA_E_INPUT;
+  }
+  // the decoded input is complete; the forest edges of the first round go
+  // back on the second stream while the solve goes on
+  HostIo io;
+  io.pieces = 0;
+  io.copy_stream = cp;
+  io.host_out = out;
+  io.ev_early = ctx->ev_early;
+  SolveOut so;
+  s = solve_device(ctx, algo, dec, g->m_directed, g->n, c, dout, &so, stats, st, nullptr, &io);
+  if (s != KAMSTA_OK) {
+    cudaStreamSynchronize(cp);  // no copy may outlive the call
+    return s;
+  }
+  if (so.count > io.early) {
+    e = cudaMemcpyAsync(out + io.early, dout + io.early,
+                        (so.count - io.early) * sizeof(kamsta_wedge), cudaMemcpyDeviceToHost, st);
     if (e != cudaSuccess) return cuda_status(e, "cudaMemcpyAsync(D2H)");
   }
-  *out_count = cnt;
+  e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(cp);
+  if (e != cudaSuccess) return cuda_status(e, "cudaStreamSynchronize");
+  *out_count = so.count;
   return KAMSTA_OK;
 }
 

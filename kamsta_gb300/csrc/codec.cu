@@ -30,8 +30,7 @@ namespace kamsta {
 
 namespace {
 
-constexpr uint32_t kMaxChunkEdges = 4096;
-constexpr int kDecBlock = 256;
+constexpr int kDecBlock = 512;
 
 inline uint32_t varint_len(uint64_t v) {
   uint32_t n = 1;
@@ -80,13 +79,37 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* excl, 
   return total;
 }
 
+// Continuation-bit positions (bit 7 of each byte) of window word q that
+// belong to the chunk, whose bytes are window bytes [skip, wend).
+__device__ __forceinline__ uint32_t chunk_bits(uint32_t q, uint32_t skip, uint32_t wend) {
+  uint32_t mask = 0x80808080u;
+  const uint32_t b = 4 * q;
+  if (b < skip) mask = skip - b >= 4 ? 0u : mask << (8 * (skip - b));
+  if (b + 4 > wend) mask &= wend <= b ? 0u : 0x80808080u >> (8 * (b + 4 - wend));
+  return mask;
+}
+
+// One chunk per CTA step:
+//   1. its bytes into shared memory (16-byte loads for the aligned middle);
+//   2. each thread counts the value terminators (bytes without bit 7) in its
+//      run of 4-byte words, and a block scan numbers the values;
+//   3. each thread walks its bytes once, in order, assembling values and
+//      emitting each at its terminator; the value whose first bytes belong
+//      to the thread before is completed from up to 9 bytes looked back;
+//   4. the srcs are restored from the deltas (a block scan of per-thread
+//      delta sums) in place of the deltas;
+//   5. the chunk's 3 * C words go out coalesced, 16 bytes per store where the
+//      output is aligned.
 __global__ void __launch_bounds__(kDecBlock)
     k_decode_7bit(const uint64_t* __restrict__ chunk_off, const kamsta_wedge* __restrict__ first,
                   const uint8_t* __restrict__ data, uint64_t m, uint32_t C, uint64_t nchunks,
                   uint32_t* __restrict__ out, uint32_t* err) {
   extern __shared__ __align__(16) unsigned char smem[];
-  uint32_t* vals = reinterpret_cast<uint32_t*>(smem);          // 3 * C values
-  uint8_t* bytes = smem + sizeof(uint32_t) * 3 * C;             // <= 15 * C bytes
+  uint32_t* vals = reinterpret_cast<uint32_t*>(smem);  // 3 * C values
+  // the chunk's bytes, placed as in a window that starts at the 16-byte
+  // boundary at or below the chunk's first byte (<= 15 * C + 16 bytes)
+  uint8_t* win = smem + ((sizeof(uint32_t) * 3 * C + 15) & ~size_t(15));
+  const uint32_t* wwin = reinterpret_cast<const uint32_t*>(win);
   __shared__ uint32_t s_warp[kDecBlock / 32 + 1];
   for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
     const uint64_t e0 = c * C;
@@ -98,31 +121,63 @@ __global__ void __launch_bounds__(kDecBlock)
       if (threadIdx.x == 0) atomicOr(err, kErrRange);
       continue;
     }
-    for (uint32_t i = threadIdx.x; i < nb; i += kDecBlock) bytes[i] = data[b0 + i];
+    // 16-byte loads for the aligned middle of the byte range, single bytes
+    // for its ragged ends; every load lies inside [b0, b0 + nb)
+    const uint64_t b1 = b0 + nb, a0 = b0 & ~15ull;
+    const uint64_t m0 = (b0 + 15) & ~15ull, m1 = b1 & ~15ull;
+    if (m0 < m1) {
+      const uint4* src = reinterpret_cast<const uint4*>(data + m0);
+      uint4* dst = reinterpret_cast<uint4*>(win + (m0 - a0));
+      for (uint32_t q = threadIdx.x; q < static_cast<uint32_t>((m1 - m0) / 16); q += kDecBlock)
+        dst[q] = src[q];
+      for (uint64_t x = b0 + threadIdx.x; x < m0; x += kDecBlock) win[x - a0] = data[x];
+      for (uint64_t x = m1 + threadIdx.x; x < b1; x += kDecBlock) win[x - a0] = data[x];
+    } else {
+      for (uint64_t x = b0 + threadIdx.x; x < b1; x += kDecBlock) win[x - a0] = data[x];
+    }
     __syncthreads();
-    // value index of every byte: terminators (no continuation bit) before it
-    const uint32_t per = (nb + kDecBlock - 1) / kDecBlock;
-    const uint32_t lo = threadIdx.x * per, hi = min(nb, lo + per);
+    const uint32_t skip = static_cast<uint32_t>(b0 - a0), wend = skip + nb;
+    const uint32_t nw = (wend + 3) / 4;
+    const uint32_t perw = (nw + kDecBlock - 1) / kDecBlock;
+    const uint32_t w_lo = min(nw, threadIdx.x * perw), w_hi = min(nw, w_lo + perw);
     uint32_t cnt = 0;
-    for (uint32_t i = lo; i < hi; ++i) cnt += (bytes[i] & 0x80) ? 0u : 1u;
+    for (uint32_t q = w_lo; q < w_hi; ++q)
+      cnt += __popc(~wwin[q] & chunk_bits(q, skip, wend));
     uint32_t vbase = 0;
     const uint32_t total = block_excl_scan(cnt, &vbase, s_warp);
     if (total != nv) {
       if (threadIdx.x == 0) atomicOr(err, kErrRange);
       continue;
     }
-    uint32_t v = vbase;
-    for (uint32_t i = lo; i < hi; ++i) {
-      if (bytes[i] & 0x80) continue;
-      uint32_t s = i;  // first byte of the value
-      while (s > 0 && (bytes[s - 1] & 0x80) && i - s < 9) --s;
-      uint64_t x = 0;
-      for (uint32_t k = s; k <= i; ++k) x |= static_cast<uint64_t>(bytes[k] & 0x7f) << (7 * (k - s));
-      vals[v++] = static_cast<uint32_t>(x);  // ids and weights are 32-bit: arithmetic mod 2^32
+    if (w_lo < w_hi) {
+      uint64_t acc = 0;
+      uint32_t sh = 0;
+      // bytes of the value that runs into this thread's words from before
+      const uint32_t s0 = 4 * w_lo;
+      uint32_t p = s0;
+      while (p > skip && (win[p - 1] & 0x80) && s0 - p < 9) --p;
+      for (uint32_t k = p; k < s0; ++k, sh += 7) acc |= static_cast<uint64_t>(win[k] & 0x7f) << sh;
+      uint32_t v = vbase;
+      for (uint32_t q = w_lo; q < w_hi; ++q) {
+        const uint32_t w = wwin[q];
+        const uint32_t in = chunk_bits(q, skip, wend);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          if (!((in >> (8 * j + 7)) & 1u)) continue;  // not a chunk byte
+          const uint32_t by = (w >> (8 * j)) & 0xffu;
+          if (sh < 64) acc |= static_cast<uint64_t>(by & 0x7fu) << sh;
+          sh += 7;
+          if (!(by & 0x80u)) {  // ids and weights are 32-bit: arithmetic mod 2^32
+            vals[v++] = static_cast<uint32_t>(acc);
+            acc = 0;
+            sh = 0;
+          }
+        }
+      }
     }
     __syncthreads();
     // src = first src + running sum of the deltas; thread t owns edges
-    // [1 + t*pe, 1 + (t+1)*pe)
+    // [1 + t*pe, 1 + (t+1)*pe) and overwrites their deltas with their srcs
     const uint32_t pe = (ce - 1 + kDecBlock - 1) / kDecBlock;
     const uint32_t a = 1 + threadIdx.x * pe, z = min(ce, a + pe);
     uint32_t dsum = 0;
@@ -131,18 +186,25 @@ __global__ void __launch_bounds__(kDecBlock)
     block_excl_scan(dsum, &dpre, s_warp);
     const kamsta_wedge f = first[c];
     uint32_t src = f.src + dpre;
-    if (threadIdx.x == 0) {
-      out[3 * e0] = f.src;
-      out[3 * e0 + 1] = f.dst;
-      out[3 * e0 + 2] = f.w;
-    }
     for (uint32_t e = a; e < z; ++e) {
       src += vals[3 * (e - 1)];
-      const uint64_t o = 3 * (e0 + e);
-      out[o] = src;
-      out[o + 1] = vals[3 * (e - 1) + 1];
-      out[o + 2] = vals[3 * (e - 1) + 2];
+      vals[3 * (e - 1)] = src;
     }
+    __syncthreads();
+    // the chunk's entries: its raw first edge, then the values
+    uint32_t* o = out + 3 * e0;
+    const uint32_t nwords = 3 * ce;
+    auto word = [&](uint32_t i) -> uint32_t {
+      return i >= 3 ? vals[i - 3] : i == 0 ? f.src : i == 1 ? f.dst : f.w;
+    };
+    uint32_t done = 0;
+    if ((reinterpret_cast<uintptr_t>(o) & 15) == 0) {
+      done = nwords & ~3u;
+      for (uint32_t q = threadIdx.x; q < nwords / 4; q += kDecBlock)
+        reinterpret_cast<uint4*>(o)[q] =
+            make_uint4(word(4 * q), word(4 * q + 1), word(4 * q + 2), word(4 * q + 3));
+    }
+    for (uint32_t i = done + threadIdx.x; i < nwords; i += kDecBlock) o[i] = word(i);
     __syncthreads();
   }
 }
@@ -219,7 +281,7 @@ kamsta_status decode_7bit(const kamsta_cgraph& g, kamsta_wedge* d_out, uint32_t*
     set_error("decode_7bit: inconsistent chunk layout");
     return KAMSTA_E_INPUT;
   }
-  const size_t smem = 27ull * g.chunk_edges + 64;
+  const size_t smem = ((12ull * g.chunk_edges + 15) & ~15ull) + 15ull * g.chunk_edges + 64;
   cudaError_t e = cudaFuncSetAttribute(k_decode_7bit, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        static_cast<int>(smem));
   if (e != cudaSuccess) return cuda_status(e, "cudaFuncSetAttribute(k_decode_7bit)");

@@ -82,7 +82,7 @@ def _graphs(oracle):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("chunk", [1, 7, 2048, 4096])
+@pytest.mark.parametrize("chunk", [1, 7, 333, 2048, 4095, 4096])
 def test_device_decode_roundtrip(kamsta, oracle, chunk):
     import torch
     ctx = kamsta.Context(0)
@@ -96,12 +96,15 @@ def test_device_decode_roundtrip(kamsta, oracle, chunk):
 
 
 @pytest.mark.gpu
-def test_solve_from_compressed_equals_plain(kamsta, oracle):
+@pytest.mark.parametrize("chunk", [5, 2048, 4096])
+def test_solve_from_compressed_equals_plain(kamsta, oracle, chunk):
+    """The host container goes to the device in pieces, each decoded as it
+    lands; the device container is decoded whole.  Same forest either way."""
     import torch
     ctx = kamsta.Context(0)
     from tests.test_parity_gpu import _check
     for name, e, n in _graphs(oracle):
-        cg = kamsta.Compressed(e, n)
+        cg = kamsta.Compressed(e, n, chunk)
         st = {}
         got = kamsta.boruvka_7bit(cg, kamsta.AlgorithmConfig(local_preprocessing=1), stats=st)
         _check(oracle, got, e, n)
@@ -127,6 +130,28 @@ def test_malformed_compressed_input_is_rejected(kamsta, oracle):
     assert ei.value.status == kamsta._native.E_INPUT
     # the context stays usable
     ctx.decode_7bit_dev(kamsta.Compressed(e, 1000, 256), d.data_ptr())
+
+
+@pytest.mark.gpu
+def test_malformed_compressed_host_input_is_rejected(kamsta, oracle):
+    """Through the host entry point: a value running into the next one, and
+    a chunk table whose byte offsets go backwards, are input errors."""
+    e = oracle.gen_gnm(1000, 5000, 2)
+    cg = kamsta.Compressed(e, 1000, 256)
+    seg = cg.data[int(cg.offset[1]):int(cg.offset[2])]
+    j = int(cg.offset[1]) + int(np.flatnonzero((seg & 0x80) == 0)[0])
+    cg.data[j] |= 0x80
+    with pytest.raises(kamsta.KamstaError) as ei:
+        kamsta.boruvka_7bit(cg)
+    assert ei.value.status == kamsta._native.E_INPUT
+    cg = kamsta.Compressed(e, 1000, 256)
+    cg.offset[2], cg.offset[3] = cg.offset[3], cg.offset[2]
+    with pytest.raises(kamsta.KamstaError) as ei:
+        kamsta.boruvka_7bit(cg)
+    assert ei.value.status == kamsta._native.E_INPUT
+    # the library stays usable
+    from tests.test_parity_gpu import _check
+    _check(oracle, kamsta.boruvka_7bit(kamsta.Compressed(e, 1000, 256)), e, 1000)
 
 
 @pytest.mark.gpu
