@@ -7,7 +7,9 @@ benchmarks/mst_benchmarks.hpp:84) -- on a seeded G(n, m) with weights uniform
 in [1, 254], stored in both directions (2^31 directed 12-byte entries).  A
 "step" is one full MSF solve; `value` = directed entries / solve time with the
 input already in HBM, `e2e` = the same through the host-buffer C ABI call
-(pinned host input, H2D + solve + D2H of the forest inside the timed region).
+(pinned host input, H2D + solve + D2H of the forest inside the timed region),
+`e2e_7bit` = the same graph held on the host in the reference's 7-bit
+difference encoding, through kamsta_mst_boruvka_7bit.
 The input (24 GiB) is far larger than L2, so no flush is needed between steps.
 
 --impl reference times the reference's own single-rank local filter-Boruvka,
