@@ -100,7 +100,9 @@ __device__ __forceinline__ uint32_t chunk_bits(uint32_t q, uint32_t skip, uint32
 //      delta sums) in place of the deltas;
 //   5. the chunk's 3 * C words go out coalesced, 16 bytes per store where the
 //      output is aligned.
-__global__ void __launch_bounds__(kDecBlock)
+// Two CTAs per SM at most (each holds up to 27 * C bytes of shared memory),
+// so up to 64 registers per thread are free.
+__global__ void __launch_bounds__(kDecBlock, 2)
     k_decode_7bit(const uint64_t* __restrict__ chunk_off, const kamsta_wedge* __restrict__ first,
                   const uint8_t* __restrict__ data, uint64_t m, uint32_t C, uint64_t nchunks,
                   uint32_t* __restrict__ out, uint32_t* err) {
@@ -150,13 +152,15 @@ __global__ void __launch_bounds__(kDecBlock)
       continue;
     }
     if (w_lo < w_hi) {
-      uint64_t acc = 0;
-      uint32_t sh = 0;
+      // ids and weights are 32-bit: a value is kept mod 2^32, so only its
+      // first five groups of 7 bits matter
+      uint32_t acc = 0, sh = 0;
       // bytes of the value that runs into this thread's words from before
       const uint32_t s0 = 4 * w_lo;
       uint32_t p = s0;
       while (p > skip && (win[p - 1] & 0x80) && s0 - p < 9) --p;
-      for (uint32_t k = p; k < s0; ++k, sh += 7) acc |= static_cast<uint64_t>(win[k] & 0x7f) << sh;
+      for (uint32_t k = p; k < s0; ++k, sh += 7)
+        if (sh < 32) acc |= static_cast<uint32_t>(win[k] & 0x7f) << sh;
       uint32_t v = vbase;
       for (uint32_t q = w_lo; q < w_hi; ++q) {
         const uint32_t w = wwin[q];
@@ -165,10 +169,10 @@ __global__ void __launch_bounds__(kDecBlock)
         for (int j = 0; j < 4; ++j) {
           if (!((in >> (8 * j + 7)) & 1u)) continue;  // not a chunk byte
           const uint32_t by = (w >> (8 * j)) & 0xffu;
-          if (sh < 64) acc |= static_cast<uint64_t>(by & 0x7fu) << sh;
+          if (sh < 32) acc |= (by & 0x7fu) << sh;
           sh += 7;
-          if (!(by & 0x80u)) {  // ids and weights are 32-bit: arithmetic mod 2^32
-            vals[v++] = static_cast<uint32_t>(acc);
+          if (!(by & 0x80u)) {
+            vals[v++] = acc;
             acc = 0;
             sh = 0;
           }
@@ -178,7 +182,8 @@ __global__ void __launch_bounds__(kDecBlock)
     __syncthreads();
     // src = first src + running sum of the deltas; thread t owns edges
     // [1 + t*pe, 1 + (t+1)*pe) and overwrites their deltas with their srcs
-    const uint32_t pe = (ce - 1 + kDecBlock - 1) / kDecBlock;
+    // (pe odd: the threads' words are 3 * pe apart, on distinct banks)
+    const uint32_t pe = ((ce - 1 + kDecBlock - 1) / kDecBlock) | 1u;
     const uint32_t a = 1 + threadIdx.x * pe, z = min(ce, a + pe);
     uint32_t dsum = 0;
     for (uint32_t e = a; e < z; ++e) dsum += vals[3 * (e - 1)];

@@ -76,7 +76,7 @@ struct PassArgs {
   uint32_t min_partner;
   uint64_t total;  // logical input items
   uint64_t chunk;  // logical items per CTA (a multiple of the tile size)
-  unsigned long long* counts;  // [0] dropped above wmax, [1] items that reached the map
+  unsigned long long* counts;  // [1] items that reached the label map ([0] unused)
   uint32_t* err;
   uint32_t n;         // ids must be < n (directed source)
   uint32_t validate;  // check id range and (src,dst) order (directed source)
@@ -293,21 +293,15 @@ __device__ __forceinline__ void seg_tile_finish(const uint8_t (&cls)[ITEMS],
 }
 
 template <int NOUT>
-__device__ __forceinline__ void seg_pass_end(const uint64_t (&run)[NOUT], uint32_t dropped_w,
-                                             uint32_t cand, const PassArgs& p) {
-  __shared__ uint32_t s_red[2];
-  if (threadIdx.x < 2) s_red[threadIdx.x] = 0;
+__device__ __forceinline__ void seg_pass_end(const uint64_t (&run)[NOUT], uint32_t cand,
+                                             const PassArgs& p) {
+  __shared__ uint32_t s_red;
+  if (threadIdx.x == 0) s_red = 0;
   __syncthreads();
-  const uint32_t d = warp_sum(dropped_w), c = warp_sum(cand);
-  if (lane_id() == 0) {
-    if (d) atomicAdd(&s_red[0], d);
-    if (c) atomicAdd(&s_red[1], c);
-  }
+  const uint32_t c = warp_sum(cand);
+  if (lane_id() == 0 && c) atomicAdd(&s_red, c);
   __syncthreads();
-  if (threadIdx.x == 0) {
-    if (s_red[0]) atomicAdd(&p.counts[0], static_cast<unsigned long long>(s_red[0]));
-    if (s_red[1]) atomicAdd(&p.counts[1], static_cast<unsigned long long>(s_red[1]));
-  }
+  if (threadIdx.x == 0 && s_red) atomicAdd(&p.counts[1], static_cast<unsigned long long>(s_red));
   // unclamped: a count above cap tells the host the exact size to retry with
   if (threadIdx.x < NOUT) p.out[threadIdx.x].count[seg_id(p)] = static_cast<uint32_t>(run[threadIdx.x]);
 }
@@ -361,7 +355,7 @@ __global__ void __launch_bounds__(kBlock, ITEMS <= 8 ? 4 : 3)
   uint64_t run[NOUT];
 #pragma unroll
   for (int c = 0; c < NOUT; ++c) run[c] = 0;
-  uint32_t dropped_w = 0, cand = 0;
+  uint32_t cand = 0;  // items that reached the label map (mapped passes)
   for (uint32_t k = 0; k < ntile; ++k) {
     const int stage = k & 1;
     uint32_t* words = s_words + stage * kDirStageWords;
@@ -416,12 +410,7 @@ __global__ void __launch_bounds__(kBlock, ITEMS <= 8 ? 4 : 3)
         // tile's updates go to a few consecutive addresses
         if (p.min_partner && in_w && weight_class<NOUT>(wt, p) == 0)
           red_min(&p.minval[s], (static_cast<uint64_t>(wt) << 32) | d);
-        if (!(s < d)) continue;
-        if (!in_w) {
-          dropped_w += (wt > p.wmax) ? 1u : 0u;
-          continue;
-        }
-        ++cand;
+        if (!(s < d) || !in_w) continue;
         cls[j] = weight_class<NOUT>(wt, p);
       }
     } else {
@@ -435,10 +424,7 @@ __global__ void __launch_bounds__(kBlock, ITEMS <= 8 ? 4 : 3)
         ww[j] = words[3 * t + 2];
         keep[j] = false;
         if (t >= cnt || !(ss[j] < dd[j]) || dd[j] >= p.n) continue;
-        if (ww[j] < p.wmin || ww[j] > p.wmax) {
-          dropped_w += (ww[j] > p.wmax) ? 1u : 0u;
-          continue;
-        }
+        if (ww[j] < p.wmin || ww[j] > p.wmax) continue;
         ++cand;
         keep[j] = true;
       }
@@ -464,7 +450,7 @@ __global__ void __launch_bounds__(kBlock, ITEMS <= 8 ? 4 : 3)
     };
     seg_tile_finish<NOUT, kItemsDir>(cls, run, p, rec_at);
   }
-  seg_pass_end<NOUT>(run, dropped_w, cand, p);
+  seg_pass_end<NOUT>(run, cand, p);
 }
 
 // Edge pass over a segmented Rec list.  Tile k of a CTA covers logical
@@ -588,7 +574,7 @@ __global__ void __launch_bounds__(kBlock, ITEMS <= 2 ? 5 : ITEMS <= 4 ? 4 : 3)
   uint64_t run[NOUT];
 #pragma unroll
   for (int c = 0; c < NOUT; ++c) run[c] = 0;
-  uint32_t dropped_w = 0, cand = 0;
+  uint32_t cand = 0;  // items that reached the label map
   for (uint32_t k = 0; k < ntile; ++k) {
     const int stage = k & 1;
     Rec* recs = s_rec + stage * kRecTile;
@@ -619,10 +605,7 @@ __global__ void __launch_bounds__(kBlock, ITEMS <= 2 ? 5 : ITEMS <= 4 ? 4 : 3)
       ra[j] = r.a;
       rb[j] = r.b;
       rw[j] = r.w;
-      if (r.w < p.wmin || r.w > p.wmax) {
-        dropped_w += (r.w > p.wmax) ? 1u : 0u;
-        continue;
-      }
+      if (r.w < p.wmin || r.w > p.wmax) continue;
       ++cand;
       keep[j] = true;
     }
@@ -648,7 +631,7 @@ __global__ void __launch_bounds__(kBlock, ITEMS <= 2 ? 5 : ITEMS <= 4 ? 4 : 3)
       if (v != kInf64) red_min(&p.minval[x], v);
     }
   }
-  seg_pass_end<NOUT>(run, dropped_w, cand, p);
+  seg_pass_end<NOUT>(run, cand, p);
 }
 
 // ---------------------------------------------------------------------------
