@@ -278,12 +278,14 @@ __device__ __forceinline__ void tile_rank(const uint8_t (&cls)[ITEMS],
   const uint32_t lt = lanemask_lt();
 #pragma unroll
   for (int j = 0; j < ITEMS; ++j) {
+    uint32_t mine = 0;  // the ballot of this item's class
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
       const uint32_t b = __ballot_sync(kFull, cls[j] == c);
-      if (cls[j] == c) offs[j] = __popc(b & lt);
+      if (cls[j] == c) mine = b;
       if (lane == 0) smem[c * ROWS + j * WARPS + warp] = __popc(b);
     }
+    offs[j] = __popc(mine & lt);
   }
   __syncthreads();
   // exclusive scan of each class row-list, one warp per class
