@@ -316,7 +316,10 @@ kamsta_status solve_cgraph_host(Algo algo, const kamsta_cgraph* g, kamsta_cfg c,
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(dfirst, g->chunk_first, sizeof(kamsta_wedge) * g->num_chunks,
                         cudaMemcpyHostToDevice, cp);
-  if (e != cudaSuccess) return cuda_status(e, "cudaMemcpyAsync(H2D)");
+  if (e != cudaSuccess) {
+    cudaStreamSynchronize(cp);  // no copy from the caller's memory outlives the call
+    return cuda_status(e, "cudaMemcpyAsync(H2D)");
+  }
   const uint64_t nch = g->num_chunks, C = g->chunk_edges;
   for (int k = 0; k < kInputPieces; ++k) {
     const uint64_t c0 = nch * k / kInputPieces, c1 = nch * (k + 1) / kInputPieces;
