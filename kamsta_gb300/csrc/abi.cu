@@ -117,13 +117,14 @@ kamsta_status solve_host(Algo algo, const kamsta_wedge* edges, uint64_t m, uint3
   for (int k = 0; k < kInputPieces; ++k) {
     const uint64_t b = std::min<uint64_t>(m, k * per), en = std::min<uint64_t>(m, b + per);
     io.piece_end[k] = en;
-    if (en > b) {
+    if (en > b)
       e = cudaMemcpyAsync(din + b, edges + b, (en - b) * sizeof(kamsta_wedge),
                           cudaMemcpyHostToDevice, ctx->aux);
-      if (e != cudaSuccess) return cuda_status(e, "cudaMemcpyAsync(H2D)");
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->piece_ev[k], ctx->aux);
+    if (e != cudaSuccess) {
+      cudaStreamSynchronize(ctx->aux);  // no copy from the caller's memory outlives the call
+      return cuda_status(e, "cudaMemcpyAsync(H2D)");
     }
-    e = cudaEventRecord(ctx->piece_ev[k], ctx->aux);
-    if (e != cudaSuccess) return cuda_status(e, "cudaEventRecord");
   }
   SolveOut so;
   s = solve_device(ctx, algo, din, m, n, c, dout, &so, stats, ctx->stream, nullptr, &io);
@@ -136,7 +137,10 @@ kamsta_status solve_host(Algo algo, const kamsta_wedge* edges, uint64_t m, uint3
     e = cudaMemcpyAsync(out + io.early, dout + io.early,
                         (so.count - io.early) * sizeof(kamsta_wedge), cudaMemcpyDeviceToHost,
                         ctx->stream);
-    if (e != cudaSuccess) return cuda_status(e, "cudaMemcpyAsync(D2H)");
+    if (e != cudaSuccess) {
+      cudaStreamSynchronize(ctx->aux);
+      return cuda_status(e, "cudaMemcpyAsync(D2H)");
+    }
   }
   e = cudaStreamSynchronize(ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->aux);
@@ -373,7 +377,10 @@ kamsta_status solve_cgraph_host(Algo algo, const kamsta_cgraph* g, kamsta_cfg c,
   if (so.count > io.early) {
     e = cudaMemcpyAsync(out + io.early, dout + io.early,
                         (so.count - io.early) * sizeof(kamsta_wedge), cudaMemcpyDeviceToHost, st);
-    if (e != cudaSuccess) return cuda_status(e, "cudaMemcpyAsync(D2H)");
+    if (e != cudaSuccess) {
+      cudaStreamSynchronize(cp);
+      return cuda_status(e, "cudaMemcpyAsync(D2H)");
+    }
   }
   e = cudaStreamSynchronize(st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(cp);
