@@ -88,6 +88,16 @@ __device__ __forceinline__ uint64_t ld_weak(const uint64_t* p) {
   return v;
 }
 
+// Weak (L1-cacheable) read of a parent entry during pointer jumping.  Parent
+// entries only ever move to ancestors and root entries do not change within
+// the walk kernel, so a stale value is still an ancestor: the walk stays
+// correct and only may take an extra step.
+__device__ __forceinline__ uint32_t ld_weak_u32(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.weak.global.ca.u32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
+}
+
 // SplitMix64's output function (Steele, Lea, Flood 2014): the counter-based
 // hash behind weight sampling and the seeded graph generators.
 __host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {

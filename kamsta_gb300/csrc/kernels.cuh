@@ -1048,7 +1048,7 @@ __global__ void k_jump_label(uint32_t n, uint32_t* parent, uint32_t* __restrict_
     for (int k = 0; k < kIlp; ++k) {
       const uint64_t v = base + k * stride;
       x[k] = static_cast<uint32_t>(v);
-      p[k] = v < n ? ld_relaxed(parent + v) : kRootTagNone;
+      p[k] = v < n ? ld_weak_u32(parent + v) : kRootTagNone;
       run[k] = !(p[k] & kRootTag);
       root[k] = x[k];
       lab[k] = run[k] ? kNone : decode(p[k]);
@@ -1058,7 +1058,7 @@ __global__ void k_jump_label(uint32_t n, uint32_t* parent, uint32_t* __restrict_
       bool any = false;
       uint32_t gp[kIlp];
 #pragma unroll
-      for (int k = 0; k < kIlp; ++k) gp[k] = run[k] ? ld_relaxed(parent + p[k]) : 0u;
+      for (int k = 0; k < kIlp; ++k) gp[k] = run[k] ? ld_weak_u32(parent + p[k]) : 0u;
 #pragma unroll
       for (int k = 0; k < kIlp; ++k) {
         if (!run[k]) continue;
@@ -1076,7 +1076,7 @@ __global__ void k_jump_label(uint32_t n, uint32_t* parent, uint32_t* __restrict_
 #pragma unroll
       for (int k = 0; k < kIlp; ++k) {
         if (!run[k]) continue;
-        p[k] = ld_relaxed(parent + x[k]);
+        p[k] = ld_weak_u32(parent + x[k]);
         if (p[k] & kRootTag) {  // x is the root
           root[k] = x[k];
           lab[k] = decode(p[k]);
