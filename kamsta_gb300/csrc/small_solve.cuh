@@ -189,15 +189,17 @@ __device__ void solve(const uint32_t* __restrict__ in, uint32_t md, uint32_t n,
     __syncthreads();
     // pointer jumping with path halving, then a read-only pass that fixes
     // pointers another thread's halving left one level short
+    // (weak, L1-cacheable reads: entries only move to ancestors and roots
+    // never change, so a stale entry is still an ancestor)
     for (uint32_t v = tid; v < nr; v += THREADS) {
-      uint32_t x = v, p = ld_relaxed(parent + x), steps = 0;
+      uint32_t x = v, p = ld_weak_u32(parent + x), steps = 0;
       if (p == x) continue;
       for (;;) {
-        const uint32_t gp = ld_relaxed(parent + p);
+        const uint32_t gp = ld_weak_u32(parent + p);
         if (gp == p) break;
         st_relaxed(parent + x, gp);
         x = gp;
-        p = ld_relaxed(parent + x);
+        p = ld_weak_u32(parent + x);
         if (++steps > 2 * kMaxN) {
           flag_err(kErrJump);
           break;
@@ -206,10 +208,10 @@ __device__ void solve(const uint32_t* __restrict__ in, uint32_t md, uint32_t n,
     }
     __syncthreads();
     for (uint32_t v = tid; v < nr; v += THREADS) {
-      uint32_t p = ld_relaxed(parent + v), steps = 0;
+      uint32_t p = ld_weak_u32(parent + v), steps = 0;
       if (p == v) continue;
       for (;;) {
-        const uint32_t gp = ld_relaxed(parent + p);
+        const uint32_t gp = ld_weak_u32(parent + p);
         if (gp == p || ++steps > 2 * kMaxN) break;
         p = gp;
       }
