@@ -410,7 +410,12 @@ kamsta_status kamsta_mst_boruvka_7bit_dev(kamsta_ctx* ctx, const kamsta_cgraph* 
                                           const kamsta_cfg* cfg, kamsta_wedge* d_out,
                                           uint64_t* out_count, kamsta_stats* stats,
                                           kamsta_stream stream);
-/* Same from host memory: only the compressed bytes cross to the device. */
+/* Same from host memory: only the compressed bytes cross to the device, in
+ * pieces that the device decodes as they land (keep the bytes in pinned
+ * memory for the link's full rate).  The chunk table is checked on the host
+ * first: byte offsets must never decrease and must end inside data_bytes
+ * (KAMSTA_E_INPUT otherwise); a chunk whose bytes do not hold exactly its
+ * values is KAMSTA_E_INPUT before the solve starts. */
 kamsta_status kamsta_mst_boruvka_7bit(const kamsta_cgraph* g, const kamsta_cfg* cfg,
                                       kamsta_wedge* out, uint64_t* out_count,
                                       kamsta_stats* stats);
